@@ -1,0 +1,461 @@
+"""Benchmark of the tube-segmentation hot path on GB300.
+
+Workload (default): the 256^3 synthetic vessel tree, 500 GVF iterations with
+16-bit (FP16) field storage and FP32 arithmetic.  One step is one pass of the
+hot path over the volume, with inputs resident in HBM:
+    blur (sigma 0.5) -> vector field -> small-radius TDF (r 1..3) ->
+    GVF (500 Jacobi iterations) -> GVF finish -> large-radius TDF (r 2.5..7)
+    -> combine -> candidate centerpoints (threshold, pyramid-order compaction,
+    cross-section filter, per-cube arg-max, vertex list).
+value = voxel-iterations of GVF per step (N * 500) / step time, in
+Gvoxel-iter/s: the metric of the workload, measured over the whole step.
+
+e2e: the same step driven through the C ABI from pinned HOST memory: the
+volume is copied host->device and the TDF, radius and vertex list device->host
+inside the timed region.
+
+Multi-GPU: the path does not shard here; --gpus N runs N independent
+replicas (one volume per GPU), value = sum over ranks.
+
+--impl reference: the CPU restatement of the reference's kernels (the oracle;
+the OpenCL reference cannot run on these machines) on all host cores, on a
+bounded sample of the same workload (full-size volume, GVF iterations reduced
+and extrapolated linearly).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tube-segmentation-framework_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np
+
+METRIC = "GVF Gvoxel-iters/s (FP16 vs FP32 store, TDF err<=1e-3), fwd+adjoint ms @256^3"
+UNIT = "Gvoxel-iter/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="tsf", choices=["tsf", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=500)
+    ap.add_argument("--storage", default="f16", choices=["f32", "f16", "bf16", "snorm16"])
+    ap.add_argument("--mu", type=float, default=0.05)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-gvf-iters", type=int, default=6)
+    return ap.parse_args()
+
+
+# workload parameters (config 1 of the benchmark: 256^3 vessel tree)
+PARAMS = dict(large_blur=0.5, fmax=0.2, vsign=1, rmin=1.0, rmax=7.0, rstep=0.5,
+              tdf_high=0.5, cube_size=4)
+
+
+def mem_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class Pipeline:
+    """Device buffers and workspaces for one volume; step() runs the hot path."""
+
+    def __init__(self, T, torch, shape, storage, iters, mu):
+        self.T, self.torch = T, torch
+        Z, Y, X = shape
+        self.shape, self.storage, self.iters, self.mu = shape, storage, iters, mu
+        dt = T.storage_dtype(storage)
+        dev = "cuda"
+        L = T.load()
+        st = T.STORAGE[storage]
+        self.vol = torch.empty(shape, dtype=torch.float32, device=dev)
+        self.blurred = torch.empty_like(self.vol)
+        self.f0 = torch.empty((3, Z, Y, X), dtype=dt, device=dev)
+        self.v = torch.empty_like(self.f0)
+        self.f4_small = torch.empty((Z, Y, X, 4), dtype=dt, device=dev)
+        self.field = torch.empty((Z, Y, X, 4), dtype=dt, device=dev)
+        self.Ts = torch.empty(shape, dtype=torch.float32, device=dev)
+        self.Rs = torch.empty_like(self.Ts)
+        self.Tl = torch.empty_like(self.Ts)
+        self.Rl = torch.empty_like(self.Ts)
+        self.gvf_ws = T.workspace(L.tsf_gvf_workspace_size(X, Y, Z, st))
+        self.cand_ws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
+        self.max_vertices = 1 << 16
+        self.verts = torch.zeros((self.max_vertices, 3), dtype=torch.int32, device=dev)
+        self.last = None
+
+    def gvf_only(self):
+        T = self.T
+        self.v.copy_(self.f0)
+        T.gvf(self.f0, self.mu, self.iters, self.storage, v=self.v, ws=self.gvf_ws)
+
+    def step(self, events=None):
+        T, P, s = self.T, PARAMS, self.storage
+        rec = (lambda name: events.append((name, self._ev()))) if events is not None else (lambda name: None)
+        rec("start")
+        T.blur(self.vol, P["large_blur"], out=self.blurred)
+        # small-radius pass on the un-diffused field of the unblurred volume (small-blur 0)
+        self._vf(self.vol, None, self.f4_small)
+        T._check(T.load().tsf_tdf_circle(T._ptr(self.f4_small), *self._xyz(), T.STORAGE[s], P["rmin"], 3.0, 0.5,
+                                         T._ptr(self.Ts), 0, T._ptr(self.Rs), T._stream()))
+        rec("tdf_small")
+        self._vf(self.blurred, self.f0, None)
+        rec("vector_field")
+        self.gvf_only()
+        rec("gvf")
+        T.gvf_finish(self.v, s, out=self.field)
+        T._check(T.load().tsf_tdf_circle(T._ptr(self.field), *self._xyz(), T.STORAGE[s], max(2.5, P["rmin"]),
+                                         P["rmax"], P["rstep"], T._ptr(self.Tl), 0, T._ptr(self.Rl), T._stream()))
+        T.tdf_combine(self.Ts, self.Rs, self.Tl, self.Rl)
+        rec("tdf_large")
+        self.last = self._candidates()
+        rec("candidates")
+
+    def _ev(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    def _xyz(self):
+        Z, Y, X = self.shape
+        return X, Y, Z
+
+    def _vf(self, src, planar, f4):
+        T = self.T
+        X, Y, Z = self._xyz()
+        T._check(T.load().tsf_vector_field(T._ptr(src), X, Y, Z, PARAMS["fmax"], PARAMS["vsign"],
+                                           T.STORAGE[self.storage], T._ptr(planar), T._ptr(f4), T._stream()))
+
+    def _candidates(self):
+        import ctypes as C
+        T = self.T
+        X, Y, Z = self._xyz()
+        nc, nv = C.c_int64(0), C.c_int64(0)
+        code = T.load().tsf_candidates(T._ptr(self.Tl), 0, T._ptr(self.Rl), T._ptr(self.field),
+                                       T.STORAGE[self.storage], X, Y, Z, PARAMS["tdf_high"], PARAMS["cube_size"],
+                                       T._ptr(self.verts), self.max_vertices, None, None, 0, C.byref(nc),
+                                       C.byref(nv), T._ptr(self.cand_ws), self.cand_ws.numel(), T._stream())
+        if code not in (0, 4):
+            T._check(code)
+        return {"status": code, "n_candidates": nc.value, "n_vertices": nv.value}
+
+
+def run_tsf(args, rank, world):
+    import torch
+    import synthetic
+    import tsf_gb300 as T
+
+    torch.cuda.set_device(rank % max(1, torch.cuda.device_count()))
+    dev_index = torch.cuda.current_device()
+    n = args.size
+    shape = (n, n, n)
+    vol = synthetic.vascular_tree(shape, seed=args.seed + rank)
+    host = torch.from_numpy(vol).pin_memory()
+    pipe = Pipeline(T, torch, shape, args.storage, args.iters, args.mu)
+    pipe.vol.copy_(host, non_blocking=True)
+    torch.cuda.synchronize()
+    N = n ** 3
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timed region --------------------------------------------
+    for _ in range(args.warmup):
+        pipe.step()
+    torch.cuda.synchronize()
+    barrier()
+    clocks = ClockSampler(dev_index)
+    clocks.start()
+    torch.cuda.synchronize()
+    l0 = T.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        pipe.step()
+    e1.record()
+    torch.cuda.synchronize()
+    launches = T.kernel_launches() - l0
+    barrier()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * (N * args.iters) / (ms * 1e-3) / 1e9
+
+    # ---- per-stage times (one instrumented step) ------------------------------------
+    evs = []
+    pipe.step(events=evs)
+    torch.cuda.synchronize()
+    stages = {}
+    for (a, ea), (b, eb) in zip(evs[:-1], evs[1:]):
+        stages[b] = round(ea.elapsed_time(eb), 4)
+
+    # ---- GVF kernel: average launch duration, both storage formats ------------------
+    def gvf_kernel_stats(storage, mu):
+        p = pipe if storage == args.storage else Pipeline(T, torch, shape, storage, args.iters, mu)
+        if p is not pipe:
+            p.vol.copy_(pipe.vol)
+            T.blur(p.vol, PARAMS["large_blur"], out=p.blurred)
+            p._vf(p.blurred, p.f0, None)
+        p.mu = mu
+        p.gvf_only()
+        torch.cuda.synchronize()
+        la = T.kernel_launches()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        reps = 2
+        a.record()
+        for _ in range(reps):
+            p.gvf_only()
+        b.record()
+        torch.cuda.synchronize()
+        nl = (T.kernel_launches() - la) / reps
+        gvf_ms = a.elapsed_time(b) / reps
+        p.mu = args.mu
+        return gvf_ms, nl
+
+    gvf_ms, gvf_launches = gvf_kernel_stats(args.storage, args.mu)
+    gvf_ms_mu01, _ = gvf_kernel_stats(args.storage, 0.1)
+    f32_ms, _ = gvf_kernel_stats("f32", args.mu)
+    s_bytes = 4 if args.storage == "f32" else 2
+    iters_per_launch = args.iters / gvf_launches
+    launch_s = gvf_ms * 1e-3 / gvf_launches
+    algo_bytes = 9 * s_bytes * N * iters_per_launch
+    peaks = mem_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = algo_bytes / launch_s / 1e9
+
+    # ---- e2e through the C ABI with host buffers --------------------------------------
+    out_T = torch.empty(shape, dtype=torch.float32).pin_memory()
+    out_R = torch.empty(shape, dtype=torch.float32).pin_memory()
+    out_V = torch.empty((pipe.max_vertices, 3), dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        pipe.vol.copy_(host, non_blocking=True)
+        pipe.step()
+        out_T.copy_(pipe.Tl, non_blocking=True)
+        out_R.copy_(pipe.Rl, non_blocking=True)
+        nv = min(pipe.last["n_vertices"], pipe.max_vertices)
+        if nv:
+            out_V[:nv].copy_(pipe.verts[:nv], non_blocking=True)
+        return nv
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    nvs = []
+    for _ in range(args.steps):
+        nvs.append(e2e_step())
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * (N * args.iters) / e2e_s / 1e9
+    h2d = N * 4
+    d2h = N * 4 * 2 + int(np.mean(nvs)) * 12
+
+    res = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 arithmetic, %s field storage" % args.storage, "data": "synthetic",
+        "config": {"workload": "vessel tree %d^3, GVF %d iterations, mu %.2f, %s storage, full hot path"
+                               % (n, args.iters, args.mu, args.storage),
+                   "volume": [n, n, n], "gvf_iterations": args.iters, "mu": args.mu,
+                   "storage": args.storage, "params": PARAMS,
+                   "l2": "inputs larger than L2 (GVF streams 3 x %.0f MB per iteration)" % (3 * N * s_bytes / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "stages_ms": stages,
+        "gvf": {"ms": round(gvf_ms, 3), "gvox_iter_s": round(N * args.iters / (gvf_ms * 1e-3) / 1e9, 2),
+                "launches": gvf_launches, "iterations_per_launch": iters_per_launch,
+                "gvox_iter_s_mu_0_1": round(N * args.iters / (gvf_ms_mu01 * 1e-3) / 1e9, 2),
+                "f32_store_gvox_iter_s": round(N * args.iters / (f32_ms * 1e-3) / 1e9, 2),
+                "speedup_vs_f32_store": round(f32_ms / gvf_ms, 3)},
+        "candidates": pipe.last,
+        "roofline": {"bound": "hbm", "kernel": "GVF iteration", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": "measured" if peaks else "fallback",
+                     "bytes_per_launch": algo_bytes, "traffic": None},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    traffic = _traffic_from_profile(args.storage)
+    if traffic:
+        res["roofline"]["traffic"] = traffic
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(args, vol)
+    return res
+
+
+def _traffic_from_profile(storage):
+    """DRAM bytes per GVF launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "gvf_traffic.json")
+    try:
+        d = json.load(open(p))
+        return d.get(storage)
+    except Exception:
+        return None
+
+
+def cpu_baseline(args, vol=None, reps=1):
+    """The oracle (CPU restatement of the reference kernels) on all host cores,
+    on the full-size volume with the GVF iterations reduced to
+    --cpu-gvf-iters and extrapolated linearly to the workload's count."""
+    import oracle as O
+    import synthetic
+    O.build()
+    if vol is None:
+        vol = synthetic.vascular_tree((args.size,) * 3, seed=args.seed)
+    n = args.size
+    N = n ** 3
+    P = PARAMS
+    cores = O.get_threads()
+    k = args.cpu_gvf_iters
+    t = {}
+    t0 = time.perf_counter()
+    b = O.blur(vol, P["large_blur"])
+    f_small = O.vector_field(vol, P["fmax"], P["vsign"], args.storage)
+    t["blur_vf_small"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Ts, Rs = O.tdf_circle(f_small, P["rmin"], 3.0, 0.5)
+    t["tdf_small"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f4 = O.vector_field(b, P["fmax"], P["vsign"], args.storage)
+    t["vector_field"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    v = O.gvf(f4, args.mu, k, args.storage)
+    t_gvf_k = time.perf_counter() - t0
+    t["gvf_extrapolated"] = t_gvf_k * args.iters / k
+    t0 = time.perf_counter()
+    field = O.gvf_finish(v, args.storage)
+    Tl, Rl = O.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"])
+    Tl, Rl = O.combine(Ts, Rs, Tl, Rl)
+    t["tdf_large"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    try:
+        O.centerpoints(Tl, Rl, field, P["tdf_high"], P["cube_size"])
+    except Exception:
+        pass
+    t["candidates"] = time.perf_counter() - t0
+    total = sum(t.values())
+    measured = total - t["gvf_extrapolated"] + t_gvf_k
+    return {"value": round(N * args.iters / total / 1e9, 5), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "full %d^3 volume and stages, GVF timed over %d of %d iterations and extrapolated "
+                      "linearly; %.1f s of CPU work measured" % (n, k, args.iters, measured),
+            "stage_s": {a: round(b_, 3) for a, b_ in t.items()}}
+
+
+def run_reference(args):
+    res = cpu_baseline(args)
+    line = {"metric": METRIC, "impl": "reference", "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": 1, "warmup": 0, "ms_per_step": round(args.size ** 3 * args.iters / res["value"] / 1e6, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 arithmetic, %s field storage" % args.storage, "data": "synthetic",
+            "config": {"workload": "vessel tree %d^3, GVF %d iterations, mu %.2f, %s storage, full hot path"
+                                   % (args.size, args.iters, args.mu, args.storage),
+                       "implementation": "CPU restatement of the reference kernels (OpenCL reference cannot "
+                                         "run: no OpenCL platform on these machines)"},
+            "cpu_baseline": res,
+            "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        torch.distributed.init_process_group("nccl")
+    res = run_tsf(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,218 @@
+/*
+ * tsf_c.h -- C ABI of libtsf_gb300, the GB300 (sm_103a) implementation of the
+ * Tube Segmentation Framework's data-parallel hot path: gradient vector flow
+ * (GVF), the fused Hessian / eigen-decomposition / circle-fitting tube
+ * detection filter (TDF), and candidate-centerpoint compaction.
+ *
+ * Conventions
+ *  - Every pointer argument named d_* is DEVICE memory on the current CUDA
+ *    device, allocated by the caller.  No entry point allocates memory that
+ *    the caller can see; scratch memory comes from a caller-provided workspace
+ *    whose size is returned by the matching *_workspace_size query.
+ *  - Volumes are X*Y*Z voxels, x fastest: index = x + X*(y + Y*z), the LPOS
+ *    layout of the reference (kernels.cl:9).
+ *  - "field4" buffers hold 4 interleaved components per voxel (x, y, z, w) in
+ *    the given storage format, like the reference's CL_RGBA images.  "planar"
+ *    buffers hold 3 consecutive planes of N = X*Y*Z values (x plane, y plane,
+ *    z plane).
+ *  - `stream` is a cudaStream_t (0 = legacy default stream).  Calls are
+ *    stream-ordered and asynchronous unless documented otherwise, and are
+ *    reentrant given distinct buffers and workspaces.
+ *  - Return value: TSF_OK or an error code; tsf_last_error_string() gives the
+ *    message of the calling thread's last failure.
+ *  - Minimum extent: 4 voxels per axis (the reference shrinks volumes to a
+ *    multiple of 4 per axis, tube-segmentation.cpp:1800-1828).
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the smistad/Tube-Segmentation-Framework source tree).  The reference's
+ * stage signatures take cl::Image3D / cl::Buffer objects and an OpenCL
+ * context, so they cannot be ABI-compatible; these functions take plain
+ * device pointers and sizes instead.
+ */
+#ifndef TSF_C_H
+#define TSF_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TSF_ABI_VERSION 1
+
+/* Status codes. */
+enum {
+    TSF_OK = 0,
+    TSF_ERR_INVALID_ARG = 1,   /* bad dimensions, parameters or null pointers   */
+    TSF_ERR_CUDA = 2,          /* a CUDA runtime call or kernel launch failed   */
+    TSF_ERR_WORKSPACE = 3,     /* workspace smaller than *_workspace_size()     */
+    TSF_ERR_COUNT_RANGE = 4,   /* candidate / vertex count outside the range
+                                  the reference accepts
+                                  (parallelCenterlineExtraction.cpp:842-844,
+                                  895-899)                                      */
+    TSF_ERR_NOT_CONVERGED = 5, /* an iteration cap was reached                  */
+    TSF_ERR_CAPACITY = 6       /* an output buffer is too small                 */
+};
+
+/* Storage formats of vector fields.  F32 and SNORM16 are the reference's
+ * 32-bit and 16-bit options (CL_FLOAT / CL_SNORM_INT16,
+ * tube-segmentation.cpp:417-423, gradientVectorFlow.cpp:1100-1106); F16 and
+ * BF16 are additional 16-bit formats.  Arithmetic is always FP32. */
+enum {
+    TSF_STORE_F32 = 0,
+    TSF_STORE_F16 = 1,
+    TSF_STORE_BF16 = 2,
+    TSF_STORE_SNORM16 = 3
+};
+
+/* Version of this ABI (TSF_ABI_VERSION). */
+int tsf_abi_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *tsf_last_error_string(void);
+
+/* Bytes per stored component for a storage format (4 or 2; 0 if invalid). */
+size_t tsf_storage_bytes(int storage);
+
+/* Number of CUDA kernels this library has launched in this process (all
+ * threads, all devices).  Lets a caller count the launches of a call. */
+unsigned long long tsf_kernel_launches(void);
+
+/* ---------------------------------------------------------------------------
+ * Input stage
+ * ------------------------------------------------------------------------- */
+
+/* Host helper: the normalised Gaussian blur mask of createBlurMask
+ * (tube-segmentation.cpp:188-211).  mask_out must hold 11*11*11 floats; the
+ * half width m (1..5) is written to *half_width. */
+int tsf_blur_mask(float sigma, float *mask_out, int *half_width);
+
+/* blurVolumeWithGaussian (kernels.cl:1017-1040, enqueued at
+ * tube-segmentation.cpp:244-300 and 536-590): dense (2m+1)^3 Gaussian with
+ * nearest clamp-to-edge reads.  d_in and d_out are float volumes and must not
+ * overlap. */
+int tsf_blur(const float *d_in, float *d_out, int X, int Y, int Z, float sigma, void *stream);
+
+/* createVectorField (kernels.cl:1042-1063, enqueued at
+ * tube-segmentation.cpp:301-443 and 603-730): F = vsign * grad(I) with the
+ * Fmax normalisation.  Writes the planar f0 (3N elements) to d_planar and/or
+ * the field4 image (4N elements, w = 1) to d_field4; either may be NULL. */
+int tsf_vector_field(const float *d_in, int X, int Y, int Z, float fmax, int vsign, int storage,
+                     void *d_planar, void *d_field4, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Gradient vector flow
+ * ------------------------------------------------------------------------- */
+
+/* Workspace bytes for tsf_gvf (one ping-pong copy of the planar field). */
+size_t tsf_gvf_workspace_size(int X, int Y, int Z, int storage);
+
+/* GVF Jacobi iterations: replaces runGVF / runFastGVF
+ * (gradientVectorFlow.cpp:1007-1172, 1448-1457) with the GVF3DIteration
+ * kernel (kernels.cl:1464-1493).  d_f0 is the planar initial field f0 (the
+ * data term, read only); d_v holds the planar start value on entry (normally
+ * a copy of f0, as GVF3DInit makes) and the result after exactly `iterations`
+ * iterations on return.  mu is the GVF regularisation constant.  Several
+ * iterations run per launch (temporal blocking); every iteration's result is
+ * still rounded to `storage`, so the result equals one-iteration-per-launch.
+ * Note: the reference's host loop returns the result of iterations - 1 when
+ * `iterations` is odd; the C++ layer (run()) reproduces that, this call does
+ * not. */
+int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
+            int storage, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* tsf_gvf with the kernel forced: mode 1 = one iteration per launch,
+ * mode 2 = temporal blocking wherever the iteration count allows, 0 = the
+ * default choice of tsf_gvf.  All modes give bit-identical results. */
+int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
+                 int storage, void *d_workspace, size_t workspace_bytes, int mode, void *stream);
+
+/* GVF3DFinish (kernels.cl:1506-1515): packs the planar field into a field4
+ * image with w = |v| (1 where |v| == 0). */
+int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int storage,
+                   void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Tube detection filter
+ * ------------------------------------------------------------------------- */
+
+/* circleFittingTDF (kernels.cl:1065-1157; driver runCircleFittingTDF,
+ * tubeDetectionFilters.cpp:57-73): per voxel the Hessian of the field, its
+ * eigen-decomposition and the circle-fitting radius sweep
+ * r = rmin, rmin+rstep, ... <= rmax with 32 trilinear samples per radius.
+ * The Hessian is normalised by w when rmax >= 4.  Writes the response to d_T
+ * (float, or uint16 unorm16 when tdf_unorm16 != 0, the reference's 16-bit
+ * mode) and the arg-max radius to d_R (float). */
+int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
+                   float rstep, void *d_T, int tdf_unorm16, float *d_R, void *stream);
+
+/* combine (kernels.cl:561-572, tube-segmentation.cpp:802-824): where the small
+ * TDF exceeds the large one, take it and its radius.  d_T_large / d_R_large
+ * are updated in place; T arrays are float or unorm16 per tdf_unorm16. */
+int tsf_tdf_combine(const void *d_T_small, const float *d_R_small, void *d_T_large,
+                    float *d_R_large, int64_t n, int tdf_unorm16, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Candidate centerpoints
+ * ------------------------------------------------------------------------- */
+
+/* Workspace bytes for tsf_candidates. */
+size_t tsf_candidates_workspace_size(int X, int Y, int Z);
+
+/* The front half of runNewCenterlineAlg (parallelCenterlineExtraction.cpp:
+ * 667-899): threshold (findCandidateCenterpoints, kernels.cl:1296-1307),
+ * compaction in histogram-pyramid order (kernels.cl:63-299, oul
+ * HistogramPyramid3D), the cross-section non-maximum filter
+ * (findCandidateCenterpoints2, kernels.cl:1309-1390), the per-cube arg-max
+ * (dd, kernels.cl:1260-1292) and a second compaction into the vertex list.
+ *
+ *  d_T          TDF (float or unorm16 per tdf_unorm16); d_R radius (float);
+ *  d_field4     the GVF result image (w = |v|);
+ *  d_vertices   int32 (x,y,z) triples, capacity max_vertices, written in the
+ *               pyramid's order (x, z, y bit-interleaved key);
+ *  d_centerpoints  optional (may be NULL) int8 volume receiving the filtered
+ *               candidate mask (the reference's `centerpoints-only` output);
+ *  d_candidates optional (may be NULL) int32 triples receiving the candidate
+ *               list before filtering, capacity max_candidates;
+ *  n_candidates, n_vertices  host outputs.
+ * Synchronises `stream` twice (the counts are needed on the host, as the
+ * reference's getSum() calls are).  Returns TSF_ERR_COUNT_RANGE, with the
+ * counts still written, when the candidate count is not in (0, N/2] or the
+ * vertex count is not in [8, 16384), the reference's sanity checks. */
+int tsf_candidates(const void *d_T, int tdf_unorm16, const float *d_R, const void *d_field4,
+                   int storage, int X, int Y, int Z, float tdf_high, int cube_size,
+                   int32_t *d_vertices, int64_t max_vertices, int8_t *d_centerpoints,
+                   int32_t *d_candidates, int64_t max_candidates, int64_t *n_candidates,
+                   int64_t *n_vertices, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Workspace bytes for tsf_compact_mask. */
+size_t tsf_compact_workspace_size(int X, int Y, int Z);
+
+/* The histogram-pyramid enumeration alone (createPositions3D,
+ * kernels.cl:279-299): positions of the voxels with d_mask[i] != 0, ordered
+ * by the pyramid traversal.  Synchronises `stream`. */
+int tsf_compact_mask(const int8_t *d_mask, int X, int Y, int Z, int32_t *d_positions,
+                     int64_t max_positions, int64_t *count, void *d_workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Multigrid GVF
+ * ------------------------------------------------------------------------- */
+
+/* Workspace bytes for tsf_gvf_fmg. */
+size_t tsf_gvf_fmg_workspace_size(int X, int Y, int Z, int storage);
+
+/* runFMGGVF (gradientVectorFlow.cpp:729-1005; kernels.cl:1775-2061): full
+ * multigrid with v0 = 1, v1 = 2, v2 = 2, three levels, `iterations` FMG cycles
+ * per component.  d_field4_in is the vector field image (createVectorField
+ * output); d_field4_out receives (vx, vy, vz, |v|).  All intermediate images
+ * are rounded to `storage`. */
+int tsf_gvf_fmg(const void *d_field4_in, void *d_field4_out, int X, int Y, int Z, float mu,
+                int iterations, int storage, void *d_workspace, size_t workspace_bytes,
+                void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TSF_C_H */

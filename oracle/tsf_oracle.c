@@ -1,0 +1,288 @@
+/*
+ * tsf_oracle.c -- CPU restatement of the Tube Segmentation Framework hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the parity checker; see tsf_oracle.h).  Parity
+ * against the reference's own outputs is UNPINNED: the reference is OpenCL and
+ * cannot run here, and it has no golden vectors.
+ *
+ * This file holds the precision-independent pieces (storage conversions, the
+ * sample-direction table, the blur mask, the histogram pyramid) and includes
+ * tsf_oracle_impl.h twice to instantiate the float and double kernels.
+ *
+ * Build: cc -O2 -std=c11 -fopenmp -ffp-contract=off -fPIC -shared (see Makefile).
+ * -ffp-contract=off is required: the float oracle must round every product and
+ * sum separately, exactly like the CUDA kernels (built with -fmad=false).
+ */
+#include "tsf_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 0;
+
+void orc_set_threads(int n) {
+    g_threads = n;
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#endif
+}
+
+int orc_get_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Storage conversions                                                       */
+/* ------------------------------------------------------------------------ */
+
+static inline uint32_t f2u(float x) { uint32_t u; memcpy(&u, &x, 4); return u; }
+static inline float u2f(uint32_t u) { float x; memcpy(&x, &u, 4); return x; }
+
+/* IEEE binary16, round to nearest even. */
+uint16_t orc_f32_to_f16_bits(float x) {
+    uint32_t u = f2u(x);
+    uint32_t sign = (u >> 16) & 0x8000u;
+    uint32_t a = u & 0x7fffffffu;
+    if (a > 0x7f800000u) return (uint16_t)(sign | 0x7e00u);       /* NaN */
+    if (a >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);      /* >= 65520 -> inf */
+    if (a >= 0x38800000u) {                                       /* normal half */
+        uint32_t h = (a - 0x38000000u) >> 13;                     /* rebias 127 -> 15 */
+        uint32_t rem = a & 0x1fffu;
+        if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+        return (uint16_t)(sign | h);
+    }
+    /* subnormal half: units of 2^-24 */
+    int e = (int)(a >> 23) - 127;
+    uint32_t m = (a & 0x7fffffu) | (a ? 0x800000u : 0u);
+    int s = -(e + 1);                     /* right shift that maps m to 2^-24 units */
+    if (a == 0 || s > 24) return (uint16_t)sign;
+    uint32_t h = m >> s;
+    uint32_t rem = m & ((1u << s) - 1u);
+    uint32_t half = 1u << (s - 1);
+    if (rem > half || (rem == half && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+}
+
+float orc_f16_bits_to_f32(uint16_t h) {
+    uint32_t sign = ((uint32_t)h & 0x8000u) << 16;
+    uint32_t e = (h >> 10) & 0x1fu;
+    uint32_t m = h & 0x3ffu;
+    if (e == 0x1fu) return u2f(sign | 0x7f800000u | (m << 13));
+    if (e == 0) {
+        /* subnormal: m * 2^-24, exact in float */
+        float v = (float)m * 5.9604644775390625e-08f;
+        return sign ? -v : v;
+    }
+    return u2f(sign | ((e + 112u) << 23) | (m << 13));
+}
+
+uint16_t orc_f32_to_bf16_bits(float x) {
+    uint32_t u = f2u(x);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+/* convert_short_sat_rte(x * 32767.0f): kernels_no_3d_write.cl:9-21 and the
+ * OpenCL 1.1 rule for writes to CL_SNORM_INT16 images. */
+int16_t orc_f32_to_snorm16(float x) {
+    float f = x * 32767.0f;
+    if (f != f) return 0;
+    float r = rintf(f);                   /* default rounding mode: nearest even */
+    if (r >= 32767.0f) return 32767;
+    if (r <= -32768.0f) return -32768;
+    return (int16_t)r;
+}
+
+float orc_snorm16_to_f32(int16_t s) {
+    float v = (float)s / 32767.0f;
+    return v < -1.0f ? -1.0f : v;
+}
+
+uint16_t orc_f32_to_unorm16(float x) {
+    float f = x * 65535.0f;
+    if (f != f) return 0;
+    float r = rintf(f);
+    if (r >= 65535.0f) return 65535;
+    if (r <= 0.0f) return 0;
+    return (uint16_t)r;
+}
+
+float orc_unorm16_to_f32(uint16_t u) { return (float)u / 65535.0f; }
+
+float orc_quantize(float x, int storage) {
+    switch (storage) {
+    case ORC_F16: return orc_f16_bits_to_f32(orc_f32_to_f16_bits(x));
+    case ORC_BF16: return u2f((uint32_t)orc_f32_to_bf16_bits(x) << 16);
+    case ORC_SNORM16: return orc_snorm16_to_f32(orc_f32_to_snorm16(x));
+    default: return x;
+    }
+}
+
+void orc_quantize_array(float *a, int64_t n, int storage) {
+    if (storage == ORC_F32) return;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) a[i] = orc_quantize(a[i], storage);
+}
+
+void orc_to_unorm16_array(const float *in, uint16_t *out, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) out[i] = orc_f32_to_unorm16(in[i]);
+}
+
+void orc_from_unorm16_array(const uint16_t *in, float *out, int64_t n) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) out[i] = orc_unorm16_to_f32(in[i]);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tables                                                                    */
+/* ------------------------------------------------------------------------ */
+
+void orc_circle_table(float cosv[32], float sinv[32]) {
+    char buf[64];
+    for (int j = 0; j < 32; j++) {
+        snprintf(buf, sizeof buf, "%.6g", cos((double)j));
+        cosv[j] = strtof(buf, NULL);
+        snprintf(buf, sizeof buf, "%.6g", sin((double)j));
+        sinv[j] = strtof(buf, NULL);
+    }
+}
+
+/* createBlurMask, tube-segmentation.cpp:188-211: half width m = ceil(sigma/0.5)
+ * clamped to [1,5]; weights exp(-(a^2+b^2+c^2)/(2 sigma^2)) normalised to sum 1.
+ * The exponential is evaluated in double (C exp) and rounded to float; the
+ * running sum is kept in float, as in the reference host code. */
+int orc_blur_mask(float sigma, float *mask) {
+    int m = (int)ceilf(sigma / 0.5f);
+    if (m < 1) m = 1;
+    if (m > 5) m = 5;
+    int S = 2 * m + 1;
+    float sum = 0.0f;
+    float two_s2 = (2.0f * sigma) * sigma;
+    for (int a = -m; a <= m; a++)
+        for (int b = -m; b <= m; b++)
+            for (int c = -m; c <= m; c++) {
+                float arg = -((float)(a * a + b * b + c * c) / two_s2);
+                double w = exp((double)arg);
+                sum = (float)((double)sum + w);
+                mask[(a + m) + (b + m) * S + (c + m) * S * S] = (float)w;
+            }
+    for (int i = 0; i < S * S * S; i++) mask[i] = mask[i] / sum;
+    return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Histogram pyramid (kernels.cl:63-299; oul::HistogramPyramid3D)            */
+/* ------------------------------------------------------------------------ */
+
+/* Child visiting order of one pyramid cell, cubeOffsets (kernels.cl:70-79). */
+static const int k_cube[8][3] = {
+    {0, 0, 0}, {1, 0, 0}, {0, 0, 1}, {1, 0, 1},
+    {0, 1, 0}, {1, 1, 0}, {0, 1, 1}, {1, 1, 1},
+};
+
+int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, int64_t cap) {
+    int hp = 8;
+    int mx = X > Y ? X : Y;
+    if (Z > mx) mx = Z;
+    while (hp < mx) hp *= 2;
+    int L = 0;
+    while ((1 << L) < hp) L++;          /* levels 0..L-1, level k has size hp>>k */
+
+    int32_t **lev = (int32_t **)calloc((size_t)L, sizeof(int32_t *));
+    /* level 0: the mask, zero outside the volume */
+    int64_t n0 = (int64_t)hp * hp * hp;
+    lev[0] = (int32_t *)calloc((size_t)n0, sizeof(int32_t));
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++)
+                lev[0][x + (int64_t)hp * (y + (int64_t)hp * z)] =
+                    mask[x + (int64_t)X * (y + (int64_t)Y * z)] != 0;
+    /* constructHPLevel3D: each cell = sum of its 8 children */
+    for (int k = 1; k < L; k++) {
+        int s = hp >> k, sp = hp >> (k - 1);
+        lev[k] = (int32_t *)calloc((size_t)s * s * s, sizeof(int32_t));
+        for (int z = 0; z < s; z++)
+            for (int y = 0; y < s; y++)
+                for (int x = 0; x < s; x++) {
+                    int32_t acc = 0;
+                    for (int c = 0; c < 8; c++) {
+                        int xx = 2 * x + k_cube[c][0], yy = 2 * y + k_cube[c][1],
+                            zz = 2 * z + k_cube[c][2];
+                        acc += lev[k - 1][xx + (int64_t)sp * (yy + (int64_t)sp * zz)];
+                    }
+                    lev[k][x + (int64_t)s * (y + (int64_t)s * z)] = acc;
+                }
+    }
+    int64_t sum = 0;
+    {
+        int s = hp >> (L - 1); /* == 2 */
+        for (int i = 0; i < s * s * s; i++) sum += lev[L - 1][i];
+    }
+    /* traverseHP3D / scanHPLevel3D for every target rank */
+    int64_t nout = sum < cap ? sum : cap;
+    for (int64_t t = 0; t < nout; t++) {
+        int cx = 0, cy = 0, cz = 0;
+        int64_t acc0 = 0;
+        for (int k = L - 1; k >= 0; k--) {
+            int s = hp >> k;
+            int64_t nb[8];
+            for (int c = 0; c < 8; c++) {
+                int xx = cx + k_cube[c][0], yy = cy + k_cube[c][1], zz = cz + k_cube[c][2];
+                nb[c] = (xx < s && yy < s && zz < s)
+                            ? lev[k][xx + (int64_t)s * (yy + (int64_t)s * zz)] : 0;
+            }
+            int64_t acc = acc0;
+            int idx = 0;
+            int64_t add = 0;
+            for (int c = 0; c < 7; c++) {
+                acc += nb[c];
+                if (acc <= t) { idx++; add += nb[c]; }
+            }
+            cx += k_cube[idx][0]; cy += k_cube[idx][1]; cz += k_cube[idx][2];
+            cx *= 2; cy *= 2; cz *= 2;
+            acc0 += add;
+        }
+        pos[3 * t + 0] = cx / 2;
+        pos[3 * t + 1] = cy / 2;
+        pos[3 * t + 2] = cz / 2;
+    }
+    for (int k = 0; k < L; k++) free(lev[k]);
+    free(lev);
+    return sum;
+}
+
+void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) mask[i] = (T[i] < thr) ? 0 : 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Precision-templated kernels                                               */
+/* ------------------------------------------------------------------------ */
+
+#define REAL float
+#define SUFFIX _f32
+#define ORC_IS_F32 1
+#include "tsf_oracle_impl.h"
+#undef REAL
+#undef SUFFIX
+#undef ORC_IS_F32
+
+#define REAL double
+#define SUFFIX _f64
+#define ORC_IS_F32 0
+#include "tsf_oracle_impl.h"
+#undef REAL
+#undef SUFFIX
+#undef ORC_IS_F32

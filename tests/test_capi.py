@@ -1,0 +1,51 @@
+"""CPU tests of the C ABI boundary: the library loads without a GPU, exports
+every function include/tsf/tsf_c.h declares, and its host-side paths
+(workspace queries, the blur mask, argument validation) work without one."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+def test_library_exports_every_declared_symbol(tsf):
+    lib = tsf.load()
+    declared = tsf.declared_symbols()
+    assert len(declared) >= 15
+    missing = [s for s in declared if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_abi_version(tsf):
+    assert tsf.load().tsf_abi_version() == 1
+
+
+def test_storage_bytes(tsf):
+    L = tsf.load()
+    assert [L.tsf_storage_bytes(s) for s in range(5)] == [4, 2, 2, 2, 0]
+
+
+def test_workspace_queries(tsf):
+    L = tsf.load()
+    assert L.tsf_gvf_workspace_size(256, 256, 256, 1) == 3 * 256 ** 3 * 2
+    assert L.tsf_gvf_workspace_size(256, 256, 256, 0) == 3 * 256 ** 3 * 4
+    assert L.tsf_gvf_workspace_size(8, 8, 8, 9) == 0
+    n = 64 ** 3
+    assert L.tsf_candidates_workspace_size(64, 64, 64) >= 2 * n + 12 * (n // 2 + 1)
+    assert L.tsf_gvf_fmg_workspace_size(64, 64, 64, 1) > 3 * n * 2
+
+
+def test_blur_mask_matches_oracle(tsf, oracle):
+    for sigma in (0.5, 1.0, 1.7, 3.0):
+        m, mask = tsf.blur_mask(sigma)
+        om, omask = oracle.blur_mask(sigma)
+        assert m == om and np.array_equal(mask, omask)
+
+
+def test_argument_validation_without_gpu(tsf):
+    L = tsf.load()
+    # extents below 4 are rejected before any device call
+    assert L.tsf_blur(None, None, 2, 8, 8, C.c_float(1.0), None) == 1
+    assert b"extents" in L.tsf_last_error_string()
+    assert L.tsf_gvf(None, None, 8, 8, 8, C.c_float(0.1), 5, 7, None, 0, None) == 1
+    assert L.tsf_gvf(C.c_void_p(16), C.c_void_p(16), 8, 8, 8, C.c_float(0.1), 5, 0, None, 0, None) == 3
+    assert L.tsf_blur_mask(C.c_float(1.0), None, None) == 1

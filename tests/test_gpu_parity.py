@@ -1,0 +1,227 @@
+"""GPU parity: libtsf_gb300 (through its C ABI) against the oracle.
+
+The float oracle evaluates every expression in the kernels' order with
+separately rounded products and sums, and both sides use IEEE division and
+square root, so the expected result is bit-identical: the tests assert exact
+equality (tolerance 0).  The spec bar for FP32 fields is 1e-4 maximum
+relative error; exactness is stronger.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STORAGES = ["f32", "f16", "bf16", "snorm16"]
+
+
+@pytest.fixture(scope="module")
+def torch_dev():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+def _vol(synth, shape, seed):
+    return synth.vascular_tree(shape, seed=seed)
+
+
+def _np_stored(t, storage):
+    """device tensor of stored values -> float32 numpy, using the oracle's rules."""
+    import oracle as O
+    a = t.detach().cpu()
+    if storage == "snorm16":
+        s = a.numpy().astype(np.float32)
+        return np.maximum(np.float32(-1.0), s / np.float32(32767.0)).astype(np.float32)
+    return a.float().numpy()
+
+
+def _u16(t):
+    return t.cpu().numpy().view(np.uint16)
+
+
+@pytest.mark.parametrize("sigma", [0.5, 1.0, 2.5])
+def test_blur_bitexact(torch_dev, tsf, oracle, synth, sigma):
+    torch = torch_dev
+    vol = _vol(synth, (20, 24, 36), 1)
+    m, mask = tsf.blur_mask(sigma)
+    om, omask = oracle.blur_mask(sigma)
+    assert m == om and np.array_equal(mask, omask)
+    out = tsf.blur(torch.from_numpy(vol).cuda(), sigma)
+    assert np.array_equal(out.cpu().numpy(), oracle.blur(vol, sigma))
+
+
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("vsign", [1, -1])
+def test_vector_field_bitexact(torch_dev, tsf, oracle, synth, storage, vsign):
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, (24, 20, 28), 2), 1.0)
+    p, f4 = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, vsign, storage, planar=True, field4=True)
+    ref = oracle.vector_field(vol, 0.2, vsign, storage)
+    assert np.array_equal(_np_stored(f4, storage), ref)
+    assert np.array_equal(_np_stored(p, storage), np.moveaxis(ref[..., :3], -1, 0))
+
+
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("mu,iters", [(0.05, 17), (0.1, 8)])
+def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters):
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, (21, 26, 33), 4), 0.5)
+    ref4 = oracle.vector_field(vol, 0.2, 1, storage)
+    p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
+    v = tsf.gvf(p, mu, iters, storage)
+    ov = oracle.gvf(ref4, mu, iters, storage)
+    assert np.array_equal(_np_stored(v, storage), ov)
+    # the finish pass
+    f4 = tsf.gvf_finish(v, storage)
+    assert np.array_equal(_np_stored(f4, storage), oracle.gvf_finish(ov, storage))
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_gvf_modes_identical(torch_dev, tsf, synth, oracle, storage):
+    """One iteration per launch and temporal blocking give the same bits."""
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, (40, 36, 44), 5), 0.5)
+    p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
+    a = tsf.gvf(p, 0.05, 23, storage, mode=1)
+    b = tsf.gvf(p, 0.05, 23, storage, mode=2)
+    assert torch.equal(a, b)
+
+
+def test_gvf_minimum_extent(torch_dev, tsf, oracle):
+    torch = torch_dev
+    rng = np.random.default_rng(0)
+    vol = rng.random((4, 4, 4), dtype=np.float32)
+    ref4 = oracle.vector_field(vol, 0.2, 1, "f32")
+    p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, "f32")
+    v = tsf.gvf(p, 0.05, 5, "f32")
+    assert np.array_equal(v.cpu().numpy(), oracle.gvf(ref4, 0.05, 5, "f32"))
+
+
+def _field(oracle, synth, shape, seed, storage, iters=30, mu=0.05):
+    vol = oracle.blur(_vol(synth, shape, seed), 0.5)
+    f4 = oracle.vector_field(vol, 0.2, 1, storage)
+    v = oracle.gvf(f4, mu, iters, storage)
+    return oracle.gvf_finish(v, storage), f4
+
+
+def _to_device_field4(torch, field4, storage):
+    """oracle float field4 (already stored-exact) -> device tensor of the storage dtype."""
+    if storage == "f32":
+        return torch.from_numpy(field4.astype(np.float32)).cuda()
+    if storage == "f16":
+        return torch.from_numpy(field4.astype(np.float16)).cuda()
+    if storage == "bf16":
+        return torch.from_numpy(field4.astype(np.float32)).to(torch.bfloat16).cuda()
+    s = np.rint(field4.astype(np.float32) * np.float32(32767.0)).clip(-32768, 32767).astype(np.int16)
+    return torch.from_numpy(s).cuda()
+
+
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)])
+@pytest.mark.parametrize("unorm", [False, True])
+def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm):
+    torch = torch_dev
+    field4, _ = _field(oracle, synth, (28, 30, 26), 6, storage)
+    d4 = _to_device_field4(torch, field4, storage)
+    assert np.array_equal(_np_stored(d4, storage), field4)
+    T, R = tsf.tdf_circle(d4, *rng_, storage=storage, unorm16=unorm)
+    oT, oR = oracle.tdf_circle(field4, *rng_)
+    if unorm:
+        assert np.array_equal(_u16(T), oracle.to_unorm16(oT))
+    else:
+        assert np.array_equal(T.cpu().numpy(), oT)
+    assert np.array_equal(R.cpu().numpy(), oR)
+
+
+@pytest.mark.parametrize("unorm", [False, True])
+def test_combine(torch_dev, tsf, oracle, unorm):
+    torch = torch_dev
+    rng = np.random.default_rng(1)
+    Ts, Tl = rng.random((2, 9, 10, 11), dtype=np.float32)
+    Rs, Rl = rng.random((2, 9, 10, 11), dtype=np.float32) * 7
+    eT, eR = oracle.combine(Ts, Rs, Tl, Rl)
+    if unorm:
+        us, ul = oracle.to_unorm16(Ts), oracle.to_unorm16(Tl)
+        dTs = torch.from_numpy(us.view(np.int16)).cuda()
+        dTl = torch.from_numpy(ul.view(np.int16).copy()).cuda()
+        dRl = torch.from_numpy(Rl.copy()).cuda()
+        tsf.tdf_combine(dTs, torch.from_numpy(Rs).cuda(), dTl, dRl, unorm16=True)
+        m = us > ul
+        assert np.array_equal(_u16(dTl), np.where(m, us, ul))
+        assert np.array_equal(dRl.cpu().numpy(), np.where(m, Rs, Rl))
+    else:
+        dTl = torch.from_numpy(Tl.copy()).cuda()
+        dRl = torch.from_numpy(Rl.copy()).cuda()
+        tsf.tdf_combine(torch.from_numpy(Ts).cuda(), torch.from_numpy(Rs).cuda(), dTl, dRl)
+        assert np.array_equal(dTl.cpu().numpy(), eT)
+        assert np.array_equal(dRl.cpu().numpy(), eR)
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (13, 17, 30), (40, 9, 21), (64, 64, 64)])
+def test_compaction_order(torch_dev, tsf, oracle, shape):
+    """Ballot + scan compaction reproduces the pyramid enumeration exactly."""
+    torch = torch_dev
+    rng = np.random.default_rng(7)
+    m = (rng.random(shape) < 0.07).astype(np.int8)
+    pos = tsf.compact_mask(torch.from_numpy(m).cuda())
+    assert np.array_equal(pos.cpu().numpy(), oracle.hp_compact(m))
+
+
+def test_compaction_empty_and_full(torch_dev, tsf, oracle):
+    torch = torch_dev
+    z = np.zeros((12, 8, 16), np.int8)
+    assert tsf.compact_mask(torch.from_numpy(z).cuda()).shape[0] == 0
+    o = np.ones((12, 8, 16), np.int8)
+    assert np.array_equal(tsf.compact_mask(torch.from_numpy(o).cuda()).cpu().numpy(), oracle.hp_compact(o))
+
+
+@pytest.mark.parametrize("storage,unorm", [("f32", False), ("snorm16", True), ("f16", False)])
+def test_candidates_bitexact(torch_dev, tsf, oracle, synth, storage, unorm):
+    torch = torch_dev
+    field4, _ = _field(oracle, synth, (48, 48, 48), 8, storage, iters=40)
+    oT, oR = oracle.tdf_circle(field4, 1.0, 7.0, 0.5)
+    T_used = oracle.from_unorm16(oracle.to_unorm16(oT)) if unorm else oT
+    ref = oracle.centerpoints(T_used, oR, field4, tdf_high=0.3, cube_size=3)
+    d4 = _to_device_field4(torch, field4, storage)
+    if unorm:
+        dT = torch.from_numpy(oracle.to_unorm16(oT).view(np.int16)).cuda()
+    else:
+        dT = torch.from_numpy(oT).cuda()
+    out = tsf.candidates(dT, torch.from_numpy(oR).cuda(), d4, storage, 0.3, 3, unorm16=unorm,
+                         want_centerpoints=True, want_candidates=True, raise_on_range=False)
+    assert out["n_candidates"] == len(ref["candidates"])
+    assert np.array_equal(out["candidates"].cpu().numpy(), ref["candidates"])
+    assert np.array_equal(out["centerpoints"].cpu().numpy(), ref["mask2"])
+    assert out["n_vertices"] == len(ref["vertices"])
+    assert np.array_equal(out["vertices"].cpu().numpy(), ref["vertices"])
+
+
+def test_candidates_count_range_error(torch_dev, tsf, oracle, synth):
+    torch = torch_dev
+    field4, _ = _field(oracle, synth, (16, 16, 16), 9, "f32", iters=4)
+    T = torch.zeros((16, 16, 16), dtype=torch.float32, device="cuda")
+    R = torch.ones_like(T)
+    with pytest.raises(tsf.TSFError, match="TSF_ERR_COUNT_RANGE"):
+        tsf.candidates(T, R, _to_device_field4(torch, field4, "f32"), "f32", 0.5, 4)
+
+
+@pytest.mark.parametrize("storage", ["f32", "snorm16", "f16"])
+@pytest.mark.parametrize("shape", [(32, 32, 32), (28, 32, 36)])
+def test_fmg_bitexact(torch_dev, tsf, oracle, synth, storage, shape):
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, shape, 10), 0.5)
+    f4 = oracle.vector_field(vol, 0.2, 1, storage)
+    ref = oracle.fmg_gvf(f4, 0.2, 2, storage)
+    out = tsf.gvf_fmg(_to_device_field4(torch, f4, storage), 0.2, 2, storage)
+    assert np.array_equal(_np_stored(out, storage), ref)
+
+
+def test_invalid_arguments(torch_dev, tsf):
+    torch = torch_dev
+    v = torch.zeros((3, 3, 3), device="cuda")
+    with pytest.raises(tsf.TSFError, match="TSF_ERR_INVALID_ARG"):
+        tsf.blur(v, 1.0)
+    f0 = torch.zeros((3, 8, 8, 8), device="cuda")
+    with pytest.raises(tsf.TSFError, match="TSF_ERR_WORKSPACE"):
+        tsf.gvf(f0, 0.05, 3, "f32", ws=torch.zeros(16, dtype=torch.uint8, device="cuda"))

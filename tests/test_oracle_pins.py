@@ -1,0 +1,172 @@
+"""CPU tests: pin the oracle.
+
+The reference publishes no golden vectors for GVF, TDF, eigen or the pyramid,
+and it cannot run here (OpenCL), so the oracle is pinned by what can be
+checked independently: published algorithms against numpy, the pyramid order
+against its closed form, the format conversions against numpy/IEEE, the
+sample-direction table against the literals in the reference's kernels, and
+method-level invariants.
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+
+def test_eigen_matches_numpy(oracle):
+    rng = np.random.default_rng(0)
+    for f64 in (True, False):
+        tol = 1e-12 if f64 else 2e-5
+        for _ in range(500):
+            A = rng.normal(size=(3, 3))
+            A = (A + A.T) / 2
+            d, V = oracle.eig3(A, f64=f64)
+            w, U = np.linalg.eigh(A.astype(np.float64))
+            o = np.argsort(np.abs(w), kind="stable")
+            w, U = w[o], U[:, o]
+            assert np.max(np.abs(d - w)) < tol * 10
+            for k in range(3):
+                err = min(np.max(np.abs(V[:, k] - U[:, k])), np.max(np.abs(V[:, k] + U[:, k])))
+                gap = np.min(np.abs(np.delete(w, k) - w[k]))
+                if gap > 1e-3:
+                    assert err < tol * 100 / gap
+
+
+def test_eigen_known_answers(oracle):
+    d, V = oracle.eig3(np.diag([1.0, -3.0, 2.0]), f64=True)
+    assert np.allclose(d, [1.0, 2.0, -3.0])                 # ascending |lambda|
+    assert np.allclose(np.abs(V), [[1, 0, 0], [0, 0, 1], [0, 1, 0]])
+    d, V = oracle.eig3(np.zeros((3, 3)), f64=True)           # degenerate: identity basis
+    assert np.allclose(d, 0) and np.allclose(np.abs(V), np.eye(3))
+
+
+def _key(x, y, z, bits=12):
+    k = np.zeros(x.shape, np.int64)
+    for b in range(bits):
+        k |= (((x >> b) & 1) | (((z >> b) & 1) << 1) | (((y >> b) & 1) << 2)).astype(np.int64) << (3 * b)
+    return k
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (20, 24, 17), (3, 40, 9), (33, 5, 64)])
+def test_pyramid_order_is_key_sort(oracle, shape):
+    rng = np.random.default_rng(1)
+    m = (rng.random(shape) < 0.1).astype(np.int8)
+    pos = oracle.hp_compact(m)
+    z, y, x = np.nonzero(m)
+    o = np.argsort(_key(x, y, z), kind="stable")
+    assert np.array_equal(pos, np.stack([x[o], y[o], z[o]], 1))
+
+
+def test_float16_rounding_matches_numpy(oracle):
+    rng = np.random.default_rng(2)
+    a = (rng.normal(size=200000) * 10.0 ** rng.integers(-9, 6, size=200000)).astype(np.float32)
+    a = np.concatenate([a, np.float32([65504, 65519, 65520, 7e-8, 2.98e-8, 0.0, -0.0])])
+    assert np.array_equal(oracle.quantize(a, "f16"), a.astype(np.float16).astype(np.float32))
+
+
+def test_bfloat16_rounding_matches_torch(oracle):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    a = (rng.normal(size=100000) * 10.0 ** rng.integers(-20, 20, size=100000)).astype(np.float32)
+    ref = torch.from_numpy(a).to(torch.bfloat16).float().numpy()
+    assert np.array_equal(oracle.quantize(a, "bf16"), ref)
+
+
+def test_snorm16_and_unorm16_conversions(oracle):
+    # OpenCL 1.1: convert_short_sat_rte(v * 32767), read max(-1, s / 32767)
+    a = np.float32([-2.0, -1.0, -0.5, 0.0, 1.5 / 32767, 2.5 / 32767, 0.25, 1.0, 3.0])
+    s = np.clip(np.rint(a * np.float32(32767)), -32768, 32767)
+    expect = np.maximum(np.float32(-1), (s / 32767).astype(np.float32))
+    assert np.array_equal(oracle.quantize(a, "snorm16"), expect)
+    u = oracle.to_unorm16(np.float32([-1, 0, 0.5, 1, 2, 0.5 / 65535, 1.5 / 65535]))
+    assert list(u) == [0, 0, 32768, 65535, 65535, 0, 2]
+    assert oracle.from_unorm16(np.uint16([65535]))[0] == 1.0
+
+
+def test_circle_table_matches_reference_literals(oracle, reference_dir):
+    src = open(os.path.join(reference_dir, "kernels.cl")).read()
+    c = re.search(r"cosValues\[32\]\s*=\s*\{([^}]*)\}", src).group(1)
+    s = re.search(r"sinValues\[32\]\s*=\s*\{([^}]*)\}", src).group(1)
+    ref_c = np.float32([float(v.strip().rstrip("f")) for v in c.split(",")])
+    ref_s = np.float32([float(v.strip().rstrip("f")) for v in s.split(",")])
+    oc, os_ = oracle.circle_table()
+    assert np.array_equal(oc, ref_c) and np.array_equal(os_, ref_s)
+
+
+def test_blur_mask(oracle):
+    for sigma, m in [(0.5, 1), (1.0, 2), (2.2, 5), (9.0, 5), (0.1, 1)]:
+        mm, mask = oracle.blur_mask(sigma)
+        assert mm == m
+        S = 2 * m + 1
+        k = mask.reshape(S, S, S)
+        assert abs(float(mask.astype(np.float64).sum()) - 1.0) < 1e-5
+        assert np.array_equal(k, k[::-1]) and np.array_equal(k, k.transpose(2, 1, 0))
+
+
+def test_gvf_constant_field_is_fixed_point(oracle):
+    f = np.zeros((6, 7, 8, 4), np.float32)
+    f[..., 0], f[..., 1], f[..., 2], f[..., 3] = 0.25, -0.5, 0.125, 1.0
+    for storage in ("f32", "f16", "snorm16"):
+        v = oracle.gvf(oracle.quantize(f, storage).reshape(f.shape), 0.05, 7, storage)
+        assert np.array_equal(v[0], np.full((6, 7, 8), oracle.quantize(np.float32([0.25]), storage)[0]))
+
+
+def test_gvf_mirror_boundary(oracle, synth):
+    """Boundary voxels carry the update computed at index 2 / size-3
+    (kernels.cl:1472-1475): after an iteration plane 0 equals plane 2."""
+    vol = oracle.blur(synth.vascular_tree((16, 18, 20), seed=1), 0.5)
+    v = oracle.gvf(oracle.vector_field(vol, 0.2, 1, "f32"), 0.05, 3, "f32")
+    assert np.array_equal(v[:, 0], v[:, 2]) and np.array_equal(v[:, -1], v[:, -3])
+    assert np.array_equal(v[:, :, 0], v[:, :, 2]) and np.array_equal(v[:, :, :, -1], v[:, :, :, -3])
+
+
+def test_gvf_f64_and_f32_agree_when_stable(oracle, synth):
+    vol = synth.vascular_tree((24, 24, 24), seed=2)
+    f32 = oracle.gvf(oracle.vector_field(oracle.blur(vol, 0.5), 0.2, 1), 0.05, 50)
+    f64 = oracle.gvf(oracle.vector_field(oracle.blur(vol, 0.5, f64=True), 0.2, 1, f64=True), 0.05, 50,
+                     f64=True)
+    assert np.max(np.abs(f32 - f64)) < 1e-5
+
+
+def test_gvf_unstable_at_mu_0_1(oracle, synth):
+    """The explicit scheme needs 12 mu + |f0|^2 <= 2: at mu = 0.1 the
+    checkerboard mode grows where |f0| = 1 (documented in the design doc)."""
+    vol = synth.vascular_tree((32, 32, 32), seed=0)
+    f4 = oracle.vector_field(oracle.blur(vol, 0.5, f64=True), 0.2, 1, f64=True)
+    assert np.abs(oracle.gvf(f4, 0.1, 150, f64=True)).max() > 10.0
+    assert np.abs(oracle.gvf(f4, 0.08, 150, f64=True)).max() <= 1.0
+
+
+def test_tdf_detects_a_straight_tube(oracle):
+    """A bright straight cylinder of radius 3 along z: the TDF peaks on its
+    axis with a radius near 3."""
+    Z = Y = X = 32
+    z, y, x = np.mgrid[:Z, :Y, :X].astype(np.float32)
+    vol = ((x - 15.5) ** 2 + (y - 15.5) ** 2 <= 9.0).astype(np.float32)
+    f4 = oracle.vector_field(oracle.blur(vol, 1.0), 0.1, 1)
+    v = oracle.gvf(f4, 0.05, 100)
+    field = oracle.gvf_finish(v)
+    T, R = oracle.tdf_circle(field, 2.5, 6.0, 0.5)
+    sl = T[16]
+    iy, ix = np.unravel_index(np.argmax(sl), sl.shape)
+    assert abs(ix - 15.5) <= 1.5 and abs(iy - 15.5) <= 1.5
+    assert sl.max() > 0.5 and 2.0 <= R[16, iy, ix] <= 4.5
+
+
+def test_fmg_reduces_residual(oracle, synth):
+    vol = synth.vascular_tree((32, 32, 32), seed=3)
+    f4 = oracle.vector_field(oracle.blur(vol, 0.5, f64=True), 0.2, 1, f64=True)
+    a = oracle.fmg_gvf(f4, 0.2, 1, f64=True)
+    b = oracle.fmg_gvf(f4, 0.2, 3, f64=True)
+
+    def res(o):
+        v = np.moveaxis(o[..., :3], -1, 0)
+        f = np.moveaxis(f4[..., :3], -1, 0)
+        s = (f ** 2).sum(0)
+        lap = (np.roll(v, 1, 1) + np.roll(v, -1, 1) + np.roll(v, 1, 2) + np.roll(v, -1, 2) +
+               np.roll(v, 1, 3) + np.roll(v, -1, 3) - 6 * v)
+        r = 0.2 * lap - s * (v - f)
+        return np.abs(r[:, 2:-2, 2:-2, 2:-2]).mean()
+
+    assert res(b) < res(a)

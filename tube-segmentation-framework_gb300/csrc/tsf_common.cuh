@@ -1,0 +1,161 @@
+// tsf_common.cuh -- shared device helpers for libtsf_gb300 (sm_103a).
+//
+// Storage formats, their conversions, clamped index helpers and the error
+// plumbing of the C ABI.  All kernels are compiled with -fmad=false: every
+// product and sum is rounded separately, so a kernel and the float oracle that
+// evaluates the same expression in the same order agree bit for bit.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/tsf/tsf_c.h"
+
+namespace tsf {
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int check_cuda(cudaError_t e, const char *what);
+void count_launches(int n);   // process-wide kernel launch counter
+
+#define TSF_TRY_CUDA(expr)                                   \
+    do {                                                     \
+        cudaError_t e__ = (expr);                            \
+        if (e__ != cudaSuccess) return ::tsf::check_cuda(e__, #expr); \
+    } while (0)
+
+// Checks the launch(es) just issued and adds `n` to the launch counter.
+#define TSF_CHECK_LAUNCHES(name, n)                                         \
+    do {                                                                    \
+        cudaError_t e__ = cudaGetLastError();                               \
+        if (e__ != cudaSuccess) return ::tsf::check_cuda(e__, name);       \
+        ::tsf::count_launches(n);                                           \
+    } while (0)
+#define TSF_CHECK_LAUNCH(name) TSF_CHECK_LAUNCHES(name, 1)
+
+inline int check_dims(int X, int Y, int Z) {
+    if (X < 4 || Y < 4 || Z < 4) return fail(TSF_ERR_INVALID_ARG, "volume extents must be >= 4 per axis");
+    if ((int64_t)X * Y * Z > (int64_t)1 << 34) return fail(TSF_ERR_INVALID_ARG, "volume too large");
+    return TSF_OK;
+}
+
+inline bool valid_storage(int s) { return s >= TSF_STORE_F32 && s <= TSF_STORE_SNORM16; }
+
+// ---------------------------------------------------------------------------
+// storage formats
+// ---------------------------------------------------------------------------
+template <int ST> struct Store;
+
+template <> struct Store<TSF_STORE_F32> {
+    using T = float;
+    static __device__ __forceinline__ float load(T v) { return v; }
+    static __device__ __forceinline__ T store(float v) { return v; }
+};
+
+template <> struct Store<TSF_STORE_F16> {
+    using T = __half;
+    static __device__ __forceinline__ float load(T v) { return __half2float(v); }
+    static __device__ __forceinline__ T store(float v) { return __float2half_rn(v); }
+};
+
+template <> struct Store<TSF_STORE_BF16> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ float load(T v) { return __bfloat162float(v); }
+    static __device__ __forceinline__ T store(float v) { return __float2bfloat16_rn(v); }
+};
+
+// OpenCL CL_SNORM_INT16: write convert_short_sat_rte(v * 32767), read
+// max(-1, s / 32767) (kernels_no_3d_write.cl:9-21, OpenCL 1.1 section 8.3).
+template <> struct Store<TSF_STORE_SNORM16> {
+    using T = int16_t;
+    static __device__ __forceinline__ float load(T v) {
+        float f = __fdiv_rn((float)v, 32767.0f);
+        return fmaxf(-1.0f, f);
+    }
+    static __device__ __forceinline__ T store(float v) {
+        float f = __fmul_rn(v, 32767.0f);
+        int i = __float2int_rn(f);          // round to nearest even; NaN -> 0
+        i = max(-32768, min(32767, i));
+        return (int16_t)i;
+    }
+};
+
+// Value after a store and a load (what the next reader sees).
+template <int ST> __device__ __forceinline__ float quantize(float v) {
+    return Store<ST>::load(Store<ST>::store(v));
+}
+
+// OpenCL CL_UNORM_INT16 TDF (kernels.cl:11-13): convert_ushort_sat_rte(v*65535).
+__device__ __forceinline__ uint16_t to_unorm16(float v) {
+    float f = __fmul_rn(v, 65535.0f);
+    int i = __float2int_rn(f);
+    i = max(0, min(65535, i));
+    return (uint16_t)i;
+}
+__device__ __forceinline__ float from_unorm16(uint16_t u) { return __fdiv_rn((float)u, 65535.0f); }
+
+// Four stored components of a field4 voxel, loaded with one vector access.
+template <int ST> struct Vec4Load;
+
+template <> struct Vec4Load<TSF_STORE_F32> {
+    static __device__ __forceinline__ float4 load(const void *base, int64_t i) {
+        return __ldg(reinterpret_cast<const float4 *>(base) + i);
+    }
+};
+
+template <int ST> struct Vec4Load {
+    static __device__ __forceinline__ float4 load(const void *base, int64_t i) {
+        uint2 raw = __ldg(reinterpret_cast<const uint2 *>(base) + i);
+        using T = typename Store<ST>::T;
+        T c[4];
+        memcpy(c, &raw, 8);
+        return make_float4(Store<ST>::load(c[0]), Store<ST>::load(c[1]), Store<ST>::load(c[2]),
+                           Store<ST>::load(c[3]));
+    }
+};
+
+template <int ST> __device__ __forceinline__ void store4(void *base, int64_t i, float a, float b,
+                                                         float c, float d) {
+    using T = typename Store<ST>::T;
+    if constexpr (ST == TSF_STORE_F32) {
+        reinterpret_cast<float4 *>(base)[i] = make_float4(a, b, c, d);
+    } else {
+        T v[4] = {Store<ST>::store(a), Store<ST>::store(b), Store<ST>::store(c), Store<ST>::store(d)};
+        uint2 raw;
+        memcpy(&raw, v, 8);
+        reinterpret_cast<uint2 *>(base)[i] = raw;
+    }
+}
+
+__host__ __device__ __forceinline__ int clampi(int v, int n) { return v < 0 ? 0 : (v >= n ? n - 1 : v); }
+
+// Mirror boundary rule of GVF3DIteration (kernels.cl:1472-1475).
+__host__ __device__ __forceinline__ int mirror(int w, int n) {
+    int p = (w == 0) ? 2 : w;
+    return (p >= n - 1) ? n - 3 : p;
+}
+
+__host__ __device__ __forceinline__ int64_t lin(int x, int y, int z, int X, int Y) {
+    return (int64_t)x + (int64_t)X * ((int64_t)y + (int64_t)Y * (int64_t)z);
+}
+
+// Dispatch a runtime storage format to a template.
+#define TSF_DISPATCH_STORAGE(st, ST, ...)                                     \
+    switch (st) {                                                             \
+    case TSF_STORE_F32: { constexpr int ST = TSF_STORE_F32; __VA_ARGS__; } break;      \
+    case TSF_STORE_F16: { constexpr int ST = TSF_STORE_F16; __VA_ARGS__; } break;      \
+    case TSF_STORE_BF16: { constexpr int ST = TSF_STORE_BF16; __VA_ARGS__; } break;    \
+    case TSF_STORE_SNORM16: { constexpr int ST = TSF_STORE_SNORM16; __VA_ARGS__; } break; \
+    default: return fail(TSF_ERR_INVALID_ARG, "unknown storage format");      \
+    }
+
+inline size_t storage_bytes(int st) { return st == TSF_STORE_F32 ? 4 : (valid_storage(st) ? 2 : 0); }
+
+}  // namespace tsf

@@ -1,0 +1,265 @@
+"""Python binding of libtsf_gb300 (ctypes over include/tsf/tsf_c.h).
+
+Test and benchmark harness: torch supplies device memory and streams; every
+computation runs in the library's CUDA kernels.  There is no CPU fallback --
+loading fails loudly when the library is missing or no GPU is present.
+
+Arrays follow the library's layout: volumes are torch tensors indexed
+[z, y, x] (x fastest in memory); planar fields are [3, z, y, x]; field4 images
+are [z, y, x, 4]; storage dtypes are float32, float16, bfloat16 or int16
+(snorm16).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "lib", "libtsf_gb300.so")
+HEADER = os.path.join(ROOT, "include", "tsf", "tsf_c.h")
+
+TSF_OK = 0
+ERRORS = {1: "TSF_ERR_INVALID_ARG", 2: "TSF_ERR_CUDA", 3: "TSF_ERR_WORKSPACE",
+          4: "TSF_ERR_COUNT_RANGE", 5: "TSF_ERR_NOT_CONVERGED", 6: "TSF_ERR_CAPACITY"}
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "snorm16": 3}
+
+
+class TSFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (no GPU needed to load it)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"libtsf_gb300 not built: {path} missing (run __graft_entry__.build())")
+        _lib = C.CDLL(path)
+        _declare(_lib)
+    return _lib
+
+
+def declared_symbols(header: str = HEADER):
+    """Function names declared in the C header."""
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(tsf_[a-z0-9_]+)\s*\(", txt)))
+
+
+_p, _i, _i64, _f, _sz = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_size_t
+
+
+def _declare(L):
+    sig = {
+        "tsf_abi_version": (_i, []),
+        "tsf_last_error_string": (C.c_char_p, []),
+        "tsf_storage_bytes": (_sz, [_i]),
+        "tsf_kernel_launches": (C.c_ulonglong, []),
+        "tsf_blur_mask": (_i, [_f, _p, _p]),
+        "tsf_blur": (_i, [_p, _p, _i, _i, _i, _f, _p]),
+        "tsf_vector_field": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p]),
+        "tsf_gvf_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_gvf": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
+        "tsf_gvf_mode": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _i, _p]),
+        "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
+        "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
+        "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
+        "tsf_candidates_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_candidates": (_i, [_p, _i, _p, _p, _i, _i, _i, _i, _f, _i, _p, _i64, _p, _p, _i64,
+                                _p, _p, _p, _sz, _p]),
+        "tsf_compact_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_compact_mask": (_i, [_p, _i, _i, _i, _p, _i64, _p, _p, _sz, _p]),
+        "tsf_gvf_fmg_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+
+
+def kernel_launches() -> int:
+    return int(load().tsf_kernel_launches())
+
+
+def _check(code):
+    if code != TSF_OK:
+        raise TSFError(code, load().tsf_last_error_string().decode())
+
+
+# ---------------------------------------------------------------------------
+# torch helpers (imported lazily so that loading the library needs no torch)
+# ---------------------------------------------------------------------------
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("libtsf_gb300 computes on the GPU only; no CUDA device is available")
+    return torch
+
+
+def storage_dtype(storage: str):
+    import torch
+    return {"f32": torch.float32, "f16": torch.float16, "bf16": torch.bfloat16,
+            "snorm16": torch.int16}[storage]
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    assert t.is_cuda and t.is_contiguous(), "device tensors must be contiguous CUDA tensors"
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def _dims(vol):
+    Z, Y, X = vol.shape[:3]
+    return int(X), int(Y), int(Z)
+
+
+def workspace(nbytes: int):
+    torch = _torch()
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device="cuda")
+
+
+# ---------------------------------------------------------------------------
+# stage wrappers
+# ---------------------------------------------------------------------------
+
+def blur_mask(sigma: float):
+    import numpy as np
+    buf = np.zeros(11 ** 3, np.float32)
+    m = C.c_int(0)
+    _check(load().tsf_blur_mask(float(sigma), buf.ctypes.data_as(C.c_void_p), C.byref(m)))
+    return m.value, buf[: (2 * m.value + 1) ** 3].copy()
+
+
+def blur(vol, sigma: float, out=None, stream=None):
+    torch = _torch()
+    out = torch.empty_like(vol) if out is None else out
+    X, Y, Z = _dims(vol)
+    _check(load().tsf_blur(_ptr(vol), _ptr(out), X, Y, Z, float(sigma), _stream(stream)))
+    return out
+
+
+def vector_field(vol, fmax: float, vsign: int = 1, storage: str = "f32", planar=True, field4=False,
+                 stream=None):
+    torch = _torch()
+    X, Y, Z = _dims(vol)
+    dt = storage_dtype(storage)
+    p = torch.empty((3, Z, Y, X), dtype=dt, device=vol.device) if planar else None
+    f4 = torch.empty((Z, Y, X, 4), dtype=dt, device=vol.device) if field4 else None
+    _check(load().tsf_vector_field(_ptr(vol), X, Y, Z, float(fmax), int(vsign), STORAGE[storage],
+                                   _ptr(p), _ptr(f4), _stream(stream)))
+    return p, f4
+
+
+def gvf(f0, mu: float, iterations: int, storage: str = "f32", v=None, ws=None, mode: int = 0,
+        stream=None):
+    """Runs `iterations` Jacobi iterations; v (planar) defaults to a copy of f0."""
+    _, Z, Y, X = f0.shape
+    L = load()
+    v = f0.clone() if v is None else v
+    need = L.tsf_gvf_workspace_size(X, Y, Z, STORAGE[storage])
+    ws = workspace(need) if ws is None else ws
+    _check(L.tsf_gvf_mode(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
+                          _ptr(ws), ws.numel(), int(mode), _stream(stream)))
+    return v
+
+
+def gvf_finish(v, storage: str = "f32", out=None, stream=None):
+    torch = _torch()
+    _, Z, Y, X = v.shape
+    out = torch.empty((Z, Y, X, 4), dtype=v.dtype, device=v.device) if out is None else out
+    _check(load().tsf_gvf_finish(_ptr(v), _ptr(out), X, Y, Z, STORAGE[storage], _stream(stream)))
+    return out
+
+
+def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, stream=None):
+    torch = _torch()
+    Z, Y, X = field4.shape[:3]
+    T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
+    R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
+    _check(load().tsf_tdf_circle(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
+                                 float(rstep), _ptr(T), int(unorm16), _ptr(R), _stream(stream)))
+    return T, R
+
+
+def tdf_combine(Ts, Rs, Tl, Rl, unorm16: bool = False, stream=None):
+    _check(load().tsf_tdf_combine(_ptr(Ts), _ptr(Rs), _ptr(Tl), _ptr(Rl), Tl.numel(), int(unorm16),
+                                  _stream(stream)))
+    return Tl, Rl
+
+
+def candidates(T, R, field4, storage: str, tdf_high: float, cube_size: int, unorm16: bool = False,
+               max_vertices: int = 1 << 16, want_centerpoints=False, want_candidates=False, ws=None,
+               stream=None, raise_on_range=True):
+    """Returns dict(vertices [n,3] int32 (x,y,z), n_candidates, n_vertices,
+    centerpoints int8 volume or None, candidates [n,3] or None, status)."""
+    torch = _torch()
+    Z, Y, X = T.shape
+    L = load()
+    need = L.tsf_candidates_workspace_size(X, Y, Z)
+    ws = workspace(need) if ws is None else ws
+    verts = torch.zeros((max_vertices, 3), dtype=torch.int32, device=T.device)
+    cp = torch.zeros((Z, Y, X), dtype=torch.int8, device=T.device) if want_centerpoints else None
+    ncap = X * Y * Z // 2 + 1
+    cand = torch.zeros((ncap, 3), dtype=torch.int32, device=T.device) if want_candidates else None
+    nc, nv = C.c_int64(0), C.c_int64(0)
+    code = L.tsf_candidates(_ptr(T), int(unorm16), _ptr(R), _ptr(field4), STORAGE[storage], X, Y, Z,
+                            float(tdf_high), int(cube_size), _ptr(verts), max_vertices, _ptr(cp),
+                            _ptr(cand), ncap if want_candidates else 0, C.byref(nc), C.byref(nv),
+                            _ptr(ws), ws.numel(), _stream(stream))
+    if code != TSF_OK and (raise_on_range or code != 4):
+        _check(code)
+    nvv = min(nv.value, max_vertices)
+    return {"vertices": verts[:nvv], "n_candidates": nc.value, "n_vertices": nv.value,
+            "centerpoints": cp, "candidates": cand[: nc.value] if cand is not None else None,
+            "status": code}
+
+
+def compact_mask(mask, cap=None, stream=None):
+    torch = _torch()
+    Z, Y, X = mask.shape
+    L = load()
+    ws = workspace(L.tsf_compact_workspace_size(X, Y, Z))
+    cap = int(mask.numel()) if cap is None else cap
+    pos = torch.zeros((max(cap, 1), 3), dtype=torch.int32, device=mask.device)
+    cnt = C.c_int64(0)
+    _check(L.tsf_compact_mask(_ptr(mask), X, Y, Z, _ptr(pos), cap, C.byref(cnt), _ptr(ws), ws.numel(),
+                              _stream(stream)))
+    return pos[: cnt.value]
+
+
+def gvf_fmg(field4, mu: float, iterations: int, storage: str = "f32", ws=None, stream=None):
+    torch = _torch()
+    Z, Y, X = field4.shape[:3]
+    L = load()
+    need = L.tsf_gvf_fmg_workspace_size(X, Y, Z, STORAGE[storage])
+    ws = workspace(need) if ws is None else ws
+    out = torch.empty_like(field4)
+    _check(L.tsf_gvf_fmg(_ptr(field4), _ptr(out), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
+                         _ptr(ws), ws.numel(), _stream(stream)))
+    return out
+
+
+def to_float(t, storage: str):
+    """Stored values -> float32 (snorm16: max(-1, s/32767))."""
+    torch = _torch()
+    if storage == "snorm16":
+        return torch.clamp_min(t.to(torch.float32) / 32767.0, -1.0)
+    return t.to(torch.float32)
