@@ -60,6 +60,141 @@ __global__ void __launch_bounds__(256) gvf_plain_kernel(const typename Store<ST>
 }
 
 // ---------------------------------------------------------------------------
+// one iteration per launch, z-streaming, VX voxels per thread along x
+//
+// A warp covers 32*VX consecutive voxels of one row; each thread walks a chunk
+// of ZC planes keeping the planes z-1, z, z+1 of its VX columns in registers,
+// so every stored component of v is fetched from HBM once (as the "next"
+// plane); the y-neighbour rows come from L1 (the adjacent warps of the block
+// fetch them) and the x-neighbours from the neighbouring lanes by shuffles.
+// The mirror boundary rule is applied as: rows compute at mirror(y); the
+// vector holding x = 0 / X-1 copies the result of x = 2 / X-3; the thread that
+// computes plane 2 / Z-3 also writes plane 0 / Z-1 (chunks are >= 3 planes
+// and the last chunk is shifted to end at Z, so those pairs never straddle a
+// chunk).  Per voxel the arithmetic is exactly gvf_plain_kernel's.
+// ---------------------------------------------------------------------------
+template <int ST, int VX> struct VecIO;
+
+template <int ST> struct VecIO<ST, 4> {
+    using T = typename Store<ST>::T;
+    static __device__ __forceinline__ void load(const T *p, float o[4]) {
+        if constexpr (ST == TSF_STORE_F32) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+            o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+        } else {
+            const uint2 raw = __ldg(reinterpret_cast<const uint2 *>(p));
+            T c[4];
+            memcpy(c, &raw, 8);
+#pragma unroll
+            for (int i = 0; i < 4; i++) o[i] = Store<ST>::load(c[i]);
+        }
+    }
+    static __device__ __forceinline__ void store(T *p, const float o[4]) {
+        if constexpr (ST == TSF_STORE_F32) {
+            *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
+        } else {
+            T c[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) c[i] = Store<ST>::store(o[i]);
+            uint2 raw;
+            memcpy(&raw, c, 8);
+            *reinterpret_cast<uint2 *>(p) = raw;
+        }
+    }
+};
+
+template <int ST, int VX, int BY>
+__global__ void __launch_bounds__(32 * BY) gvf_stream_kernel(const typename Store<ST>::T *__restrict__ f,
+                                                             const typename Store<ST>::T *__restrict__ src,
+                                                             typename Store<ST>::T *__restrict__ dst,
+                                                             int X, int Y, int Z, float mu, int ZC) {
+    using T = typename Store<ST>::T;
+    using IO = VecIO<ST, VX>;
+    const int lane = threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    if (y >= Y) return;                              // whole warp
+    const int x0 = (blockIdx.x * 32 + lane) * VX;
+    const bool act = x0 < X;
+    const int z0 = min((int)blockIdx.z * ZC, Z - ZC);
+    const int z1 = z0 + ZC;
+    const int zs = max(z0, 1), ze = min(z1, Z - 1);
+    const int py = mirror(y, Y);
+    const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
+    const int64_t col = (int64_t)py * X + x0;       // offset of this vector within a plane (row py)
+    const int64_t ocol = (int64_t)y * X + x0;       // output row y
+    const unsigned full = 0xffffffffu;
+
+    float prv[3][VX], cur[3][VX], nxt[3][VX];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (act) {
+            IO::load(src + c * n + (int64_t)(zs - 1) * plane + col, prv[c]);
+            IO::load(src + c * n + (int64_t)zs * plane + col, cur[c]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < VX; i++) prv[c][i] = cur[c][i] = 0.0f;
+        }
+    }
+    for (int z = zs; z < ze; z++) {
+        const int64_t zo = (int64_t)z * plane;
+        float fv[3][VX], sqr[VX];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (act) IO::load(f + c * n + zo + col, fv[c]);
+            else {
+#pragma unroll
+                for (int i = 0; i < VX; i++) fv[c][i] = 0.0f;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < VX; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const T *sc = src + c * n + zo + col;
+            float yp[VX], ym[VX], res[VX];
+            if (act) {
+                IO::load(sc + plane, nxt[c]);
+                IO::load(sc + X, yp);
+                IO::load(sc - X, ym);
+            } else {
+#pragma unroll
+                for (int i = 0; i < VX; i++) nxt[c][i] = yp[i] = ym[i] = 0.0f;
+            }
+            float xl = __shfl_up_sync(full, cur[c][VX - 1], 1);
+            float xr = __shfl_down_sync(full, cur[c][0], 1);
+            if (lane == 0) xl = (act && x0 > 0) ? Store<ST>::load(sc[-1]) : 0.0f;
+            if (lane == 31) xr = (act && x0 + VX < X) ? Store<ST>::load(sc[VX]) : 0.0f;
+#pragma unroll
+            for (int i = 0; i < VX; i++) {
+                const float v = cur[c][i];
+                float lap = -6.0f * v;
+                lap = lap + (i == VX - 1 ? xr : cur[c][i + 1 < VX ? i + 1 : i]);
+                lap = lap + (i == 0 ? xl : cur[c][i > 0 ? i - 1 : 0]);
+                lap = lap + yp[i];
+                lap = lap + ym[i];
+                lap = lap + nxt[c][i];
+                lap = lap + prv[c][i];
+                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+                res[i] = quantize<ST>(v + upd);
+            }
+            if (x0 == 0) res[0] = res[2];
+            if (x0 + VX == X) res[VX - 1] = res[VX - 3];
+            if (act) {
+                T *dc = dst + c * n;
+                IO::store(dc + zo + ocol, res);
+                if (z == 2 && z0 == 0) IO::store(dc + ocol, res);
+                if (z == Z - 3 && z1 == Z) IO::store(dc + (int64_t)(Z - 1) * plane + ocol, res);
+            }
+#pragma unroll
+            for (int i = 0; i < VX; i++) {
+                prv[c][i] = cur[c][i];
+                cur[c][i] = nxt[c][i];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // GVF3DFinish: planar -> field4 with w = |v| (1 if 0)
 // ---------------------------------------------------------------------------
 template <int ST>
@@ -81,8 +216,21 @@ size_t gvf_workspace_size(int X, int Y, int Z, int st) {
     return (size_t)3 * (size_t)X * (size_t)Y * (size_t)Z * storage_bytes(st);
 }
 
+constexpr int kStreamVX = 4, kStreamBY = 8, kStreamZC = 16;
+
 static int launch_gvf_plain(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z,
                             float mu, cudaStream_t s) {
+    if (X % kStreamVX == 0 && Z >= 3) {
+        const int zc = Z < kStreamZC ? Z : kStreamZC;
+        dim3 b(32, kStreamBY), g((X / kStreamVX + 31) / 32, (Y + kStreamBY - 1) / kStreamBY, (Z + zc - 1) / zc);
+        TSF_DISPATCH_STORAGE(st, ST, {
+            using T = typename Store<ST>::T;
+            gvf_stream_kernel<ST, kStreamVX, kStreamBY><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst,
+                                                                        X, Y, Z, mu, zc);
+        });
+        TSF_CHECK_LAUNCH("gvf_stream_kernel");
+        return TSF_OK;
+    }
     dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
     TSF_DISPATCH_STORAGE(st, ST, {
         using T = typename Store<ST>::T;
