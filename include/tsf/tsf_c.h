@@ -128,6 +128,21 @@ int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
 int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                  int storage, void *d_workspace, size_t workspace_bytes, int mode, void *stream);
 
+/* tsf_gvf for callers that cannot allocate device memory.  No counterpart in
+ * the reference: it exists for hosts that can neither call cudaMalloc nor
+ * provide a workspace (plug-in hosts that own the device allocator,
+ * real-time pipelines that forbid device allocation once running).  Same
+ * arguments and result as tsf_gvf, without the workspace: the scratch is a
+ * fixed 96 MiB array in the library's device memory, held on every GPU that
+ * loads the library until the process exits.  Limit: 3 * X*Y*Z stored
+ * components must fit in 96 MiB (256^3 voxels in a 16-bit format, 8,388,608
+ * in FP32); larger volumes return TSF_ERR_CAPACITY.  The first call on a
+ * device looks up the array's address with that device current -- make it
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU race.  Allocates nothing. */
+int tsf_gvf_static(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
+                   int storage, void *stream);
+
 /* GVF3DFinish (kernels.cl:1506-1515): packs the planar field into a field4
  * image with w = |v| (1 where |v| == 0). */
 int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int storage,
