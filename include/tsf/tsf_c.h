@@ -83,6 +83,23 @@ unsigned long long tsf_kernel_launches(void);
  * Input stage
  * ------------------------------------------------------------------------- */
 
+/* Voxel types of raw input volumes (MET_UCHAR, MET_CHAR, MET_USHORT,
+ * MET_SHORT, MET_FLOAT in the reference's .mhd reader,
+ * tube-segmentation.cpp:1490-1536). */
+enum {
+    TSF_TYPE_UINT8 = 0,
+    TSF_TYPE_INT8 = 1,
+    TSF_TYPE_UINT16 = 2,
+    TSF_TYPE_INT16 = 3,
+    TSF_TYPE_FLOAT32 = 4
+};
+
+/* toFloat (kernels.cl:989-1015, enqueued at tube-segmentation.cpp:1833-1892):
+ * v = clamp(v, minimum, maximum); d_out = (v - minimum) / (maximum - minimum),
+ * for n voxels of the given TSF_TYPE_*. */
+int tsf_to_float(const void *d_in, int type, int64_t n, float minimum, float maximum, float *d_out,
+                 void *stream);
+
 /* Host helper: the normalised Gaussian blur mask of createBlurMask
  * (tube-segmentation.cpp:188-211).  mask_out must hold 11*11*11 floats; the
  * half width m (1..5) is written to *half_width. */

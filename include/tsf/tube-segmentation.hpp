@@ -1,0 +1,39 @@
+// tube-segmentation.hpp -- the library entry point of the Tube Segmentation
+// Framework API (reference tube-segmentation.hpp:47).
+//
+//   TSFOutput *run(std::string filename, paramList &parameters, std::string kernel_dir);
+//   TSFOutput *runSegmentation(...)   -- the same call under the name the
+//                                        benchmark description uses
+//
+// run() reads an .mhd/.raw volume, converts it to [0,1] floats, and runs the
+// GPU hot path of the `gpu` centerline method on the current CUDA device:
+// Gaussian blur, the vector field, the small-radius TDF on the un-diffused
+// field, GVF (Jacobi, or full multigrid with use-fmg-gvf), the large-radius
+// TDF and the combination of both, then the candidate stage (threshold,
+// compaction, cross-section filter, per-cube arg-max).  kernel_dir is
+// accepted and ignored (the kernels are compiled into the library).
+//
+// Results: the TDF always; with `tdf-only` nothing else.  With
+// `centerpoints-only` the centerline voxels are the filtered candidate mask,
+// exactly the reference's output for that option.  Otherwise the centerline
+// voxels mark the centerpoint vertices and getCenterpoints() lists them; the
+// linking of vertices into centerlines and the segmentation are not part of
+// this library (hasSegmentation() stays false).
+//
+// Exceptions follow the reference: SIPL::IOException for a missing file,
+// SIPL::SIPLException for a bad header, an unsupported type or option, or a
+// candidate / vertex count outside the accepted range.
+#ifndef TSF_TUBE_SEGMENTATION_HPP
+#define TSF_TUBE_SEGMENTATION_HPP
+
+#include <string>
+
+#include "tsf/SIPL/Exceptions.hpp"
+#include "tsf/SIPL/Types.hpp"
+#include "tsf/inputOutput.hpp"
+#include "tsf/parameters.hpp"
+
+TSFOutput *run(std::string filename, paramList &parameters, std::string kernel_dir);
+TSFOutput *runSegmentation(std::string filename, paramList &parameters, std::string kernel_dir);
+
+#endif

@@ -23,6 +23,7 @@ HOST = os.path.join(HERE, "host")
 BUILD = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIB_DIR, "libtsf_gb300.so")
+API_TESTS = os.path.join(LIB_DIR, "tsf_api_tests")
 INCLUDE = os.path.join(ROOT, "include")
 
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
@@ -31,7 +32,7 @@ CUDA_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "--expt-re
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE]
 
-CU_SOURCES = ["capi.cu", "vector_field.cu", "gvf.cu", "gvf_tb.cu", "tdf.cu", "candidates.cu", "fmg.cu", "noalloc.cu"]
+CU_SOURCES = ["capi.cu", "vector_field.cu", "gvf.cu", "gvf_tb.cu", "tdf.cu", "candidates.cu", "fmg.cu", "noalloc.cu", "input.cu"]
 
 
 def _cuda_lib_dir():
@@ -94,10 +95,15 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         for o in outs:
             if o.strip():
                 print(o)
+    cudadir = _cuda_lib_dir()
     if jobs or not os.path.exists(LIB):
-        cudadir = _cuda_lib_dir()
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs +
              ["-cudart", "shared", "-L", cudadir, "-Xlinker", "-rpath," + cudadir])
+    # C++ test driver of the drop-in API (tests/cpp/test_api.cpp)
+    src = os.path.join(ROOT, "tests", "cpp", "test_api.cpp")
+    if os.path.exists(src) and _newer([src, LIB] + deps, API_TESTS):
+        _run(["g++"] + CXX_FLAGS + [src, "-o", API_TESTS, "-L", LIB_DIR, "-ltsf_gb300",
+                                     "-Wl,-rpath," + LIB_DIR, "-L", cudadir, "-lcudart", "-Wl,-rpath," + cudadir])
     return LIB
 
 

@@ -103,94 +103,140 @@ template <int ST> struct VecIO<ST, 4> {
     }
 };
 
-template <int ST, int VX, int BY>
-__global__ void __launch_bounds__(32 * BY) gvf_stream_kernel(const typename Store<ST>::T *__restrict__ f,
-                                                             const typename Store<ST>::T *__restrict__ src,
-                                                             typename Store<ST>::T *__restrict__ dst,
-                                                             int X, int Y, int Z, float mu, int ZC) {
+template <int ST> struct VecIO<ST, 2> {
     using T = typename Store<ST>::T;
-    using IO = VecIO<ST, VX>;
+    static __device__ __forceinline__ void load(const T *p, float o[2]) {
+        if constexpr (ST == TSF_STORE_F32) {
+            const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+            o[0] = v.x; o[1] = v.y;
+        } else {
+            const unsigned raw = __ldg(reinterpret_cast<const unsigned *>(p));
+            T c[2];
+            memcpy(c, &raw, 4);
+            o[0] = Store<ST>::load(c[0]);
+            o[1] = Store<ST>::load(c[1]);
+        }
+    }
+    static __device__ __forceinline__ void store(T *p, const float o[2]) {
+        if constexpr (ST == TSF_STORE_F32) {
+            *reinterpret_cast<float2 *>(p) = make_float2(o[0], o[1]);
+        } else {
+            T c[2] = {Store<ST>::store(o[0]), Store<ST>::store(o[1])};
+            unsigned raw;
+            memcpy(&raw, c, 4);
+            *reinterpret_cast<unsigned *>(p) = raw;
+        }
+    }
+};
+
+// Eight bytes of stored components: 4 voxels of a 16-bit format or 2 of FP32.
+template <int ST> struct Packed8 {
+    using T = typename Store<ST>::T;
+    static constexpr int VX = 8 / (int)sizeof(T);
+    static __device__ __forceinline__ uint2 load(const T *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
+    static __device__ __forceinline__ void unpack(uint2 raw, float o[VX]) {
+        T c[VX];
+        memcpy(c, &raw, 8);
+#pragma unroll
+        for (int i = 0; i < VX; i++) o[i] = Store<ST>::load(c[i]);
+    }
+    static __device__ __forceinline__ void store(T *p, const float o[VX]) {
+        T c[VX];
+#pragma unroll
+        for (int i = 0; i < VX; i++) c[i] = Store<ST>::store(o[i]);
+        uint2 raw;
+        memcpy(&raw, c, 8);
+        *reinterpret_cast<uint2 *>(p) = raw;
+    }
+};
+
+// One thread = the VX voxels of one 8-byte vector of one row of one plane.
+// All loads of a thread are independent and issued together -- per component
+// the centre vector and its y+-1 and z+-1 neighbours, plus the f0 vectors --
+// and stay packed in registers until used, so a warp keeps 18 eight-byte
+// loads in flight at ~40 registers.  The neighbour vectors are other threads'
+// centre vectors, served by L1/L2, so HBM still sees each stored component
+// once.  x-neighbours come from the adjacent lanes by shuffles.  Mirror rule:
+// rows and planes are computed at mirror(y), mirror(z); the vector holding
+// x = 0 / X-1 copies the result of x = 2 / X-3 (needs VX >= 3, or the
+// neighbouring vector, see below).  Per voxel the arithmetic is exactly
+// gvf_plain_kernel's.
+template <int ST>
+__global__ void __launch_bounds__(256) gvf_vec_kernel(const typename Store<ST>::T *__restrict__ f,
+                                                      const typename Store<ST>::T *__restrict__ src,
+                                                      typename Store<ST>::T *__restrict__ dst, int X, int Y, int Z,
+                                                      float mu) {
+    using T = typename Store<ST>::T;
+    using P = Packed8<ST>;
+    constexpr int VX = P::VX;
     const int lane = threadIdx.x;
-    const int y = blockIdx.y * BY + threadIdx.y;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
     if (y >= Y) return;                              // whole warp
     const int x0 = (blockIdx.x * 32 + lane) * VX;
     const bool act = x0 < X;
-    const int z0 = min((int)blockIdx.z * ZC, Z - ZC);
-    const int z1 = z0 + ZC;
-    const int zs = max(z0, 1), ze = min(z1, Z - 1);
-    const int py = mirror(y, Y);
+    const int py = mirror(y, Y), pz = mirror(z, Z);
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
-    const int64_t col = (int64_t)py * X + x0;       // offset of this vector within a plane (row py)
-    const int64_t ocol = (int64_t)y * X + x0;       // output row y
+    const int64_t p = (int64_t)pz * plane + (int64_t)py * X + x0;
     const unsigned full = 0xffffffffu;
 
-    float prv[3][VX], cur[3][VX], nxt[3][VX];
+    uint2 rf[3], rc[3], ryp[3], rym[3], rzp[3], rzm[3];
+    const uint2 zero = make_uint2(0u, 0u);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        if (act) {
-            IO::load(src + c * n + (int64_t)(zs - 1) * plane + col, prv[c]);
-            IO::load(src + c * n + (int64_t)zs * plane + col, cur[c]);
-        } else {
-#pragma unroll
-            for (int i = 0; i < VX; i++) prv[c][i] = cur[c][i] = 0.0f;
-        }
+        const T *s = src + c * n + p;
+        rf[c] = act ? P::load(f + c * n + p) : zero;
+        rc[c] = act ? P::load(s) : zero;
+        ryp[c] = act ? P::load(s + X) : zero;
+        rym[c] = act ? P::load(s - X) : zero;
+        rzp[c] = act ? P::load(s + plane) : zero;
+        rzm[c] = act ? P::load(s - plane) : zero;
     }
-    for (int z = zs; z < ze; z++) {
-        const int64_t zo = (int64_t)z * plane;
-        float fv[3][VX], sqr[VX];
+    float fv[3][VX], sqr[VX];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            if (act) IO::load(f + c * n + zo + col, fv[c]);
-            else {
+    for (int c = 0; c < 3; c++) P::unpack(rf[c], fv[c]);
 #pragma unroll
-                for (int i = 0; i < VX; i++) fv[c][i] = 0.0f;
-            }
+    for (int i = 0; i < VX; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+    const int64_t o = (int64_t)z * plane + (int64_t)y * X + x0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        float cc[VX], yp[VX], ym[VX], zp[VX], zm[VX];
+        P::unpack(rc[c], cc);
+        P::unpack(ryp[c], yp);
+        P::unpack(rym[c], ym);
+        P::unpack(rzp[c], zp);
+        P::unpack(rzm[c], zm);
+        // x-neighbours: the last voxel of the lane to the left, the first of the lane to the right
+        float xl = __shfl_up_sync(full, cc[VX - 1], 1);
+        float xr = __shfl_down_sync(full, cc[0], 1);
+        if (lane == 0) xl = (act && x0 > 0) ? Store<ST>::load(src[c * n + p - 1]) : 0.0f;
+        if (lane == 31) xr = (act && x0 + VX < X) ? Store<ST>::load(src[c * n + p + VX]) : 0.0f;
+        float res[VX];
+#pragma unroll
+        for (int i = 0; i < VX; i++) {
+            const float v = cc[i];
+            float lap = -6.0f * v;
+            lap = lap + (i == VX - 1 ? xr : cc[i + 1 < VX ? i + 1 : i]);
+            lap = lap + (i == 0 ? xl : cc[i > 0 ? i - 1 : 0]);
+            lap = lap + yp[i];
+            lap = lap + ym[i];
+            lap = lap + zp[i];
+            lap = lap + zm[i];
+            const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+            res[i] = quantize<ST>(v + upd);
         }
-#pragma unroll
-        for (int i = 0; i < VX; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const T *sc = src + c * n + zo + col;
-            float yp[VX], ym[VX], res[VX];
-            if (act) {
-                IO::load(sc + plane, nxt[c]);
-                IO::load(sc + X, yp);
-                IO::load(sc - X, ym);
-            } else {
-#pragma unroll
-                for (int i = 0; i < VX; i++) nxt[c][i] = yp[i] = ym[i] = 0.0f;
-            }
-            float xl = __shfl_up_sync(full, cur[c][VX - 1], 1);
-            float xr = __shfl_down_sync(full, cur[c][0], 1);
-            if (lane == 0) xl = (act && x0 > 0) ? Store<ST>::load(sc[-1]) : 0.0f;
-            if (lane == 31) xr = (act && x0 + VX < X) ? Store<ST>::load(sc[VX]) : 0.0f;
-#pragma unroll
-            for (int i = 0; i < VX; i++) {
-                const float v = cur[c][i];
-                float lap = -6.0f * v;
-                lap = lap + (i == VX - 1 ? xr : cur[c][i + 1 < VX ? i + 1 : i]);
-                lap = lap + (i == 0 ? xl : cur[c][i > 0 ? i - 1 : 0]);
-                lap = lap + yp[i];
-                lap = lap + ym[i];
-                lap = lap + nxt[c][i];
-                lap = lap + prv[c][i];
-                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
-                res[i] = quantize<ST>(v + upd);
-            }
+        if constexpr (VX >= 3) {
             if (x0 == 0) res[0] = res[2];
             if (x0 + VX == X) res[VX - 1] = res[VX - 3];
-            if (act) {
-                T *dc = dst + c * n;
-                IO::store(dc + zo + ocol, res);
-                if (z == 2 && z0 == 0) IO::store(dc + ocol, res);
-                if (z == Z - 3 && z1 == Z) IO::store(dc + (int64_t)(Z - 1) * plane + ocol, res);
-            }
-#pragma unroll
-            for (int i = 0; i < VX; i++) {
-                prv[c][i] = cur[c][i];
-                cur[c][i] = nxt[c][i];
-            }
+        } else {
+            // VX == 2: x = 0 takes x = 2 (first voxel of the next lane), x = X-1
+            // takes x = X-3 (last voxel of the previous lane)
+            const float r_next0 = __shfl_down_sync(full, res[0], 1);
+            const float r_prev1 = __shfl_up_sync(full, res[1], 1);
+            if (x0 == 0) res[0] = (lane == 31) ? 0.0f : r_next0;
+            if (x0 + VX == X) res[1] = (lane == 0) ? 0.0f : r_prev1;
         }
+        if (act) P::store(dst + c * n + o, res);
     }
 }
 
@@ -216,19 +262,19 @@ size_t gvf_workspace_size(int X, int Y, int Z, int st) {
     return (size_t)3 * (size_t)X * (size_t)Y * (size_t)Z * storage_bytes(st);
 }
 
-constexpr int kStreamVX = 4, kStreamBY = 8, kStreamZC = 16;
+constexpr int kVecBY = 8;
 
 static int launch_gvf_plain(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z,
                             float mu, cudaStream_t s) {
-    if (X % kStreamVX == 0 && Z >= 3) {
-        const int zc = Z < kStreamZC ? Z : kStreamZC;
-        dim3 b(32, kStreamBY), g((X / kStreamVX + 31) / 32, (Y + kStreamBY - 1) / kStreamBY, (Z + zc - 1) / zc);
+    const int vx = st == TSF_STORE_F32 ? 2 : 4;     // voxels per 8-byte vector
+    // the x-boundary copy needs the vector holding x = 2 / X-3 in the same warp
+    if (X % vx == 0 && X >= 8 && !(vx == 2 && X % 64 == 2)) {
+        dim3 b(32, kVecBY), g((X / vx + 31) / 32, (Y + kVecBY - 1) / kVecBY, Z);
         TSF_DISPATCH_STORAGE(st, ST, {
             using T = typename Store<ST>::T;
-            gvf_stream_kernel<ST, kStreamVX, kStreamBY><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst,
-                                                                        X, Y, Z, mu, zc);
+            gvf_vec_kernel<ST><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst, X, Y, Z, mu);
         });
-        TSF_CHECK_LAUNCH("gvf_stream_kernel");
+        TSF_CHECK_LAUNCH("gvf_vec_kernel");
         return TSF_OK;
     }
     dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);

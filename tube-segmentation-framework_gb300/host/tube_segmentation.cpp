@@ -1,0 +1,371 @@
+// tube_segmentation.cpp -- run() / runSegmentation(): the reference's library
+// entry point (tube-segmentation.cpp:53-163) driving the GPU hot path through
+// the C ABI of this library.
+//
+// Stage order and parameter semantics follow the reference:
+//  readDatasetAndTransfer  (tube-segmentation.cpp:1399-1905): .mhd header,
+//      raw data, limits (getLimits :1380-1396), shrink to a multiple of 4,
+//      toFloat;
+//  runCircleFittingMethod  (:212-939): small-radius TDF on the un-diffused
+//      field when radius-min < 2.5, GVF (Jacobi or FMG) of the large-blur
+//      field, large-radius TDF, combine;
+//  runNewCenterlineAlg front half (parallelCenterlineExtraction.cpp:667-899).
+// The reference's GVF loop returns the result of iterations - 1 when the
+// iteration count is odd (gradientVectorFlow.cpp:1137-1172); run() does the
+// same.  Options outside this library's scope (other centerline methods, the
+// spline TDF, cropping, a CPU device) raise SIPL::SIPLException.
+#include <cuda_runtime_api.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <sstream>
+#include <vector>
+
+#include "tsf/tsf_c.h"
+#include "tsf/tube-segmentation.hpp"
+
+namespace {
+
+[[noreturn]] void raise(const std::string &msg) { throw SIPL::SIPLException(msg.c_str()); }
+
+void check(int code, const char *what) {
+    if (code == TSF_OK) return;
+    raise(std::string(what) + ": " + tsf_last_error_string());
+}
+
+void check_cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) raise(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Device buffer owned by a scope unless released.
+struct DevBuf {
+    void *p = nullptr;
+    DevBuf() = default;
+    explicit DevBuf(size_t bytes) { alloc(bytes); }
+    void alloc(size_t bytes) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        check_cuda(cudaMalloc(&p, bytes ? bytes : 256), "cudaMalloc");
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    void *release() {
+        void *q = p;
+        p = nullptr;
+        return q;
+    }
+    template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+};
+
+struct Stream {
+    cudaStream_t s = nullptr;
+    Stream() { check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate"); }
+    ~Stream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+};
+
+std::string trim(const std::string &v) {
+    size_t b = 0, e = v.size();
+    while (b < e && std::isspace((unsigned char)v[b])) b++;
+    while (e > b && std::isspace((unsigned char)v[e - 1])) e--;
+    return v.substr(b, e - b);
+}
+
+// value of "Key = value" lines; empty if the line is another key
+bool header_value(const std::string &line, const char *key, std::string &value) {
+    const size_t k = std::strlen(key);
+    if (line.compare(0, k, key) != 0) return false;
+    const size_t eq = line.find('=', k);
+    if (eq == std::string::npos) return false;
+    value = trim(line.substr(eq + 1));
+    return true;
+}
+
+struct HostVolume {
+    std::vector<char> data;
+    int type = -1;           // TSF_TYPE_*
+    int elem = 0;
+    SIPL::int3 size;
+    SIPL::float3 spacing{1, 1, 1};
+};
+
+template <typename T> void limits_of(const std::vector<char> &raw, float &lo, float &hi) {
+    const T *p = reinterpret_cast<const T *>(raw.data());
+    const size_t n = raw.size() / sizeof(T);
+    // reference getMinimum/getMaximum start from numeric_limits<T>::max()/min()
+    T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::min();
+    for (size_t i = 0; i < n; i++) {
+        mn = std::min(mn, p[i]);
+        mx = std::max(mx, p[i]);
+    }
+    lo = (float)mn;
+    hi = (float)mx;
+}
+
+HostVolume read_volume(const std::string &filename, paramList &parameters, float &minimum, float &maximum) {
+    std::ifstream mhd(filename.c_str());
+    if (!mhd) throw SIPL::IOException(filename.c_str(), __LINE__, __FILE__);
+    HostVolume v;
+    std::string line, value, typeName, rawName;
+    bool haveSize = false;
+    while (std::getline(mhd, line)) {
+        if (header_value(line, "ElementType", value)) {
+            std::istringstream(value) >> typeName;
+        } else if (header_value(line, "ElementDataFile", value)) {
+            std::istringstream(value) >> rawName;
+        } else if (header_value(line, "DimSize", value)) {
+            std::istringstream in(value);
+            in >> v.size.x >> v.size.y >> v.size.z;
+            haveSize = (bool)in;
+        } else if (header_value(line, "ElementSpacing", value)) {
+            std::istringstream in(value);
+            in >> v.spacing.x >> v.spacing.y >> v.spacing.z;
+        }
+    }
+    if (typeName.empty() || rawName.empty() || !haveSize)
+        throw SIPL::SIPLException("Error reading mhd file. Type, filename or size not found", __LINE__, __FILE__);
+    const size_t slash = filename.rfind('/');
+    if (slash != std::string::npos) rawName = filename.substr(0, slash + 1) + rawName;
+
+    if (typeName == "MET_SHORT") { v.type = TSF_TYPE_INT16; v.elem = 2; }
+    else if (typeName == "MET_USHORT") { v.type = TSF_TYPE_UINT16; v.elem = 2; }
+    else if (typeName == "MET_CHAR") { v.type = TSF_TYPE_INT8; v.elem = 1; }
+    else if (typeName == "MET_UCHAR") { v.type = TSF_TYPE_UINT8; v.elem = 1; }
+    else if (typeName == "MET_FLOAT") { v.type = TSF_TYPE_FLOAT32; v.elem = 4; }
+    else raise("unsupported data type " + typeName);
+
+    const size_t bytes = (size_t)v.size.x * v.size.y * v.size.z * v.elem;
+    v.data.resize(bytes);
+    FILE *f = std::fopen(rawName.c_str(), "rb");
+    if (!f) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
+    const size_t got = std::fread(v.data.data(), 1, bytes, f);
+    std::fclose(f);
+    if (got != bytes) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
+
+    // getLimits (tube-segmentation.cpp:1380-1396)
+    float lo = 0.0f, hi = 1.0f;
+    switch (v.type) {
+    case TSF_TYPE_INT16: limits_of<int16_t>(v.data, lo, hi); break;
+    case TSF_TYPE_UINT16: limits_of<uint16_t>(v.data, lo, hi); break;
+    case TSF_TYPE_INT8: limits_of<int8_t>(v.data, lo, hi); break;
+    case TSF_TYPE_UINT8: limits_of<uint8_t>(v.data, lo, hi); break;
+    default: limits_of<float>(v.data, lo, hi); break;
+    }
+    const std::string pmin = getParamStr(parameters, "minimum"), pmax = getParamStr(parameters, "maximum");
+    minimum = pmin != "off" ? (float)std::atof(pmin.c_str()) : lo;
+    maximum = pmax != "off" ? (float)std::atof(pmax.c_str()) : hi;
+    if (v.type == TSF_TYPE_UINT16) {
+        // unsigned CT data with the airway / AAA presets: HU limits shifted by 1024
+        const std::string preset = getParamStr(parameters, "parameters");
+        if (preset == "Lung-Airways-CT" || preset == "AAA-Vessels-CT") {
+            minimum = (float)std::atof(pmin.c_str()) + 1024.0f;
+            maximum = (float)std::atof(pmax.c_str()) + 1024.0f;
+        }
+    }
+    return v;
+}
+
+// Shrink every extent down to a multiple of 4 (tube-segmentation.cpp:1800-1828).
+void shrink_to_multiple_of_4(HostVolume &v) {
+    SIPL::int3 s = v.size;
+    s.x -= s.x % 4;
+    s.y -= s.y % 4;
+    s.z -= s.z % 4;
+    if (s.x == v.size.x && s.y == v.size.y && s.z == v.size.z) return;
+    std::vector<char> out((size_t)s.x * s.y * s.z * v.elem);
+    for (int z = 0; z < s.z; z++)
+        for (int y = 0; y < s.y; y++)
+            std::memcpy(&out[((size_t)z * s.y + y) * s.x * v.elem],
+                        &v.data[((size_t)z * v.size.y + y) * v.size.x * v.elem], (size_t)s.x * v.elem);
+    std::cout << "NOTE: reduced size to " << s.x << ", " << s.y << ", " << s.z << std::endl;
+    v.data.swap(out);
+    v.size = s;
+}
+
+int storage_from_parameters(paramList &p) {
+    const std::string s = getParamStr(p, "gvf-storage");
+    if (s == "f32") return TSF_STORE_F32;
+    if (s == "f16") return TSF_STORE_F16;
+    if (s == "bf16") return TSF_STORE_BF16;
+    if (s == "snorm16") return TSF_STORE_SNORM16;
+    return (getParamBool(p, "16bit-vectors") && !getParamBool(p, "32bit-vectors")) ? TSF_STORE_SNORM16
+                                                                                    : TSF_STORE_F32;
+}
+
+struct FieldResult {
+    DevBuf T, R, field;
+};
+
+// runCircleFittingMethod, tube-segmentation.cpp:212-939
+void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z, int st, bool tdf16,
+                           cudaStream_t s, FieldResult &out) {
+    const float rMin = getParam(P, "radius-min"), rMax = getParam(P, "radius-max"), rStep = getParam(P, "radius-step");
+    const float fmax = getParam(P, "fmax");
+    const int vsign = getParamStr(P, "mode") == "black" ? -1 : 1;
+    const float smallBlur = getParam(P, "small-blur"), largeBlur = getParam(P, "large-blur");
+    const size_t n = (size_t)X * Y * Z, es = tsf_storage_bytes(st), ts = tdf16 ? 2 : 4;
+    void *S = (void *)s;
+
+    DevBuf Ts, Rs, f4small;
+    if (rMin < 2.5f) {
+        DevBuf blurred;
+        const float *src = d_vol;
+        if (smallBlur > 0) {
+            blurred.alloc(n * 4);
+            check(tsf_blur(d_vol, blurred.as<float>(), X, Y, Z, smallBlur, S), "blur");
+            src = blurred.as<float>();
+        }
+        f4small.alloc(n * 4 * es);
+        check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4small.p, S), "vector field");
+        Ts.alloc(n * ts);
+        Rs.alloc(n * 4);
+        check(tsf_tdf_circle(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), S), "TDF");
+        if (rMax < 2.5f) {
+            out.T.p = Ts.release();
+            out.R.p = Rs.release();
+            out.field.p = f4small.release();
+            return;
+        }
+        f4small.alloc(0);   // free early, as the reference does
+    }
+    if (getParamBool(P, "use-spline-tdf")) raise("the spline TDF (use-spline-tdf) is not part of this library");
+
+    DevBuf blurred;
+    const float *src = d_vol;
+    if (largeBlur > 0) {
+        blurred.alloc(n * 4);
+        check(tsf_blur(d_vol, blurred.as<float>(), X, Y, Z, largeBlur, S), "blur");
+        src = blurred.as<float>();
+    }
+    out.field.alloc(n * 4 * es);
+    const int iterations = (int)getParam(P, "gvf-iterations");
+    const float mu = getParam(P, "gvf-mu");
+    if (getParamBool(P, "use-fmg-gvf")) {
+        DevBuf f4in(n * 4 * es);
+        check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4in.p, S), "vector field");
+        blurred.alloc(0);
+        DevBuf ws(tsf_gvf_fmg_workspace_size(X, Y, Z, st));
+        check(tsf_gvf_fmg(f4in.p, out.field.p, X, Y, Z, mu, iterations, st, ws.p,
+                          tsf_gvf_fmg_workspace_size(X, Y, Z, st), S), "multigrid GVF");
+    } else {
+        DevBuf f0(n * 3 * es), v(n * 3 * es);
+        check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, f0.p, nullptr, S), "vector field");
+        blurred.alloc(0);
+        check_cuda(cudaMemcpyAsync(v.p, f0.p, n * 3 * es, cudaMemcpyDeviceToDevice, s), "copy");
+        const size_t wsb = tsf_gvf_workspace_size(X, Y, Z, st);
+        DevBuf ws(wsb);
+        // the reference's ping-pong returns the even part of the iteration count
+        check(tsf_gvf(f0.p, v.p, X, Y, Z, mu, iterations - iterations % 2, st, ws.p, wsb, S), "GVF");
+        check(tsf_gvf_finish(v.p, out.field.p, X, Y, Z, st, S), "GVF finish");
+    }
+    out.T.alloc(n * ts);
+    out.R.alloc(n * 4);
+    check(tsf_tdf_circle(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
+                         out.R.as<float>(), S), "TDF");
+    if (rMin < 2.5f)
+        check(tsf_tdf_combine(Ts.p, Rs.as<float>(), out.T.p, out.R.as<float>(), (int64_t)n, tdf16, S), "combine");
+}
+
+}  // namespace
+
+TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel_dir*/) {
+    if (getParamStr(parameters, "device") != "gpu")
+        raise("device " + getParamStr(parameters, "device") + " is not supported: this library runs on the GPU");
+    const std::string method = getParamStr(parameters, "centerline-method");
+    if (method != "gpu") raise("centerline-method " + method + " is not part of this library (use gpu)");
+    if (getParamStr(parameters, "cropping") != "no")
+        raise("cropping " + getParamStr(parameters, "cropping") +
+              " is not part of this library; crop the volume beforehand and use --cropping no");
+
+    float minimum = 0.0f, maximum = 1.0f;
+    HostVolume hv = read_volume(filename, parameters, minimum, maximum);
+    std::cout << "Dataset of size " << hv.size.x << " " << hv.size.y << " " << hv.size.z << " loaded" << std::endl;
+    shrink_to_multiple_of_4(hv);
+    const int X = hv.size.x, Y = hv.size.y, Z = hv.size.z;
+    const size_t n = (size_t)X * Y * Z;
+    const bool tdf16 = getParamBool(parameters, "16bit-vectors");
+    const int st = storage_from_parameters(parameters);
+
+    TSFOutput *output = new TSFOutput(new SIPL::int3(X, Y, Z), tdf16);
+    output->setSpacing(hv.spacing);
+    output->setShiftVector(SIPL::int3(0, 0, 0));
+    try {
+        Stream stream;
+        void *S = (void *)stream.s;
+        DevBuf raw(hv.data.size()), vol(n * 4);
+        check_cuda(cudaMemcpyAsync(raw.p, hv.data.data(), hv.data.size(), cudaMemcpyHostToDevice, stream.s), "upload");
+        check(tsf_to_float(raw.p, hv.type, (int64_t)n, minimum, maximum, vol.as<float>(), S), "toFloat");
+        raw.alloc(0);
+
+        FieldResult fr;
+        circle_fitting_method(parameters, vol.as<float>(), X, Y, Z, st, tdf16, stream.s, fr);
+        vol.alloc(0);
+        check_cuda(cudaStreamSynchronize(stream.s), "TDF");
+        void *d_T = fr.T.p;                      // the output owns it from here on
+        output->setDeviceTDF(fr.T.release());
+        if (getParamBool(parameters, "tdf-only")) return output;
+
+        // runNewCenterlineAlg, front half (parallelCenterlineExtraction.cpp:667-899)
+        const size_t wsb = tsf_candidates_workspace_size(X, Y, Z);
+        const int64_t max_vertices = 16384;
+        DevBuf ws(wsb), cp(n), verts(sizeof(int32_t) * 3 * max_vertices);
+        int64_t nc = 0, nv = 0;
+        const int code = tsf_candidates(d_T, tdf16, fr.R.as<float>(), fr.field.p, st, X, Y, Z,
+                                        getParam(parameters, "tdf-high"), (int)getParam(parameters, "cube-size"),
+                                        verts.as<int32_t>(), max_vertices, cp.as<int8_t>(), nullptr, 0, &nc, &nv,
+                                        ws.p, wsb, S);
+        std::cout << "candidates: " << nc << std::endl;
+        if (nc <= 0 || (double)nc > 0.5 * (double)n)
+            throw SIPL::SIPLException("The number of candidate voxels is too low or too high. Something went "
+                                      "wrong... Wrong parameters? Out of memory?", __LINE__, __FILE__);
+        if (getParamBool(parameters, "centerpoints-only")) {
+            check_cuda(cudaStreamSynchronize(stream.s), "candidates");
+            output->setDeviceCenterlineVoxels(static_cast<int8_t *>(cp.release()));
+            return output;
+        }
+        std::cout << "number of vertices detected " << nv << std::endl;
+        if (code != TSF_OK && code != TSF_ERR_COUNT_RANGE) check(code, "candidates");
+        if (nv < 8) throw SIPL::SIPLException("Too few centerpoints detected. Revise parameters.", __LINE__, __FILE__);
+        if (nv >= 16384)
+            throw SIPL::SIPLException("Too many centerpoints detected. More cropping of dataset is probably needed.",
+                                      __LINE__, __FILE__);
+        std::vector<int32_t> hv3((size_t)nv * 3);
+        check_cuda(cudaMemcpyAsync(hv3.data(), verts.p, hv3.size() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                   stream.s), "vertices");
+        check_cuda(cudaStreamSynchronize(stream.s), "vertices");
+        std::vector<SIPL::int3> vlist((size_t)nv);
+        char *mask = new char[n]();
+        for (int64_t i = 0; i < nv; i++) {
+            vlist[(size_t)i] = SIPL::int3(hv3[3 * i], hv3[3 * i + 1], hv3[3 * i + 2]);
+            mask[(size_t)hv3[3 * i] + (size_t)X * ((size_t)hv3[3 * i + 1] + (size_t)Y * hv3[3 * i + 2])] = 1;
+        }
+        output->setCenterpoints(vlist);
+        output->setCenterlineVoxels(mask);
+        std::cout << "NOTE: centerline linking and segmentation are not part of this library; the centerline "
+                     "voxels mark the detected centerpoints"
+                  << std::endl;
+        if (getParamStr(parameters, "storage-dir") != "off")
+            writeDataToDisk(output, getParamStr(parameters, "storage-dir"), getParamStr(parameters, "storage-name"));
+        return output;
+    } catch (...) {
+        delete output;
+        throw;
+    }
+}
+
+TSFOutput *runSegmentation(std::string filename, paramList &parameters, std::string kernel_dir) {
+    return run(filename, parameters, kernel_dir);
+}

@@ -35,6 +35,7 @@ def _tree_segments(shape, rng, n_generations, r0, r_factor, r_floor, len_range,
     rooted at a random point of a random face, growing inwards."""
     Z, Y, X = shape
     ext = np.array([X, Y, Z], float)
+    margin = np.minimum(margin, ext / 4.0)      # thin volumes
     face = rng.integers(6)
     axis, side = face // 2, face % 2
     p0 = rng.uniform(margin, ext - margin)

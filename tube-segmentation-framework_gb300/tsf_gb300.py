@@ -63,6 +63,7 @@ def _declare(L):
         "tsf_storage_bytes": (_sz, [_i]),
         "tsf_kernel_launches": (C.c_ulonglong, []),
         "tsf_blur_mask": (_i, [_f, _p, _p]),
+        "tsf_to_float": (_i, [_p, _i, _i64, _f, _f, _p, _p]),
         "tsf_blur": (_i, [_p, _p, _i, _i, _i, _f, _p]),
         "tsf_vector_field": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p]),
         "tsf_gvf_workspace_size": (_sz, [_i, _i, _i, _i]),
