@@ -160,6 +160,21 @@ int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int
 int tsf_gvf_static(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                    int storage, void *stream);
 
+/* Workspace bytes for tsf_gvf_adjoint. */
+size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iterations,
+                                      int checkpoint_every);
+
+/* Reverse-mode derivative of `iterations` GVF Jacobi iterations started from
+ * v_0 = f0 (no counterpart in the reference, which has no derivatives).
+ * Given d_gv = dL/dv_K (planar FP32), writes dL/df0 (planar FP32, all paths
+ * through the data term, |f0|^2 and v_0) to d_gf0 and dL/dmu to *dmu (host,
+ * FP64; NULL to skip -- otherwise the call synchronises `stream`).  Forward
+ * states are recomputed from checkpoints kept every `checkpoint_every`
+ * iterations (<= 0: ceil(sqrt(iterations))); memory (K/C + C) states. */
+int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,
+                    const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every,
+                    void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* GVF3DFinish (kernels.cl:1506-1515): packs the planar field into a field4
  * image with w = |v| (1 where |v| == 0). */
 int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int storage,

@@ -129,23 +129,52 @@ template <int ST> struct VecIO<ST, 2> {
     }
 };
 
-// Eight bytes of stored components: 4 voxels of a 16-bit format or 2 of FP32.
+// Eight bytes of stored components: 4 voxels of a 16-bit format or 2 of FP32,
+// unpacked / packed two at a time with the paired conversion intrinsics.
 template <int ST> struct Packed8 {
     using T = typename Store<ST>::T;
     static constexpr int VX = 8 / (int)sizeof(T);
     static __device__ __forceinline__ uint2 load(const T *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
     static __device__ __forceinline__ void unpack(uint2 raw, float o[VX]) {
-        T c[VX];
-        memcpy(c, &raw, 8);
-#pragma unroll
-        for (int i = 0; i < VX; i++) o[i] = Store<ST>::load(c[i]);
+        if constexpr (ST == TSF_STORE_F32) {
+            o[0] = __uint_as_float(raw.x);
+            o[1] = __uint_as_float(raw.y);
+        } else if constexpr (ST == TSF_STORE_F16) {
+            const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&raw.x));
+            const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&raw.y));
+            o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+        } else if constexpr (ST == TSF_STORE_BF16) {
+            o[0] = __uint_as_float(raw.x << 16);
+            o[1] = __uint_as_float(raw.x & 0xffff0000u);
+            o[2] = __uint_as_float(raw.y << 16);
+            o[3] = __uint_as_float(raw.y & 0xffff0000u);
+        } else {
+            o[0] = Store<ST>::load((int16_t)(raw.x & 0xffffu));
+            o[1] = Store<ST>::load((int16_t)(raw.x >> 16));
+            o[2] = Store<ST>::load((int16_t)(raw.y & 0xffffu));
+            o[3] = Store<ST>::load((int16_t)(raw.y >> 16));
+        }
     }
+    // rounds to the storage format (the only rounding of an iteration's result)
     static __device__ __forceinline__ void store(T *p, const float o[VX]) {
-        T c[VX];
-#pragma unroll
-        for (int i = 0; i < VX; i++) c[i] = Store<ST>::store(o[i]);
         uint2 raw;
-        memcpy(&raw, c, 8);
+        if constexpr (ST == TSF_STORE_F32) {
+            raw.x = __float_as_uint(o[0]);
+            raw.y = __float_as_uint(o[1]);
+        } else if constexpr (ST == TSF_STORE_F16) {
+            const __half2 a = __floats2half2_rn(o[0], o[1]), b = __floats2half2_rn(o[2], o[3]);
+            raw.x = *reinterpret_cast<const unsigned *>(&a);
+            raw.y = *reinterpret_cast<const unsigned *>(&b);
+        } else if constexpr (ST == TSF_STORE_BF16) {
+            const __nv_bfloat162 a = __floats2bfloat162_rn(o[0], o[1]), b = __floats2bfloat162_rn(o[2], o[3]);
+            raw.x = *reinterpret_cast<const unsigned *>(&a);
+            raw.y = *reinterpret_cast<const unsigned *>(&b);
+        } else {
+            T c[VX];
+#pragma unroll
+            for (int i = 0; i < VX; i++) c[i] = Store<ST>::store(o[i]);
+            memcpy(&raw, c, 8);
+        }
         *reinterpret_cast<uint2 *>(p) = raw;
     }
 };
@@ -223,7 +252,7 @@ __global__ void __launch_bounds__(256) gvf_vec_kernel(const typename Store<ST>::
             lap = lap + zp[i];
             lap = lap + zm[i];
             const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
-            res[i] = quantize<ST>(v + upd);
+            res[i] = v + upd;                        // rounded to storage by the store
         }
         if constexpr (VX >= 3) {
             if (x0 == 0) res[0] = res[2];

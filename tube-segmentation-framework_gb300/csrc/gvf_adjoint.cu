@@ -1,0 +1,269 @@
+// gvf_adjoint.cu -- reverse-mode derivative of K GVF Jacobi iterations with
+// respect to the data term f0 and to mu (no counterpart in the reference,
+// which has no derivatives).
+//
+// Forward map of one iteration, per component c, at output w with p = m(w)
+// (the mirror rule, applied per axis: 0 -> 2, size-1 -> size-3):
+//     v'_c[w] = v_c[p] + mu * L(v_c)[p] - (v_c[p] - f_c[p]) * s[p],
+//     L(u)[p] = sum_{6 neighbours q} u[q] - 6 u[p],   s = |f|^2.
+// Given lambda' = dL/dv', with g = fold(lambda'), g[p] = sum_{w : m(w) = p} lambda'[w]
+// (zero outside the interior [1, size-2]^3, the image of m):
+//     lambda_c[q] = g_c[q] (1 - 6 mu - s[q]) + mu * sum_{6 neighbours r of q} g_c[r]
+//     dL/df_c[q] += g_c[q] s[q] - 2 f_c[q] sum_d g_d[q] (v_d[q] - f_d[q])
+//     dL/dmu    += sum_c sum_q g_c[q] L(v_c)[q]
+// and, since v_0 = f0 (GVF3DInit), dL/df0 += lambda_0 at the end.
+// Storage rounding of the forward states is treated as the identity.
+//
+// Checkpointing: the forward states v_0, v_C, v_2C, ... are kept (C =
+// checkpoint interval, ceil(sqrt(K)) by default); each segment is recomputed
+// from its checkpoint into a C-state buffer and then reversed, so the memory is
+// (K/C + C) states and the extra work one forward pass.  Cotangents are FP32;
+// the mu derivative is accumulated in FP64, per block in a fixed order, so the
+// result does not depend on scheduling.
+#include "tsf_common.cuh"
+
+namespace tsf {
+
+int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st, void *ws,
+            size_t ws_bytes, int mode, cudaStream_t s);
+size_t gvf_workspace_size(int X, int Y, int Z, int st);
+
+// folded cotangent at (x, y, z): sum of lambda' over the voxels that mirror to it
+__device__ __forceinline__ float fold_at(const float *__restrict__ lp, int x, int y, int z, int X, int Y, int Z) {
+    if (x < 1 || y < 1 || z < 1 || x > X - 2 || y > Y - 2 || z > Z - 2) return 0.0f;
+    int xs[2] = {x, 0}, ys[2] = {y, 0}, zs[2] = {z, 0};
+    int nx = 1, ny = 1, nz = 1;
+    if (x == 2) xs[nx++] = 0;
+    else if (x == X - 3) xs[nx++] = X - 1;
+    if (y == 2) ys[ny++] = 0;
+    else if (y == Y - 3) ys[ny++] = Y - 1;
+    if (z == 2) zs[nz++] = 0;
+    else if (z == Z - 3) zs[nz++] = Z - 1;
+    // X == 5: index 2 is both 2 and X-3 -> sources 0, 2, 4
+    int xs3 = -1, ys3 = -1, zs3 = -1;
+    if (x == 2 && X - 3 == 2) xs3 = X - 1;
+    if (y == 2 && Y - 3 == 2) ys3 = Y - 1;
+    if (z == 2 && Z - 3 == 2) zs3 = Z - 1;
+    float g = 0.0f;
+    for (int c = 0; c < nz + (zs3 >= 0); c++) {
+        const int zz = c < nz ? zs[c] : zs3;
+        for (int b = 0; b < ny + (ys3 >= 0); b++) {
+            const int yy = b < ny ? ys[b] : ys3;
+            for (int a = 0; a < nx + (xs3 >= 0); a++) {
+                const int xx = a < nx ? xs[a] : xs3;
+                g += lp[lin(xx, yy, zz, X, Y)];
+            }
+        }
+    }
+    return g;
+}
+
+template <int ST>
+__global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__restrict__ lam_in,
+                                                               const typename Store<ST>::T *__restrict__ v,
+                                                               const typename Store<ST>::T *__restrict__ f,
+                                                               float *__restrict__ lam_out, float *__restrict__ gf,
+                                                               double *__restrict__ dmu_block, int X, int Y, int Z,
+                                                               float mu) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    const bool in = x < X && y < Y && z < Z;
+    const int64_t n = (int64_t)X * Y * Z;
+    double dmu = 0.0;
+    if (in) {
+        const int64_t q = lin(x, y, z, X, Y);
+        float fv[3], vv[3], g[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            fv[c] = Store<ST>::load(f[c * n + q]);
+            vv[c] = Store<ST>::load(v[c * n + q]);
+        }
+        const float s = (fv[0] * fv[0] + fv[1] * fv[1]) + fv[2] * fv[2];
+        const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= X - 2 && y <= Y - 2 && z <= Z - 2;
+        float gdot = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float *lp = lam_in + c * n;
+            g[c] = fold_at(lp, x, y, z, X, Y, Z);
+            float nb = 0.0f;
+            nb += fold_at(lp, x + 1, y, z, X, Y, Z);
+            nb += fold_at(lp, x - 1, y, z, X, Y, Z);
+            nb += fold_at(lp, x, y + 1, z, X, Y, Z);
+            nb += fold_at(lp, x, y - 1, z, X, Y, Z);
+            nb += fold_at(lp, x, y, z + 1, X, Y, Z);
+            nb += fold_at(lp, x, y, z - 1, X, Y, Z);
+            lam_out[c * n + q] = g[c] * (1.0f - 6.0f * mu - s) + mu * nb;
+            gdot += g[c] * (vv[c] - fv[c]);
+            if (interior && g[c] != 0.0f) {
+                const typename Store<ST>::T *vc = v + c * n;
+                const int64_t sx = 1, sy = X, sz = (int64_t)X * Y;
+                float L = Store<ST>::load(vc[q + sx]) + Store<ST>::load(vc[q - sx]);
+                L += Store<ST>::load(vc[q + sy]) + Store<ST>::load(vc[q - sy]);
+                L += Store<ST>::load(vc[q + sz]) + Store<ST>::load(vc[q - sz]);
+                L -= 6.0f * vv[c];
+                dmu += (double)g[c] * (double)L;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; c++) gf[c * n + q] += g[c] * s - 2.0f * fv[c] * gdot;
+    }
+    // deterministic per-block reduction of the mu derivative
+    __shared__ double red[32];
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dmu += __shfl_down_sync(0xffffffffu, dmu, o);
+    if ((t & 31) == 0) red[t >> 5] = dmu;
+    __syncthreads();
+    if (t == 0) {
+        const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) / 32;
+        double sum = 0.0;
+        for (int i = 0; i < nw; i++) sum += red[i];
+        const int64_t b = blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+        dmu_block[b] += sum;
+    }
+}
+
+__global__ void add_planar_kernel(float *__restrict__ a, const float *__restrict__ b, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += b[i];
+}
+
+__global__ void reduce_double_kernel(const double *__restrict__ in, int64_t n, double *out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += in[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x / 32); i++) t += red[i];
+        *out = t;
+    }
+}
+
+static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+struct AdjLayout {
+    int C, nck;
+    size_t state, ck, seg, lam0, lam1, dmu, dmu_out, gvf_ws, bytes;
+    int64_t nblocks;
+};
+
+static dim3 adj_block() { return dim3(32, 4, 2); }
+static dim3 adj_grid(int X, int Y, int Z) { return dim3((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2); }
+
+static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
+    AdjLayout L;
+    if (C <= 0) {
+        C = 1;
+        while (C * C < K) C++;
+    }
+    L.C = C;
+    L.nck = K > 0 ? (K + C - 1) / C : 0;
+    const size_t n = (size_t)X * Y * Z;
+    L.state = al256(3 * n * storage_bytes(st));
+    const dim3 g = adj_grid(X, Y, Z);
+    L.nblocks = (int64_t)g.x * g.y * g.z;
+    size_t off = 0;
+    L.ck = off; off += L.state * (size_t)L.nck;
+    L.seg = off; off += L.state * (size_t)C;
+    L.lam0 = off; off += al256(3 * n * sizeof(float));
+    L.lam1 = off; off += al256(3 * n * sizeof(float));
+    L.dmu = off; off += al256(sizeof(double) * (size_t)L.nblocks);
+    L.dmu_out = off; off += 256;
+    L.gvf_ws = off; off += al256(gvf_workspace_size(X, Y, Z, st));
+    L.bytes = off;
+    return L;
+}
+
+size_t gvf_adjoint_workspace_size(int X, int Y, int Z, int st, int K, int C) {
+    return adj_layout(X, Y, Z, st, K, C).bytes;
+}
+
+int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int st, const float *d_gv, float *d_gf0,
+                    double *dmu_host, int C, void *ws, size_t ws_bytes, cudaStream_t s) {
+    int r = check_dims(X, Y, Z);
+    if (r) return r;
+    if (!valid_storage(st)) return fail(TSF_ERR_INVALID_ARG, "unknown storage format");
+    if (!d_f0 || !d_gv || !d_gf0) return fail(TSF_ERR_INVALID_ARG, "null buffer");
+    if (K < 0) return fail(TSF_ERR_INVALID_ARG, "iterations must be >= 0");
+    const AdjLayout L = adj_layout(X, Y, Z, st, K, C);
+    if (!ws || ws_bytes < L.bytes) return fail(TSF_ERR_WORKSPACE, "GVF adjoint workspace too small");
+    char *w = (char *)ws;
+    const int64_t n = (int64_t)X * Y * Z;
+    const size_t sb = storage_bytes(st);
+    const size_t state_bytes = 3 * (size_t)n * sb;
+    float *lam = (float *)(w + L.lam0), *lam2 = (float *)(w + L.lam1);
+    double *dmu_b = (double *)(w + L.dmu);
+    TSF_TRY_CUDA(cudaMemsetAsync(d_gf0, 0, sizeof(float) * 3 * (size_t)n, s));
+    TSF_TRY_CUDA(cudaMemsetAsync(dmu_b, 0, sizeof(double) * (size_t)L.nblocks, s));
+    TSF_TRY_CUDA(cudaMemcpyAsync(lam, d_gv, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    void *gws = w + L.gvf_ws;
+    const size_t gws_bytes = gvf_workspace_size(X, Y, Z, st);
+
+    // forward pass keeping checkpoints v_0, v_C, ...
+    for (int i = 0; i < L.nck; i++) {
+        void *ck = w + L.ck + (size_t)i * L.state;
+        const void *prev = i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
+        TSF_TRY_CUDA(cudaMemcpyAsync(ck, prev, state_bytes, cudaMemcpyDeviceToDevice, s));
+        if (i > 0) {
+            r = run_gvf(d_f0, ck, X, Y, Z, mu, L.C, st, gws, gws_bytes, 1, s);
+            if (r) return r;
+        }
+    }
+    // reverse, one segment at a time
+    for (int seg = L.nck - 1; seg >= 0; seg--) {
+        const int k0 = seg * L.C, k1 = (k0 + L.C < K) ? k0 + L.C : K;
+        // states k0 .. k1-1 into the segment buffer
+        for (int k = k0; k < k1; k++) {
+            void *dstate = w + L.seg + (size_t)(k - k0) * L.state;
+            const void *from = k == k0 ? (const void *)(w + L.ck + (size_t)seg * L.state)
+                                       : (const void *)(w + L.seg + (size_t)(k - k0 - 1) * L.state);
+            TSF_TRY_CUDA(cudaMemcpyAsync(dstate, from, state_bytes, cudaMemcpyDeviceToDevice, s));
+            if (k > k0) {
+                r = run_gvf(d_f0, dstate, X, Y, Z, mu, 1, st, gws, gws_bytes, 1, s);
+                if (r) return r;
+            }
+        }
+        for (int k = k1 - 1; k >= k0; k--) {
+            const void *vk = w + L.seg + (size_t)(k - k0) * L.state;
+            TSF_DISPATCH_STORAGE(st, ST, {
+                using T = typename Store<ST>::T;
+                gvf_adjoint_step_kernel<ST><<<adj_grid(X, Y, Z), adj_block(), 0, s>>>(
+                    lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_b, X, Y, Z, mu);
+            });
+            TSF_CHECK_LAUNCH("gvf_adjoint_step_kernel");
+            float *t = lam; lam = lam2; lam2 = t;
+        }
+    }
+    // v_0 = f0
+    const int64_t n3 = 3 * n;
+    add_planar_kernel<<<(unsigned)((n3 + 255) / 256), 256, 0, s>>>(d_gf0, lam, n3);
+    TSF_CHECK_LAUNCH("add_planar_kernel");
+    double *dmu_dev = (double *)(w + L.dmu_out);
+    reduce_double_kernel<<<1, 1024, 0, s>>>(dmu_b, L.nblocks, dmu_dev);
+    TSF_CHECK_LAUNCH("reduce_double_kernel");
+    if (dmu_host) {
+        TSF_TRY_CUDA(cudaMemcpyAsync(dmu_host, dmu_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+        TSF_TRY_CUDA(cudaStreamSynchronize(s));
+    }
+    return TSF_OK;
+}
+
+}  // namespace tsf
+
+extern "C" size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iterations,
+                                                 int checkpoint_every) {
+    if (!tsf::valid_storage(storage) || X <= 0 || Y <= 0 || Z <= 0 || iterations < 0) return 0;
+    return tsf::gvf_adjoint_workspace_size(X, Y, Z, storage, iterations, checkpoint_every);
+}
+
+extern "C" int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,
+                               const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every, void *d_workspace,
+                               size_t workspace_bytes, void *stream) {
+    return tsf::run_gvf_adjoint(d_f0, X, Y, Z, mu, iterations, storage, d_gv, d_gf0, dmu, checkpoint_every,
+                                d_workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}

@@ -71,6 +71,8 @@ def _declare(L):
         "tsf_gvf_mode": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _i, _p]),
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
+        "tsf_gvf_adjoint_workspace_size": (_sz, [_i, _i, _i, _i, _i, _i]),
+        "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
         "tsf_candidates_workspace_size": (_sz, [_i, _i, _i]),
@@ -181,6 +183,21 @@ def gvf(f0, mu: float, iterations: int, storage: str = "f32", v=None, ws=None, m
     _check(L.tsf_gvf_mode(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
                           _ptr(ws), ws.numel(), int(mode), _stream(stream)))
     return v
+
+
+def gvf_adjoint(f0, mu: float, iterations: int, gv, storage: str = "f32", checkpoint_every: int = 0,
+                stream=None):
+    """dL/df0 (planar float32) and dL/dmu for L with dL/dv_K = gv."""
+    torch = _torch()
+    _, Z, Y, X = f0.shape
+    L = load()
+    need = L.tsf_gvf_adjoint_workspace_size(X, Y, Z, STORAGE[storage], int(iterations), int(checkpoint_every))
+    ws = workspace(need)
+    gf = torch.empty((3, Z, Y, X), dtype=torch.float32, device=f0.device)
+    dmu = C.c_double(0.0)
+    _check(L.tsf_gvf_adjoint(_ptr(f0), X, Y, Z, float(mu), int(iterations), STORAGE[storage], _ptr(gv), _ptr(gf),
+                             C.byref(dmu), int(checkpoint_every), _ptr(ws), ws.numel(), _stream(stream)))
+    return gf, dmu.value
 
 
 def gvf_finish(v, storage: str = "f32", out=None, stream=None):
