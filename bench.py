@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-gvf-iters", type=int, default=6)
+    ap.add_argument("--accuracy", action="store_true",
+                    help="instead of timing: errors of every storage format against the FP64 oracle")
     return ap.parse_args()
 
 
@@ -437,8 +439,63 @@ def run_reference(args):
     return line
 
 
+def run_accuracy(args):
+    """GVF field, TDF and centerpoint agreement of the GPU path for each storage
+    format against the FP64 oracle run of the same method (same volume, same
+    parameters).  TDF errors are absolute (T is in [0, 1])."""
+    import torch
+    import oracle as O
+    import synthetic
+    import tsf_gb300 as T
+
+    O.build()
+    n = args.size
+    shape = (n, n, n)
+    vol = synthetic.vascular_tree(shape, seed=args.seed)
+    P = PARAMS
+    t0 = time.perf_counter()
+    b64 = O.blur(vol, P["large_blur"], f64=True)
+    f64 = O.vector_field(b64, P["fmax"], P["vsign"], "f32", f64=True)
+    v64 = O.gvf(f64, args.mu, args.iters, f64=True)
+    field64 = O.gvf_finish(v64, f64=True)
+    fs64 = O.vector_field(vol.astype(np.float64), P["fmax"], P["vsign"], "f32", f64=True)
+    Ts64, Rs64 = O.tdf_circle(fs64, P["rmin"], 3.0, 0.5, f64=True)
+    Tl64, Rl64 = O.tdf_circle(field64, max(2.5, P["rmin"]), P["rmax"], P["rstep"], f64=True)
+    T64, R64 = O.combine(Ts64, Rs64, Tl64, Rl64, f64=True)
+    ref = O.centerpoints(T64, R64, field64, P["tdf_high"], P["cube_size"], f64=True)
+    t_oracle = time.perf_counter() - t0
+    out = {"size": n, "iterations": args.iters, "mu": args.mu, "oracle_s": round(t_oracle, 1),
+           "fp64_vertices": int(len(ref["vertices"]))}
+    vset = set(map(tuple, ref["vertices"].tolist()))
+    for st in ("f32", "f16", "bf16", "snorm16"):
+        pipe = Pipeline(T, torch, shape, st, args.iters, args.mu)
+        pipe.vol.copy_(torch.from_numpy(vol))
+        pipe.step()
+        torch.cuda.synchronize()
+        v = T.to_float(pipe.v, st).cpu().numpy()
+        Tg = pipe.Tl.cpu().numpy()
+        dT = np.abs(Tg.astype(np.float64) - T64)
+        got = pipe.verts[: min(pipe.last["n_vertices"], pipe.max_vertices)].cpu().numpy()
+        gset = set(map(tuple, got.tolist()))
+        inter = len(vset & gset)
+        out[st] = {"gvf_max_abs_err": float(np.abs(v - v64).max()),
+                   "tdf_max_abs_err": float(dT.max()),
+                   "tdf_p999_abs_err": float(np.quantile(dT, 0.999)),
+                   "tdf_mean_abs_err": float(dT.mean()),
+                   "tdf_frac_within_1e-3": float((dT <= 1e-3).mean()),
+                   "vertices": int(len(gset)), "vertices_equal_fp64": inter,
+                   "vertex_jaccard": round(inter / max(1, len(vset | gset)), 5),
+                   "same_vertex_list": bool(np.array_equal(got, ref["vertices"]))}
+        del pipe
+        torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
+    if args.accuracy:
+        print(json.dumps(run_accuracy(args)))
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

@@ -194,6 +194,12 @@ int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int sto
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
                    float rstep, void *d_T, int tdf_unorm16, float *d_R, void *stream);
 
+/* tsf_tdf_circle with the kernel forced: mode 1 = one voxel per lane, 0 = the
+ * default (radius sweeps load-balanced within each warp).  Identical results. */
+int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, float rmin,
+                        float rmax, float rstep, void *d_T, int tdf_unorm16, float *d_R, int mode,
+                        void *stream);
+
 /* combine (kernels.cl:561-572, tube-segmentation.cpp:802-824): where the small
  * TDF exceeds the large one, take it and its radius.  d_T_large / d_R_large
  * are updated in place; T arrays are float or unorm16 per tdf_unorm16. */

@@ -125,12 +125,16 @@ def _to_device_field4(torch, field4, storage):
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)])
 @pytest.mark.parametrize("unorm", [False, True])
-def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm, mode):
+    """Both TDF kernels (load-balanced sweeps, one voxel per lane); X = 26 and
+    X = 150 give one partial segment and a full plus a partial segment."""
     torch = torch_dev
-    field4, _ = _field(oracle, synth, (28, 30, 26), 6, storage)
+    shape = (28, 30, 26) if mode == 1 or storage != "f32" else (9, 10, 150)
+    field4, _ = _field(oracle, synth, shape, 6, storage)
     d4 = _to_device_field4(torch, field4, storage)
     assert np.array_equal(_np_stored(d4, storage), field4)
-    T, R = tsf.tdf_circle(d4, *rng_, storage=storage, unorm16=unorm)
+    T, R = tsf.tdf_circle(d4, *rng_, storage=storage, unorm16=unorm, mode=mode)
     oT, oR = oracle.tdf_circle(field4, *rng_)
     if unorm:
         assert np.array_equal(_u16(T), oracle.to_unorm16(oT))

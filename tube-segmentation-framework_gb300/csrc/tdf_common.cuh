@@ -1,0 +1,97 @@
+// tdf_common.cuh -- device pieces of the circle-fitting TDF shared by the
+// forward kernel (tdf.cu) and its reverse-mode derivative (tdf_adjoint.cu):
+// the sample-direction table, the Hessian of the field and the OpenCL linear
+// sampler (reference kernels.cl:700-810, 1065-1157).
+#pragma once
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+
+#include "eigen3.cuh"
+#include "tsf_common.cuh"
+
+namespace tsf {
+
+struct CircleTable {
+    float c[32];
+    float s[32];
+};
+
+// cos(j), sin(j), j = 0..31 radians, rounded to 6 significant digits: the
+// sample directions of the reference (kernels.cl:1068-1069).
+inline CircleTable host_circle_table() {
+    CircleTable t;
+    char buf[64];
+    for (int j = 0; j < 32; j++) {
+        snprintf(buf, sizeof buf, "%.6g", cos((double)j));
+        t.c[j] = strtof(buf, nullptr);
+        snprintf(buf, sizeof buf, "%.6g", sin((double)j));
+        t.s[j] = strtof(buf, nullptr);
+    }
+    return t;
+}
+
+// Hessian of the field at (x,y,z): central differences of the x, y, z
+// channels (reference gradient / gradientNormalized, kernels.cl:700-810),
+// optionally divided by each neighbour's w.  Symmetric from the lower
+// triangle (kernels.cl:1094-1098).
+template <int ST, bool NORM>
+__device__ __forceinline__ void hessian(const void *F, int X, int Y, int Z, int x, int y, int z, float H[3][3]) {
+    const float4 xp = Vec4Load<ST>::load(F, lin(clampi(x + 1, X), y, z, X, Y));
+    const float4 xm = Vec4Load<ST>::load(F, lin(clampi(x - 1, X), y, z, X, Y));
+    const float4 yp = Vec4Load<ST>::load(F, lin(x, clampi(y + 1, Y), z, X, Y));
+    const float4 ym = Vec4Load<ST>::load(F, lin(x, clampi(y - 1, Y), z, X, Y));
+    const float4 zp = Vec4Load<ST>::load(F, lin(x, y, clampi(z + 1, Z), X, Y));
+    const float4 zm = Vec4Load<ST>::load(F, lin(x, y, clampi(z - 1, Z), X, Y));
+    float Fxx, Fyx, Fyy, Fzx, Fzy, Fzz;
+    if (NORM) {
+        Fxx = 0.5f * (xp.x / xp.w - xm.x / xm.w);
+        Fyx = 0.5f * (xp.y / xp.w - xm.y / xm.w);
+        Fyy = 0.5f * (yp.y / yp.w - ym.y / ym.w);
+        Fzx = 0.5f * (xp.z / xp.w - xm.z / xm.w);
+        Fzy = 0.5f * (yp.z / yp.w - ym.z / ym.w);
+        Fzz = 0.5f * (zp.z / zp.w - zm.z / zm.w);
+    } else {
+        Fxx = 0.5f * (xp.x - xm.x);
+        Fyx = 0.5f * (xp.y - xm.y);
+        Fyy = 0.5f * (yp.y - ym.y);
+        Fzx = 0.5f * (xp.z - xm.z);
+        Fzy = 0.5f * (yp.z - ym.z);
+        Fzz = 0.5f * (zp.z - zm.z);
+    }
+    H[0][0] = Fxx; H[0][1] = Fyx; H[0][2] = Fzx;
+    H[1][0] = Fyx; H[1][1] = Fyy; H[1][2] = Fzy;
+    H[2][0] = Fzx; H[2][1] = Fzy; H[2][2] = Fzz;
+}
+
+// OpenCL linear filter, unnormalised coordinates, clamp to edge (OpenCL 1.1
+// section 8.2); weights summed in the specification's order.
+template <int ST>
+__device__ __forceinline__ float3 sample_linear(const void *F, int X, int Y, int Z, float u, float v, float w) {
+    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
+    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
+    const float a = uu - fu, b = vv - fv, c = ww - fw;
+    int i0 = (int)fu, j0 = (int)fv, k0 = (int)fw;
+    const int i1 = clampi(i0 + 1, X), j1 = clampi(j0 + 1, Y), k1 = clampi(k0 + 1, Z);
+    i0 = clampi(i0, X); j0 = clampi(j0, Y); k0 = clampi(k0, Z);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
+    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    const int64_t r00 = lin(0, j0, k0, X, Y), r10 = lin(0, j1, k0, X, Y);
+    const int64_t r01 = lin(0, j0, k1, X, Y), r11 = lin(0, j1, k1, X, Y);
+    const float4 t000 = Vec4Load<ST>::load(F, r00 + i0), t100 = Vec4Load<ST>::load(F, r00 + i1);
+    const float4 t010 = Vec4Load<ST>::load(F, r10 + i0), t110 = Vec4Load<ST>::load(F, r10 + i1);
+    const float4 t001 = Vec4Load<ST>::load(F, r01 + i0), t101 = Vec4Load<ST>::load(F, r01 + i1);
+    const float4 t011 = Vec4Load<ST>::load(F, r11 + i0), t111 = Vec4Load<ST>::load(F, r11 + i1);
+    float3 o;
+    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
+    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
+    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
+    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
+    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
+    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
+    return o;
+}
+
+}  // namespace tsf

@@ -75,6 +75,7 @@ def _declare(L):
         "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
+        "tsf_tdf_circle_mode": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _i, _p]),
         "tsf_candidates_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_candidates": (_i, [_p, _i, _p, _p, _i, _i, _i, _i, _f, _i, _p, _i64, _p, _p, _i64,
                                 _p, _p, _p, _sz, _p]),
@@ -208,13 +209,14 @@ def gvf_finish(v, storage: str = "f32", out=None, stream=None):
     return out
 
 
-def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, stream=None):
+def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, mode: int = 0,
+               stream=None):
     torch = _torch()
     Z, Y, X = field4.shape[:3]
     T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
     R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
-    _check(load().tsf_tdf_circle(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
-                                 float(rstep), _ptr(T), int(unorm16), _ptr(R), _stream(stream)))
+    _check(load().tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
+                                      float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
     return T, R
 
 
