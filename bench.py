@@ -358,12 +358,43 @@ def run_tsf(args, rank, world):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    res["fwd_adjoint"] = fwd_adjoint_timing(torch, pipe, args)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(args, vol)
     return res
+
+
+def fwd_adjoint_timing(torch, pipe, args):
+    """Forward (both TDF passes, GVF K iterations) and forward + hand-written
+    adjoint of the loss mean((T - G)^2) with respect to the volume, mu and
+    sigma (sqrt(K) checkpointing), FP32 storage, on the benchmark volume."""
+    import calibration as CAL
+    p = CAL.Params(mu=args.mu, sigma=PARAMS["large_blur"], iterations=args.iters, fmax=PARAMS["fmax"],
+                   rmin=PARAMS["rmin"], rmax=PARAMS["rmax"], rstep=PARAMS["rstep"])
+    vol = pipe.vol
+    G = torch.zeros_like(vol)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    CAL.forward(vol, p)
+    torch.cuda.synchronize()
+    ev[0].record()
+    Tc, state = CAL.forward(vol, p)
+    ev[1].record()
+    torch.cuda.synchronize()
+    ev[2].record()
+    Tc, state = CAL.forward(vol, p)
+    gT = ((2.0 / Tc.numel()) * (Tc - G)).contiguous()
+    gI, dmu, dsig = CAL.backward(state, gT, p)
+    ev[3].record()
+    torch.cuda.synchronize()
+    fwd = ev[0].elapsed_time(ev[1])
+    both = ev[2].elapsed_time(ev[3])
+    return {"storage": "f32", "iterations": args.iters, "volume": list(vol.shape),
+            "checkpoint_every": int(np.ceil(np.sqrt(args.iters))),
+            "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
+            "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
 
 
 def _traffic_from_profile(storage):

@@ -206,6 +206,31 @@ int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, 
 int tsf_tdf_combine(const void *d_T_small, const float *d_R_small, void *d_T_large,
                     float *d_R_large, int64_t n, int tdf_unorm16, void *stream);
 
+/* Reverse-mode derivative of tsf_tdf_circle (no counterpart in the
+ * reference): given d_gT = dL/dT (float per voxel), ADDS dL/d(field x,y,z) to
+ * d_gfield (planar FP32, 3N) -- through the trilinear samples at the arg-max
+ * radius, through the sample directions (eigenvectors of the Hessian, by
+ * first-order eigenvector perturbation) and through the Hessian's central
+ * differences (of v/|v| when rmax >= 4, w taken as |v|).  The arg-max radius
+ * is held fixed (sub-gradient of the max over radii). */
+size_t tsf_tdf_backward_workspace_size(int X, int Y, int Z);
+int tsf_tdf_circle_backward(const void *d_field4, int X, int Y, int Z, int storage, float rmin,
+                            float rmax, float rstep, const float *d_gT, float *d_gfield,
+                            void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Reverse-mode derivative of tsf_vector_field with respect to its input
+ * volume: ADDS to d_gin the gradient from d_gf (planar FP32 dL/df). */
+int tsf_vector_field_backward(const float *d_in, const float *d_gf, int X, int Y, int Z, float fmax,
+                              int vsign, float *d_gin, void *stream);
+
+/* Reverse-mode derivative of tsf_blur: ADDS the transposed blur of d_gout to
+ * d_gin and, when dsigma is not NULL, writes dL/dsigma (host, FP64; the call
+ * then synchronises `stream`). */
+size_t tsf_blur_backward_workspace_size(int X, int Y, int Z);
+int tsf_blur_backward(const float *d_in, const float *d_gout, int X, int Y, int Z, float sigma,
+                      float *d_gin, double *dsigma, void *d_workspace, size_t workspace_bytes,
+                      void *stream);
+
 /* ---------------------------------------------------------------------------
  * Candidate centerpoints
  * ------------------------------------------------------------------------- */

@@ -73,6 +73,11 @@ def _declare(L):
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
         "tsf_gvf_adjoint_workspace_size": (_sz, [_i, _i, _i, _i, _i, _i]),
         "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _p, _sz, _p]),
+        "tsf_tdf_backward_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_tdf_circle_backward": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _p, _sz, _p]),
+        "tsf_vector_field_backward": (_i, [_p, _p, _i, _i, _i, _f, _i, _p, _p]),
+        "tsf_blur_backward_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_blur_backward": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
         "tsf_tdf_circle_mode": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _i, _p]),
@@ -199,6 +204,39 @@ def gvf_adjoint(f0, mu: float, iterations: int, gv, storage: str = "f32", checkp
     _check(L.tsf_gvf_adjoint(_ptr(f0), X, Y, Z, float(mu), int(iterations), STORAGE[storage], _ptr(gv), _ptr(gf),
                              C.byref(dmu), int(checkpoint_every), _ptr(ws), ws.numel(), _stream(stream)))
     return gf, dmu.value
+
+
+def tdf_backward(field4, rmin, rmax, rstep, gT, storage: str = "f32", gfield=None, stream=None):
+    """Adds dL/d(field xyz) (planar float32) for dL/dT = gT; returns gfield."""
+    torch = _torch()
+    Z, Y, X = field4.shape[:3]
+    L = load()
+    gfield = torch.zeros((3, Z, Y, X), dtype=torch.float32, device=field4.device) if gfield is None else gfield
+    ws = workspace(L.tsf_tdf_backward_workspace_size(X, Y, Z))
+    _check(L.tsf_tdf_circle_backward(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax), float(rstep),
+                                     _ptr(gT), _ptr(gfield), _ptr(ws), ws.numel(), _stream(stream)))
+    return gfield
+
+
+def vector_field_backward(vol, gf, fmax, vsign=1, gin=None, stream=None):
+    torch = _torch()
+    X, Y, Z = _dims(vol)
+    gin = torch.zeros_like(vol) if gin is None else gin
+    _check(load().tsf_vector_field_backward(_ptr(vol), _ptr(gf), X, Y, Z, float(fmax), int(vsign), _ptr(gin),
+                                            _stream(stream)))
+    return gin
+
+
+def blur_backward(vol, gout, sigma, gin=None, stream=None):
+    torch = _torch()
+    X, Y, Z = _dims(vol)
+    L = load()
+    gin = torch.zeros_like(vol) if gin is None else gin
+    ws = workspace(L.tsf_blur_backward_workspace_size(X, Y, Z))
+    ds = C.c_double(0.0)
+    _check(L.tsf_blur_backward(_ptr(vol), _ptr(gout), X, Y, Z, float(sigma), _ptr(gin), C.byref(ds), _ptr(ws),
+                               ws.numel(), _stream(stream)))
+    return gin, ds.value
 
 
 def gvf_finish(v, storage: str = "f32", out=None, stream=None):
