@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--cpu-gvf-iters", type=int, default=6)
     ap.add_argument("--accuracy", action="store_true",
                     help="instead of timing: errors of every storage format against the FP64 oracle")
+    ap.add_argument("--fmg", action="store_true",
+                    help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
+    ap.add_argument("--fmg-cycles", type=int, default=10)
     return ap.parse_args()
 
 
@@ -391,7 +394,33 @@ def fwd_adjoint_timing(torch, pipe, args):
     torch.cuda.synchronize()
     fwd = ev[0].elapsed_time(ev[1])
     both = ev[2].elapsed_time(ev[3])
-    return {"storage": "f32", "iterations": args.iters, "volume": list(vol.shape),
+    # breakdown of the backward stages
+    import tsf_gb300 as T
+    small = state["small"]
+    gTs = torch.where(small, gT, torch.zeros_like(gT)).contiguous()
+    gTl = torch.where(small, torch.zeros_like(gT), gT).contiguous()
+    marks = []
+
+    def mark():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        marks.append(e)
+
+    mark()
+    g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, "f32")
+    mark()
+    g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, "f32")
+    mark()
+    g_f0, _ = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, "f32", ws=state["gvf_ws"], checkpoints_stored=True)
+    mark()
+    gI2 = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
+    g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)
+    T.blur_backward(vol, g_b, p.sigma, gin=gI2)
+    mark()
+    torch.cuda.synchronize()
+    names = ["tdf_small_backward", "tdf_large_backward", "gvf_adjoint", "vector_field_and_blur_backward"]
+    bw = {k: round(marks[i].elapsed_time(marks[i + 1]), 3) for i, k in enumerate(names)}
+    return {"storage": "f32", "iterations": args.iters, "volume": list(vol.shape), "backward_ms": bw,
             "checkpoint_every": int(np.ceil(np.sqrt(args.iters))),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
@@ -522,8 +551,74 @@ def run_accuracy(args):
     return out
 
 
+def run_fmg_workload(args):
+    """The 512x512x400 lung-airway CT (int16 HU, window [-1100, -600], dark
+    tubes: vsign -1) through the hot path with full-multigrid GVF (3 levels,
+    V-cycles) and FP16 storage; reported as ms per volume and per stage."""
+    import torch
+    import synthetic
+    import tsf_gb300 as T
+
+    shape = (400, 512, 512)
+    hu = synthetic.lung_ct(shape, seed=args.seed)
+    st = "f16"
+    L = T.load()
+    Z, Y, X = shape
+    dt = T.storage_dtype(st)
+    vol = torch.from_numpy(synthetic.window_to_unit(hu)).cuda()
+    P = dict(fmax=0.3, vsign=-1, blur=1.0, rmin=1.0, rmax=9.0, rstep=0.5, tdf_high=0.45, cube_size=4)
+    b = torch.empty_like(vol)
+    f4 = torch.empty((Z, Y, X, 4), dtype=dt, device="cuda")
+    f4s = torch.empty_like(f4)
+    out = torch.empty_like(f4)
+    ws = T.workspace(L.tsf_gvf_fmg_workspace_size(X, Y, Z, T.STORAGE[st]))
+    Ts = torch.empty_like(vol); Rs = torch.empty_like(vol); Tl = torch.empty_like(vol); Rl = torch.empty_like(vol)
+    cws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
+    verts = torch.zeros((1 << 16, 3), dtype=torch.int32, device="cuda")
+    import ctypes as C
+
+    def step(evs=None):
+        rec = (lambda: evs.append(torch.cuda.Event(enable_timing=True)) or evs[-1].record()) if evs is not None \
+            else (lambda: None)
+        rec()
+        T._check(L.tsf_vector_field(T._ptr(vol), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4s), T._stream()))
+        T._check(L.tsf_tdf_circle(T._ptr(f4s), X, Y, Z, T.STORAGE[st], P["rmin"], 3.0, 0.5, T._ptr(Ts), 0, T._ptr(Rs), T._stream()))
+        T.blur(vol, P["blur"], out=b)
+        T._check(L.tsf_vector_field(T._ptr(b), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4), T._stream()))
+        rec()
+        T._check(L.tsf_gvf_fmg(T._ptr(f4), T._ptr(out), X, Y, Z, 0.2, args.fmg_cycles, T.STORAGE[st], T._ptr(ws), ws.numel(), T._stream()))
+        rec()
+        T._check(L.tsf_tdf_circle(T._ptr(out), X, Y, Z, T.STORAGE[st], 2.5, P["rmax"], P["rstep"], T._ptr(Tl), 0, T._ptr(Rl), T._stream()))
+        T.tdf_combine(Ts, Rs, Tl, Rl)
+        rec()
+        nc, nv = C.c_int64(0), C.c_int64(0)
+        L.tsf_candidates(T._ptr(Tl), 0, T._ptr(Rl), T._ptr(out), T.STORAGE[st], X, Y, Z, P["tdf_high"], P["cube_size"],
+                         T._ptr(verts), 1 << 16, None, None, 0, C.byref(nc), C.byref(nv), T._ptr(cws), cws.numel(),
+                         T._stream())
+        rec()
+        return nc.value, nv.value
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    l0 = T.kernel_launches()
+    evs = []
+    nc, nv = step(evs)
+    torch.cuda.synchronize()
+    launches = T.kernel_launches() - l0
+    names = ["tdf_small_and_fields", "fmg_gvf", "tdf_large", "candidates"]
+    stages = {k: round(evs[i].elapsed_time(evs[i + 1]), 3) for i, k in enumerate(names)}
+    total = evs[0].elapsed_time(evs[-1])
+    return {"workload": "lung-airway CT 512x512x400, FMG GVF %d cycles x 3 components, FP16 storage" % args.fmg_cycles,
+            "ms_per_volume": round(total, 3), "volumes_per_s": round(1000.0 / total, 3), "stages_ms": stages,
+            "kernel_launches": int(launches), "n_candidates": nc, "n_vertices": nv}
+
+
 def main():
     args = parse()
+    if args.fmg:
+        print(json.dumps(run_fmg_workload(args)))
+        return
     if args.accuracy:
         print(json.dumps(run_accuracy(args)))
         return

@@ -170,10 +170,20 @@ size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iter
  * through the data term, |f0|^2 and v_0) to d_gf0 and dL/dmu to *dmu (host,
  * FP64; NULL to skip -- otherwise the call synchronises `stream`).  Forward
  * states are recomputed from checkpoints kept every `checkpoint_every`
- * iterations (<= 0: ceil(sqrt(iterations))); memory (K/C + C) states. */
+ * iterations (<= 0: ceil(sqrt(iterations))); memory (K/C + C) states.
+ * flags bit 0: the checkpoints are already in the workspace
+ * (tsf_gvf_checkpointed ran with the same arguments). */
 int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,
-                    const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every,
+                    const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every, int flags,
                     void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Forward GVF that also stores the adjoint's checkpoints in the workspace of
+ * tsf_gvf_adjoint (same sizes and interval); d_v (may be NULL) receives the
+ * result after `iterations` iterations.  A following tsf_gvf_adjoint call with
+ * flags bit 0 set reuses the checkpoints instead of recomputing them. */
+int tsf_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
+                         int storage, int checkpoint_every, void *d_workspace,
+                         size_t workspace_bytes, void *stream);
 
 /* GVF3DFinish (kernels.cl:1506-1515): packs the planar field into a field4
  * image with w = |v| (1 where |v| == 0). */

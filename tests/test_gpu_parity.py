@@ -64,12 +64,12 @@ def test_vector_field_bitexact(torch_dev, tsf, oracle, synth, storage, vsign):
 
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("mu,iters", [(0.05, 17), (0.1, 8)])
-@pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130)])
+@pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130), (9, 10, 256)])
 def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape):
-    """Odd x extents take the one-thread-per-voxel kernel, even ones the
-    vectorised kernel (several warps per row, a last warp with few lanes, the
-    8-voxel minimum, and X = 130, which the FP32 vector path hands back to the
-    per-voxel kernel)."""
+    """Odd x extents take the one-thread-per-voxel kernel, the others the
+    vectorised kernel: 16- or 8-byte vectors, full rows (X = 256) and ragged
+    ones (several warps per row, a last warp with few lanes, the smallest
+    rows), and X = 130, which goes back to the per-voxel kernel."""
     torch = torch_dev
     vol = oracle.blur(_vol(synth, shape, 4), 0.5)
     ref4 = oracle.vector_field(vol, 0.2, 1, storage)

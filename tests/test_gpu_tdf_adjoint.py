@@ -36,35 +36,60 @@ def _with_norm_w(field4):
     return f
 
 
+def _smooth_fd(f, h):
+    """Central difference of the scalar function f at 0, or None where f is not
+    smooth on [-2h, 2h] (a stopping decision or an eigenvector sign of the
+    reference's procedure changes there)."""
+    f0, fp, fm, fp2, fm2 = f(0.0), f(h), f(-h), f(2 * h), f(-2 * h)
+    d1 = (fp - fm) / (2 * h)
+    d2 = (fp2 - fm2) / (4 * h)
+    scale = max(abs(d1), 1e-6)
+    if abs(d1 - d2) > 1e-4 * scale or abs(f0 - 0.5 * (fp + fm)) > 1e-6 * max(1.0, abs(f0)):
+        return None
+    return d1
+
+
 @pytest.mark.parametrize("rng_", [(2.5, 7.0, 0.5), (1.0, 3.0, 0.5)])
 def test_tdf_backward_directional(torch_dev, tsf, oracle, synth, rng_):
+    """dT(x)/d(field) along random directions, one voxel at a time.  Voxels
+    next to a face are skipped: there the mirror rule makes a Hessian row
+    exactly zero and the reference's eigenvector signs jump."""
     torch = torch_dev
     field = _gvf_field(oracle, synth, (20, 22, 24), 3)
     if rng_[1] < 4:                          # small pass: un-normalised Hessian, w = 1
         field[..., 3] = 1.0
     f64 = _with_norm_w(field) if rng_[1] >= 4 else field.astype(np.float64)
     T0, _ = oracle.tdf_circle(f64, *rng_, f64=True)
-    rng = np.random.default_rng(4)
-    gT = (rng.normal(size=T0.shape) * (T0 > 0)).astype(np.float32)
     d4 = torch.from_numpy(f64.astype(np.float32)).cuda()
-    g = tsf.tdf_backward(d4, *rng_, torch.from_numpy(gT).cuda()).cpu().numpy().astype(np.float64)
-    rels = []
-    for trial in range(3):
-        D = rng.normal(size=(3,) + T0.shape)
-        h = 1e-6
+    rng = np.random.default_rng(4)
+    inner = np.zeros(T0.shape, bool)
+    inner[2:-2, 2:-2, 2:-2] = True
+    cand = np.argwhere((T0 > 0.05) & inner)
+    checked, bad = 0, []
+    for t in range(16):
+        z, y, x = cand[rng.integers(len(cand))]
+        gT = np.zeros(T0.shape, np.float32)
+        gT[z, y, x] = 1.0
+        g = tsf.tdf_backward(d4, *rng_, torch.from_numpy(gT).cuda()).cpu().numpy()
+        g = np.moveaxis(g, 0, -1).astype(np.float64)
+        D = rng.normal(size=f64.shape[:3] + (3,))
 
-        def L(sign):
+        def T_at(h):
             f = f64.copy()
-            f[..., :3] += sign * h * np.moveaxis(D, 0, -1)
+            f[..., :3] += h * D
             if rng_[1] >= 4:
                 f = _with_norm_w(f)
-            T, _ = oracle.tdf_circle(f, *rng_, f64=True)
-            return float((T * gT).sum())
+            return float(oracle.tdf_circle(f, *rng_, f64=True)[0][z, y, x])
 
-        fd = (L(1) - L(-1)) / (2 * h)
+        fd = _smooth_fd(T_at, 1e-6)
+        if fd is None:
+            continue
+        checked += 1
         an = float((g * D).sum())
-        rels.append(abs(fd - an) / max(abs(fd), 1e-12))
-    assert sorted(rels)[1] < 2e-3, rels          # median of three directions
+        if abs(fd - an) > 2e-3 * max(abs(fd), 1e-3):
+            bad.append(((z, y, x), fd, an))
+    assert checked >= 6, checked
+    assert not bad, bad
 
 
 def test_vector_field_backward_directional(torch_dev, tsf, oracle, synth):
@@ -86,8 +111,10 @@ def test_vector_field_backward_directional(torch_dev, tsf, oracle, synth):
     assert abs(fd - an) <= 1e-4 * abs(fd)
 
 
-@pytest.mark.parametrize("sigma", [0.5, 1.3])
+@pytest.mark.parametrize("sigma", [0.7, 1.3])
 def test_blur_backward_directional(torch_dev, tsf, oracle, synth, sigma):
+    """The mask width m = ceil(sigma / 0.5) jumps at multiples of 0.5, so sigma
+    is checked inside a constant-width interval."""
     torch = torch_dev
     vol = synth.vascular_tree((14, 16, 18), seed=6).astype(np.float32)
     rng = np.random.default_rng(6)
@@ -135,24 +162,35 @@ def _oracle_pipeline_T(oracle, vol, mu, sigma, iters):
 
 
 def test_pipeline_gradient_mu(torch_dev, tsf, oracle, synth):
-    """dL/dmu of the whole chain against an FP64 central difference."""
+    """dL/dmu of the whole chain (both TDF passes, GVF, vector field, blur)
+    against an FP64 central difference, for a loss on interior voxels whose
+    response is smooth in mu."""
     torch = torch_dev
     import calibration as CAL
     shape = (20, 20, 24)
     vol, truth = synth.vascular_tree(shape, seed=8, with_truth=True)
     G = synth.centerline_gaussian(shape, truth["points"], 1.0)
-    p = CAL.Params(mu=0.05, sigma=0.5, iterations=16)
-    L, gI, dmu, dsig = CAL.loss_and_grad(torch.from_numpy(vol).cuda(), torch.from_numpy(G).cuda(), p)
-    hm = 2.0 ** -12
+    p = CAL.Params(mu=0.05, sigma=0.7, iterations=16)
+    Tc, state = CAL.forward(torch.from_numpy(vol).cuda(), p)
+    T = Tc.cpu().numpy()
+    inner = np.zeros(shape, bool)
+    inner[2:-2, 2:-2, 2:-2] = True
+    rng = np.random.default_rng(3)
+    cand = np.argwhere((T > 0.1) & inner)
+    sel = cand[rng.choice(len(cand), size=min(12, len(cand)), replace=False)]
+    mask = np.zeros(shape, bool)
+    mask[tuple(sel.T)] = True
+    gT = np.where(mask, 2.0 * (T - G), 0.0).astype(np.float32)
+    _, dmu, _ = CAL.backward(state, torch.from_numpy(gT).cuda(), p)
 
-    def Lo(mu):
-        T = _oracle_pipeline_T(oracle, vol, mu, 0.5, 16)
-        return float(((T - G) ** 2).mean())
+    def Lo(dm):
+        mu = float(np.float32(0.05 + dm))
+        To = _oracle_pipeline_T(oracle, vol, mu, 0.7, 16)
+        return float(((To - G) ** 2)[mask].sum())
 
-    mp, mm = float(np.float32(0.05 + hm)), float(np.float32(0.05 - hm))
-    fd = (Lo(mp) - Lo(mm)) / (mp - mm)
-    assert abs(fd - dmu) <= 0.02 * abs(fd) + 1e-9, (fd, dmu)
-    assert np.isfinite(gI.cpu().numpy()).all()
+    fd = _smooth_fd(Lo, 2.0 ** -16)
+    assert fd is not None
+    assert abs(fd - dmu) <= 0.01 * abs(fd) + 1e-7, (fd, dmu)
 
 
 def test_calibration_reduces_loss(torch_dev, tsf, synth):

@@ -38,12 +38,13 @@ def forward(vol, p: Params):
     Ts, Rs = T.tdf_circle(f_s, p.rmin, 3.0, 0.5, st)
     b = T.blur(vol, p.sigma)
     f0, _ = T.vector_field(b, p.fmax, p.vsign, st, planar=True, field4=False)
-    v = T.gvf(f0, p.mu, p.iterations, st)
+    ws = T.gvf_adjoint_workspace(f0, p.iterations, st, p.checkpoint_every)
+    v = T.gvf_checkpointed(f0, p.mu, p.iterations, ws, st, p.checkpoint_every)
     F = T.gvf_finish(v, st)
     Tl, Rl = T.tdf_circle(F, max(2.5, p.rmin), p.rmax, p.rstep, st)
     small = Ts > Tl                       # combine (kernels.cl:561-572): T_l < T_s -> take T_s
     Tc = torch.where(small, Ts, Tl)
-    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small)
+    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small, gvf_ws=ws)
     return Tc, s
 
 
@@ -60,7 +61,8 @@ def backward(state, gT, p: Params):
     gI = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
     # large pass -> GVF -> vector field -> blur
     g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, st)
-    g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, p.checkpoint_every)
+    g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, p.checkpoint_every, ws=state["gvf_ws"],
+                              checkpoints_stored=True)
     g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)
     gI, dsigma = T.blur_backward(vol, g_b, p.sigma, gin=gI)
     return gI, dmu, dsigma

@@ -73,173 +73,148 @@ __global__ void __launch_bounds__(256) gvf_plain_kernel(const typename Store<ST>
 // and the last chunk is shifted to end at Z, so those pairs never straddle a
 // chunk).  Per voxel the arithmetic is exactly gvf_plain_kernel's.
 // ---------------------------------------------------------------------------
-template <int ST, int VX> struct VecIO;
-
-template <int ST> struct VecIO<ST, 4> {
+// BYTES (8 or 16) bytes of stored components -- 4 or 8 voxels of a 16-bit
+// format, 2 or 4 of FP32 -- unpacked / packed two at a time with the paired
+// conversion intrinsics.
+template <int ST, int BYTES> struct PackedV {
     using T = typename Store<ST>::T;
-    static __device__ __forceinline__ void load(const T *p, float o[4]) {
-        if constexpr (ST == TSF_STORE_F32) {
-            const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
-            o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    static constexpr int VX = BYTES / (int)sizeof(T);
+    static constexpr int W = BYTES / 4;              // 32-bit words
+    struct Raw { unsigned u[W]; };
+    static __device__ __forceinline__ Raw load(const T *p) {
+        Raw r;
+        if constexpr (BYTES == 16) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+            r.u[0] = v.x; r.u[1] = v.y; r.u[2] = v.z; r.u[3] = v.w;
         } else {
-            const uint2 raw = __ldg(reinterpret_cast<const uint2 *>(p));
-            T c[4];
-            memcpy(c, &raw, 8);
+            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
+            r.u[0] = v.x; r.u[1] = v.y;
+        }
+        return r;
+    }
+    static __device__ __forceinline__ Raw zero() {
+        Raw r;
 #pragma unroll
-            for (int i = 0; i < 4; i++) o[i] = Store<ST>::load(c[i]);
-        }
+        for (int i = 0; i < W; i++) r.u[i] = 0u;
+        return r;
     }
-    static __device__ __forceinline__ void store(T *p, const float o[4]) {
-        if constexpr (ST == TSF_STORE_F32) {
-            *reinterpret_cast<float4 *>(p) = make_float4(o[0], o[1], o[2], o[3]);
-        } else {
-            T c[4];
+    static __device__ __forceinline__ void unpack(const Raw &raw, float o[VX]) {
 #pragma unroll
-            for (int i = 0; i < 4; i++) c[i] = Store<ST>::store(o[i]);
-            uint2 raw;
-            memcpy(&raw, c, 8);
-            *reinterpret_cast<uint2 *>(p) = raw;
-        }
-    }
-};
-
-template <int ST> struct VecIO<ST, 2> {
-    using T = typename Store<ST>::T;
-    static __device__ __forceinline__ void load(const T *p, float o[2]) {
-        if constexpr (ST == TSF_STORE_F32) {
-            const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
-            o[0] = v.x; o[1] = v.y;
-        } else {
-            const unsigned raw = __ldg(reinterpret_cast<const unsigned *>(p));
-            T c[2];
-            memcpy(c, &raw, 4);
-            o[0] = Store<ST>::load(c[0]);
-            o[1] = Store<ST>::load(c[1]);
-        }
-    }
-    static __device__ __forceinline__ void store(T *p, const float o[2]) {
-        if constexpr (ST == TSF_STORE_F32) {
-            *reinterpret_cast<float2 *>(p) = make_float2(o[0], o[1]);
-        } else {
-            T c[2] = {Store<ST>::store(o[0]), Store<ST>::store(o[1])};
-            unsigned raw;
-            memcpy(&raw, c, 4);
-            *reinterpret_cast<unsigned *>(p) = raw;
-        }
-    }
-};
-
-// Eight bytes of stored components: 4 voxels of a 16-bit format or 2 of FP32,
-// unpacked / packed two at a time with the paired conversion intrinsics.
-template <int ST> struct Packed8 {
-    using T = typename Store<ST>::T;
-    static constexpr int VX = 8 / (int)sizeof(T);
-    static __device__ __forceinline__ uint2 load(const T *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
-    static __device__ __forceinline__ void unpack(uint2 raw, float o[VX]) {
-        if constexpr (ST == TSF_STORE_F32) {
-            o[0] = __uint_as_float(raw.x);
-            o[1] = __uint_as_float(raw.y);
-        } else if constexpr (ST == TSF_STORE_F16) {
-            const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&raw.x));
-            const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&raw.y));
-            o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
-        } else if constexpr (ST == TSF_STORE_BF16) {
-            o[0] = __uint_as_float(raw.x << 16);
-            o[1] = __uint_as_float(raw.x & 0xffff0000u);
-            o[2] = __uint_as_float(raw.y << 16);
-            o[3] = __uint_as_float(raw.y & 0xffff0000u);
-        } else {
-            o[0] = Store<ST>::load((int16_t)(raw.x & 0xffffu));
-            o[1] = Store<ST>::load((int16_t)(raw.x >> 16));
-            o[2] = Store<ST>::load((int16_t)(raw.y & 0xffffu));
-            o[3] = Store<ST>::load((int16_t)(raw.y >> 16));
+        for (int k = 0; k < W; k++) {
+            const unsigned u = raw.u[k];
+            if constexpr (ST == TSF_STORE_F32) {
+                o[k] = __uint_as_float(u);
+            } else if constexpr (ST == TSF_STORE_F16) {
+                const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u));
+                o[2 * k] = a.x; o[2 * k + 1] = a.y;
+            } else if constexpr (ST == TSF_STORE_BF16) {
+                o[2 * k] = __uint_as_float(u << 16);
+                o[2 * k + 1] = __uint_as_float(u & 0xffff0000u);
+            } else {
+                o[2 * k] = Store<ST>::load((int16_t)(u & 0xffffu));
+                o[2 * k + 1] = Store<ST>::load((int16_t)(u >> 16));
+            }
         }
     }
     // rounds to the storage format (the only rounding of an iteration's result)
     static __device__ __forceinline__ void store(T *p, const float o[VX]) {
-        uint2 raw;
-        if constexpr (ST == TSF_STORE_F32) {
-            raw.x = __float_as_uint(o[0]);
-            raw.y = __float_as_uint(o[1]);
-        } else if constexpr (ST == TSF_STORE_F16) {
-            const __half2 a = __floats2half2_rn(o[0], o[1]), b = __floats2half2_rn(o[2], o[3]);
-            raw.x = *reinterpret_cast<const unsigned *>(&a);
-            raw.y = *reinterpret_cast<const unsigned *>(&b);
-        } else if constexpr (ST == TSF_STORE_BF16) {
-            const __nv_bfloat162 a = __floats2bfloat162_rn(o[0], o[1]), b = __floats2bfloat162_rn(o[2], o[3]);
-            raw.x = *reinterpret_cast<const unsigned *>(&a);
-            raw.y = *reinterpret_cast<const unsigned *>(&b);
-        } else {
-            T c[VX];
+        unsigned u[W];
 #pragma unroll
-            for (int i = 0; i < VX; i++) c[i] = Store<ST>::store(o[i]);
-            memcpy(&raw, c, 8);
+        for (int k = 0; k < W; k++) {
+            if constexpr (ST == TSF_STORE_F32) {
+                u[k] = __float_as_uint(o[k]);
+            } else if constexpr (ST == TSF_STORE_F16) {
+                const __half2 h = __floats2half2_rn(o[2 * k], o[2 * k + 1]);
+                u[k] = *reinterpret_cast<const unsigned *>(&h);
+            } else if constexpr (ST == TSF_STORE_BF16) {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(o[2 * k], o[2 * k + 1]);
+                u[k] = *reinterpret_cast<const unsigned *>(&h);
+            } else {
+                const int16_t lo = Store<ST>::store(o[2 * k]), hi = Store<ST>::store(o[2 * k + 1]);
+                u[k] = (unsigned)(uint16_t)lo | ((unsigned)(uint16_t)hi << 16);
+            }
         }
-        *reinterpret_cast<uint2 *>(p) = raw;
+        if constexpr (BYTES == 16) *reinterpret_cast<uint4 *>(p) = make_uint4(u[0], u[1], u[2], u[3]);
+        else *reinterpret_cast<uint2 *>(p) = make_uint2(u[0], u[1]);
     }
 };
 
-// One thread = the VX voxels of one 8-byte vector of one row of one plane.
-// All loads of a thread are independent and issued together -- per component
-// the centre vector and its y+-1 and z+-1 neighbours, plus the f0 vectors --
-// and stay packed in registers until used, so a warp keeps 18 eight-byte
-// loads in flight at ~40 registers.  The neighbour vectors are other threads'
-// centre vectors, served by L1/L2, so HBM still sees each stored component
-// once.  x-neighbours come from the adjacent lanes by shuffles.  Mirror rule:
-// rows and planes are computed at mirror(y), mirror(z); the vector holding
-// x = 0 / X-1 copies the result of x = 2 / X-3 (needs VX >= 3, or the
-// neighbouring vector, see below).  Per voxel the arithmetic is exactly
-// gvf_plain_kernel's.
-template <int ST>
+// One thread = the VX voxels of one vector (BYTES bytes) of one row of one
+// plane.  All loads of a thread are independent and issued together -- per
+// component the centre vector and its y+-1 and z+-1 neighbours, plus the f0
+// vectors -- and stay packed in registers until used.  The neighbour vectors
+// are other threads' centre vectors, served by L1/L2, so HBM sees each stored
+// component once.  x-neighbours come from the adjacent lanes by shuffles (the
+// first / last lane of a warp reads its one outside neighbour itself).  FULL:
+// every lane of every warp holds a vector (X / VX a multiple of 32), so no
+// per-lane activity test is needed.  Mirror rule: rows and planes are computed
+// at mirror(y), mirror(z); the vector holding x = 0 / X-1 copies the result of
+// x = 2 / X-3.  Per voxel the arithmetic is exactly gvf_plain_kernel's.
+template <int ST, int BYTES, bool FULL>
 __global__ void __launch_bounds__(256) gvf_vec_kernel(const typename Store<ST>::T *__restrict__ f,
                                                       const typename Store<ST>::T *__restrict__ src,
                                                       typename Store<ST>::T *__restrict__ dst, int X, int Y, int Z,
                                                       float mu) {
     using T = typename Store<ST>::T;
-    using P = Packed8<ST>;
+    using P = PackedV<ST, BYTES>;
+    using Raw = typename P::Raw;
     constexpr int VX = P::VX;
+    static_assert(VX >= 4, "the x-boundary copy needs x = 2 in the first vector");
     const int lane = threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z;
     if (y >= Y) return;                              // whole warp
     const int x0 = (blockIdx.x * 32 + lane) * VX;
-    const bool act = x0 < X;
+    const bool act = FULL || x0 < X;
     const int py = mirror(y, Y), pz = mirror(z, Z);
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
     const int64_t p = (int64_t)pz * plane + (int64_t)py * X + x0;
     const unsigned full = 0xffffffffu;
 
-    uint2 rf[3], rc[3], ryp[3], rym[3], rzp[3], rzm[3];
-    const uint2 zero = make_uint2(0u, 0u);
+    Raw rf[3], rc[3], ryp[3], rym[3], rzp[3], rzm[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const T *s = src + c * n + p;
-        rf[c] = act ? P::load(f + c * n + p) : zero;
-        rc[c] = act ? P::load(s) : zero;
-        ryp[c] = act ? P::load(s + X) : zero;
-        rym[c] = act ? P::load(s - X) : zero;
-        rzp[c] = act ? P::load(s + plane) : zero;
-        rzm[c] = act ? P::load(s - plane) : zero;
+        const T *sp = src + c * n + p;
+        if (act) {
+            rf[c] = P::load(f + c * n + p);
+            rc[c] = P::load(sp);
+            ryp[c] = P::load(sp + X);
+            rym[c] = P::load(sp - X);
+            rzp[c] = P::load(sp + plane);
+            rzm[c] = P::load(sp - plane);
+        } else {
+            rf[c] = rc[c] = ryp[c] = rym[c] = rzp[c] = rzm[c] = P::zero();
+        }
     }
-    float fv[3][VX], sqr[VX];
+    float sqr[VX];
+    {
+        float f0[VX], f1[VX], f2[VX];
+        P::unpack(rf[0], f0);
+        P::unpack(rf[1], f1);
+        P::unpack(rf[2], f2);
 #pragma unroll
-    for (int c = 0; c < 3; c++) P::unpack(rf[c], fv[c]);
-#pragma unroll
-    for (int i = 0; i < VX; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+        for (int i = 0; i < VX; i++) sqr[i] = (f0[i] * f0[i] + f1[i] * f1[i]) + f2[i] * f2[i];
+    }
     const int64_t o = (int64_t)z * plane + (int64_t)y * X + x0;
+    // the lanes at a warp's edge read their outside x-neighbour themselves
+    const bool left_out = lane == 0 && act && x0 > 0;
+    const bool right_out = lane == 31 && act && x0 + VX < X;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        float cc[VX], yp[VX], ym[VX], zp[VX], zm[VX];
+        const T *sp = src + c * n + p;
+        const float xl_edge = left_out ? Store<ST>::load(sp[-1]) : 0.0f;
+        const float xr_edge = right_out ? Store<ST>::load(sp[VX]) : 0.0f;
+        float cc[VX], yp[VX], ym[VX], zp[VX], zm[VX], fc[VX];
         P::unpack(rc[c], cc);
         P::unpack(ryp[c], yp);
         P::unpack(rym[c], ym);
         P::unpack(rzp[c], zp);
         P::unpack(rzm[c], zm);
-        // x-neighbours: the last voxel of the lane to the left, the first of the lane to the right
+        P::unpack(rf[c], fc);
         float xl = __shfl_up_sync(full, cc[VX - 1], 1);
         float xr = __shfl_down_sync(full, cc[0], 1);
-        if (lane == 0) xl = (act && x0 > 0) ? Store<ST>::load(src[c * n + p - 1]) : 0.0f;
-        if (lane == 31) xr = (act && x0 + VX < X) ? Store<ST>::load(src[c * n + p + VX]) : 0.0f;
+        xl = lane == 0 ? xl_edge : xl;
+        xr = lane == 31 ? xr_edge : xr;
         float res[VX];
 #pragma unroll
         for (int i = 0; i < VX; i++) {
@@ -251,20 +226,11 @@ __global__ void __launch_bounds__(256) gvf_vec_kernel(const typename Store<ST>::
             lap = lap + ym[i];
             lap = lap + zp[i];
             lap = lap + zm[i];
-            const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+            const float upd = mu * lap - (v - fc[i]) * sqr[i];
             res[i] = v + upd;                        // rounded to storage by the store
         }
-        if constexpr (VX >= 3) {
-            if (x0 == 0) res[0] = res[2];
-            if (x0 + VX == X) res[VX - 1] = res[VX - 3];
-        } else {
-            // VX == 2: x = 0 takes x = 2 (first voxel of the next lane), x = X-1
-            // takes x = X-3 (last voxel of the previous lane)
-            const float r_next0 = __shfl_down_sync(full, res[0], 1);
-            const float r_prev1 = __shfl_up_sync(full, res[1], 1);
-            if (x0 == 0) res[0] = (lane == 31) ? 0.0f : r_next0;
-            if (x0 + VX == X) res[1] = (lane == 0) ? 0.0f : r_prev1;
-        }
+        if (x0 == 0) res[0] = res[2];
+        if (x0 + VX == X) res[VX - 1] = res[VX - 3];
         if (act) P::store(dst + c * n + o, res);
     }
 }
@@ -293,16 +259,35 @@ size_t gvf_workspace_size(int X, int Y, int Z, int st) {
 
 constexpr int kVecBY = 8;
 
+template <int ST, int BYTES>
+static void launch_vec(const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s) {
+    using T = typename Store<ST>::T;
+    constexpr int VX = PackedV<ST, BYTES>::VX;
+    const int nvec = X / VX;
+    dim3 b(32, kVecBY), g((nvec + 31) / 32, (Y + kVecBY - 1) / kVecBY, Z);
+    if (nvec % 32 == 0)
+        gvf_vec_kernel<ST, BYTES, true><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst, X, Y, Z, mu);
+    else
+        gvf_vec_kernel<ST, BYTES, false><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst, X, Y, Z, mu);
+}
+
 static int launch_gvf_plain(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z,
                             float mu, cudaStream_t s) {
-    const int vx = st == TSF_STORE_F32 ? 2 : 4;     // voxels per 8-byte vector
-    // the x-boundary copy needs the vector holding x = 2 / X-3 in the same warp
-    if (X % vx == 0 && X >= 8 && !(vx == 2 && X % 64 == 2)) {
-        dim3 b(32, kVecBY), g((X / vx + 31) / 32, (Y + kVecBY - 1) / kVecBY, Z);
-        TSF_DISPATCH_STORAGE(st, ST, {
-            using T = typename Store<ST>::T;
-            gvf_vec_kernel<ST><<<g, b, 0, s>>>((const T *)d_f0, (const T *)src, (T *)dst, X, Y, Z, mu);
-        });
+    // 16-byte vectors when the row splits into them, else 8-byte ones (FP32
+    // 8-byte vectors hold 2 voxels, too few for the in-vector boundary copy)
+    const int es = (int)storage_bytes(st);
+    const int vx16 = 16 / es, vx8 = 8 / es;
+    if (X % vx16 == 0 && X >= 2 * vx16) {
+        TSF_DISPATCH_STORAGE(st, ST, launch_vec<ST, 16>(d_f0, src, dst, X, Y, Z, mu, s));
+        TSF_CHECK_LAUNCH("gvf_vec_kernel");
+        return TSF_OK;
+    }
+    if (es == 2 && X % vx8 == 0 && X >= 2 * vx8) {
+        switch (st) {
+        case TSF_STORE_F16: launch_vec<TSF_STORE_F16, 8>(d_f0, src, dst, X, Y, Z, mu, s); break;
+        case TSF_STORE_BF16: launch_vec<TSF_STORE_BF16, 8>(d_f0, src, dst, X, Y, Z, mu, s); break;
+        default: launch_vec<TSF_STORE_SNORM16, 8>(d_f0, src, dst, X, Y, Z, mu, s); break;
+        }
         TSF_CHECK_LAUNCH("gvf_vec_kernel");
         return TSF_OK;
     }

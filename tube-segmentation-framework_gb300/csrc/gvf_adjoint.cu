@@ -64,11 +64,16 @@ __global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__re
                                                                const typename Store<ST>::T *__restrict__ f,
                                                                float *__restrict__ lam_out, float *__restrict__ gf,
                                                                double *__restrict__ dmu_block, int X, int Y, int Z,
-                                                               float mu) {
+                                                               float mu, int skip_fast) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    const bool in = x < X && y < Y && z < Z;
+    bool in = x < X && y < Y && z < Z;
+    if (skip_fast) {
+        // voxels of the 4-voxel vectors that gvf_adjoint_vec_kernel handled
+        const int x0 = x & ~3;
+        if (y >= 3 && y <= Y - 4 && z >= 3 && z <= Z - 4 && x0 >= 4 && x0 + 4 <= X - 4) in = false;
+    }
     const int64_t n = (int64_t)X * Y * Z;
     double dmu = 0.0;
     if (in) {
@@ -124,6 +129,111 @@ __global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__re
     }
 }
 
+// Interior fast path of the adjoint step: every thread owns 4 consecutive
+// voxels of a row whose whole stencil lies at least 3 voxels inside every
+// face, where the folded cotangent equals lambda' itself.  Vector loads of
+// lambda' (FP32) and of the stored states, x-neighbours by shuffles, the
+// same formulas as gvf_adjoint_step_kernel.  Threads with any voxel near a
+// face write nothing; gvf_adjoint_step_kernel (skip_fast) covers those voxels.
+template <int ST>
+__global__ void __launch_bounds__(256) gvf_adjoint_vec_kernel(const float *__restrict__ lam_in,
+                                                              const typename Store<ST>::T *__restrict__ v,
+                                                              const typename Store<ST>::T *__restrict__ f,
+                                                              float *__restrict__ lam_out, float *__restrict__ gf,
+                                                              double *__restrict__ dmu_block, int X, int Y, int Z,
+                                                              float mu) {
+    using T = typename Store<ST>::T;
+    constexpr int VX = 4;
+    const int lane = threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const int x0 = (blockIdx.x * 32 + lane) * VX;
+    const bool act = y < Y && x0 < X;
+    const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
+    const unsigned full = 0xffffffffu;
+    const bool fast = act && y >= 3 && y <= Y - 4 && z >= 3 && z <= Z - 4 && x0 >= 4 && x0 + VX <= X - 4;
+    double dmu = 0.0;
+    const int64_t q = (int64_t)z * plane + (int64_t)y * X + x0;
+    auto ld4 = [](const float *p, float o[VX]) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+        o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+    };
+    auto ldv = [](const T *p, float o[VX]) {
+#pragma unroll
+        for (int i = 0; i < VX; i++) o[i] = Store<ST>::load(p[i]);
+    };
+    float fv[3][VX], s[VX], gd[VX];
+    float gc[3][VX];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (act) ldv(f + c * n + q, fv[c]);
+        else for (int i = 0; i < VX; i++) fv[c][i] = 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < VX; i++) {
+        s[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+        gd[i] = 0.0f;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float *lp = lam_in + c * n + q;
+        const T *vp = v + c * n + q;
+        float g[VX], gyp[VX], gym[VX], gzp[VX], gzm[VX], vv[VX], vyp[VX], vym[VX], vzp[VX], vzm[VX];
+        if (act) {
+            ld4(lp, g); ld4(lp + X, gyp); ld4(lp - X, gym); ld4(lp + plane, gzp); ld4(lp - plane, gzm);
+            ldv(vp, vv);
+            if (fast) { ldv(vp + X, vyp); ldv(vp - X, vym); ldv(vp + plane, vzp); ldv(vp - plane, vzm); }
+        } else {
+            for (int i = 0; i < VX; i++) g[i] = gyp[i] = gym[i] = gzp[i] = gzm[i] = vv[i] = 0.0f;
+        }
+        float gl = __shfl_up_sync(full, g[VX - 1], 1), gr = __shfl_down_sync(full, g[0], 1);
+        float vl = __shfl_up_sync(full, vv[VX - 1], 1), vr = __shfl_down_sync(full, vv[0], 1);
+        if (fast && lane == 0) { gl = lp[-1]; vl = Store<ST>::load(vp[-1]); }
+        if (fast && lane == 31) { gr = lp[VX]; vr = Store<ST>::load(vp[VX]); }
+        if (fast) {
+            float out[VX];
+#pragma unroll
+            for (int i = 0; i < VX; i++) {
+                const float xp = i == VX - 1 ? gr : g[i + 1 < VX ? i + 1 : i];
+                const float xm = i == 0 ? gl : g[i > 0 ? i - 1 : 0];
+                const float nb = ((((xp + xm) + gyp[i]) + gym[i]) + gzp[i]) + gzm[i];
+                out[i] = g[i] * (1.0f - 6.0f * mu - s[i]) + mu * nb;
+                const float vxp = i == VX - 1 ? vr : vv[i + 1 < VX ? i + 1 : i];
+                const float vxm = i == 0 ? vl : vv[i > 0 ? i - 1 : 0];
+                const float L = (((((vxp + vxm) + vyp[i]) + vym[i]) + vzp[i]) + vzm[i]) - 6.0f * vv[i];
+                dmu += (double)(g[i] * L);
+                gd[i] += g[i] * (vv[i] - fv[c][i]);
+                gc[c][i] = g[i];
+            }
+            *reinterpret_cast<float4 *>(lam_out + c * n + q) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+    }
+    if (fast) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float4 *gp = reinterpret_cast<float4 *>(gf + c * n + q);
+            float4 a = *gp;
+            a.x += gc[c][0] * s[0] - 2.0f * fv[c][0] * gd[0];
+            a.y += gc[c][1] * s[1] - 2.0f * fv[c][1] * gd[1];
+            a.z += gc[c][2] * s[2] - 2.0f * fv[c][2] * gd[2];
+            a.w += gc[c][3] * s[3] - 2.0f * fv[c][3] * gd[3];
+            *gp = a;
+        }
+    }
+    // per-block FP64 partial of dL/dmu, accumulated over the steps in a fixed order
+    __shared__ double red[8];
+    const int t = threadIdx.x + blockDim.x * threadIdx.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dmu += __shfl_down_sync(full, dmu, o);
+    if ((t & 31) == 0) red[t >> 5] = dmu;
+    __syncthreads();
+    if (t == 0) {
+        double sum = 0.0;
+        for (int i = 0; i < (int)(blockDim.x * blockDim.y) / 32; i++) sum += red[i];
+        dmu_block[blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z)] += sum;
+    }
+}
+
 __global__ void add_planar_kernel(float *__restrict__ a, const float *__restrict__ b, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] += b[i];
@@ -152,8 +262,11 @@ struct AdjLayout {
     int64_t nblocks;
 };
 
+static bool adj_vec(int X) { return X % 4 == 0; }
 static dim3 adj_block() { return dim3(32, 4, 2); }
 static dim3 adj_grid(int X, int Y, int Z) { return dim3((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2); }
+static dim3 adjv_block() { return dim3(32, 8, 1); }
+static dim3 adjv_grid(int X, int Y, int Z) { return dim3((X / 4 + 31) / 32, (Y + 7) / 8, Z); }
 
 static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
     AdjLayout L;
@@ -165,8 +278,8 @@ static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
     L.nck = K > 0 ? (K + C - 1) / C : 0;
     const size_t n = (size_t)X * Y * Z;
     L.state = al256(3 * n * storage_bytes(st));
-    const dim3 g = adj_grid(X, Y, Z);
-    L.nblocks = (int64_t)g.x * g.y * g.z;
+    const dim3 g = adj_grid(X, Y, Z), gv = adjv_grid(X, Y, Z);
+    L.nblocks = (int64_t)g.x * g.y * g.z + (adj_vec(X) ? (int64_t)gv.x * gv.y * gv.z : 0);
     size_t off = 0;
     L.ck = off; off += L.state * (size_t)L.nck;
     L.seg = off; off += L.state * (size_t)C;
@@ -183,8 +296,42 @@ size_t gvf_adjoint_workspace_size(int X, int Y, int Z, int st, int K, int C) {
     return adj_layout(X, Y, Z, st, K, C).bytes;
 }
 
+// Forward pass keeping the checkpoints v_0, v_C, ... in the adjoint workspace;
+// the result v_K goes to d_v (may be NULL).
+int run_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int K, int st, int C, void *ws,
+                         size_t ws_bytes, cudaStream_t s) {
+    int r = check_dims(X, Y, Z);
+    if (r) return r;
+    if (!valid_storage(st)) return fail(TSF_ERR_INVALID_ARG, "unknown storage format");
+    if (!d_f0) return fail(TSF_ERR_INVALID_ARG, "null buffer");
+    if (K < 0) return fail(TSF_ERR_INVALID_ARG, "iterations must be >= 0");
+    const AdjLayout L = adj_layout(X, Y, Z, st, K, C);
+    if (!ws || ws_bytes < L.bytes) return fail(TSF_ERR_WORKSPACE, "GVF adjoint workspace too small");
+    char *w = (char *)ws;
+    const size_t state_bytes = 3 * (size_t)X * Y * Z * storage_bytes(st);
+    void *gws = w + L.gvf_ws;
+    const size_t gws_bytes = gvf_workspace_size(X, Y, Z, st);
+    for (int i = 0; i < L.nck; i++) {
+        void *ck = w + L.ck + (size_t)i * L.state;
+        const void *prev = i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
+        TSF_TRY_CUDA(cudaMemcpyAsync(ck, prev, state_bytes, cudaMemcpyDeviceToDevice, s));
+        if (i > 0) {
+            r = run_gvf(d_f0, ck, X, Y, Z, mu, L.C, st, gws, gws_bytes, 0, s);
+            if (r) return r;
+        }
+    }
+    if (d_v) {
+        const void *last = L.nck > 0 ? (const void *)(w + L.ck + (size_t)(L.nck - 1) * L.state) : d_f0;
+        TSF_TRY_CUDA(cudaMemcpyAsync(d_v, last, state_bytes, cudaMemcpyDeviceToDevice, s));
+        const int done = L.nck > 0 ? (L.nck - 1) * L.C : 0;
+        r = run_gvf(d_f0, d_v, X, Y, Z, mu, K - done, st, gws, gws_bytes, 0, s);
+        if (r) return r;
+    }
+    return TSF_OK;
+}
+
 int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int st, const float *d_gv, float *d_gf0,
-                    double *dmu_host, int C, void *ws, size_t ws_bytes, cudaStream_t s) {
+                    double *dmu_host, int C, int flags, void *ws, size_t ws_bytes, cudaStream_t s) {
     int r = check_dims(X, Y, Z);
     if (r) return r;
     if (!valid_storage(st)) return fail(TSF_ERR_INVALID_ARG, "unknown storage format");
@@ -204,8 +351,9 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
     void *gws = w + L.gvf_ws;
     const size_t gws_bytes = gvf_workspace_size(X, Y, Z, st);
 
-    // forward pass keeping checkpoints v_0, v_C, ...
-    for (int i = 0; i < L.nck; i++) {
+    // forward pass keeping checkpoints v_0, v_C, ... (unless a checkpointed
+    // forward already stored them)
+    for (int i = 0; i < L.nck && !(flags & 1); i++) {
         void *ck = w + L.ck + (size_t)i * L.state;
         const void *prev = i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
         TSF_TRY_CUDA(cudaMemcpyAsync(ck, prev, state_bytes, cudaMemcpyDeviceToDevice, s));
@@ -230,12 +378,18 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
         }
         for (int k = k1 - 1; k >= k0; k--) {
             const void *vk = w + L.seg + (size_t)(k - k0) * L.state;
+            const dim3 g = adj_grid(X, Y, Z);
+            double *dmu_v = dmu_b + (int64_t)g.x * g.y * g.z;
+            const bool vec = adj_vec(X);
             TSF_DISPATCH_STORAGE(st, ST, {
                 using T = typename Store<ST>::T;
-                gvf_adjoint_step_kernel<ST><<<adj_grid(X, Y, Z), adj_block(), 0, s>>>(
-                    lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_b, X, Y, Z, mu);
+                if (vec)
+                    gvf_adjoint_vec_kernel<ST><<<adjv_grid(X, Y, Z), adjv_block(), 0, s>>>(
+                        lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu);
+                gvf_adjoint_step_kernel<ST><<<g, adj_block(), 0, s>>>(lam, (const T *)vk, (const T *)d_f0, lam2,
+                                                                     d_gf0, dmu_b, X, Y, Z, mu, vec ? 1 : 0);
             });
-            TSF_CHECK_LAUNCH("gvf_adjoint_step_kernel");
+            TSF_CHECK_LAUNCHES("gvf_adjoint_step_kernel", vec ? 2 : 1);
             float *t = lam; lam = lam2; lam2 = t;
         }
     }
@@ -262,8 +416,15 @@ extern "C" size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storag
 }
 
 extern "C" int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,
-                               const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every, void *d_workspace,
-                               size_t workspace_bytes, void *stream) {
-    return tsf::run_gvf_adjoint(d_f0, X, Y, Z, mu, iterations, storage, d_gv, d_gf0, dmu, checkpoint_every,
+                               const float *d_gv, float *d_gf0, double *dmu, int checkpoint_every, int flags,
+                               void *d_workspace, size_t workspace_bytes, void *stream) {
+    return tsf::run_gvf_adjoint(d_f0, X, Y, Z, mu, iterations, storage, d_gv, d_gf0, dmu, checkpoint_every, flags,
                                 d_workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsf_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
+                                    int storage, int checkpoint_every, void *d_workspace, size_t workspace_bytes,
+                                    void *stream) {
+    return tsf::run_gvf_checkpointed(d_f0, d_v, X, Y, Z, mu, iterations, storage, checkpoint_every, d_workspace,
+                                     workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
 }

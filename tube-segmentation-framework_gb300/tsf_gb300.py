@@ -72,7 +72,8 @@ def _declare(L):
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
         "tsf_gvf_adjoint_workspace_size": (_sz, [_i, _i, _i, _i, _i, _i]),
-        "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _p, _sz, _p]),
+        "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _i, _p, _sz, _p]),
+        "tsf_gvf_checkpointed": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _sz, _p]),
         "tsf_tdf_backward_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_tdf_circle_backward": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _p, _sz, _p]),
         "tsf_vector_field_backward": (_i, [_p, _p, _i, _i, _i, _f, _i, _p, _p]),
@@ -191,18 +192,34 @@ def gvf(f0, mu: float, iterations: int, storage: str = "f32", v=None, ws=None, m
     return v
 
 
+def gvf_adjoint_workspace(f0, iterations: int, storage: str = "f32", checkpoint_every: int = 0):
+    _, Z, Y, X = f0.shape
+    return workspace(load().tsf_gvf_adjoint_workspace_size(X, Y, Z, STORAGE[storage], int(iterations),
+                                                           int(checkpoint_every)))
+
+
+def gvf_checkpointed(f0, mu: float, iterations: int, ws, storage: str = "f32", checkpoint_every: int = 0,
+                     stream=None):
+    """Forward GVF (result returned) keeping the adjoint's checkpoints in ws."""
+    _, Z, Y, X = f0.shape
+    v = f0.clone()
+    _check(load().tsf_gvf_checkpointed(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
+                                       int(checkpoint_every), _ptr(ws), ws.numel(), _stream(stream)))
+    return v
+
+
 def gvf_adjoint(f0, mu: float, iterations: int, gv, storage: str = "f32", checkpoint_every: int = 0,
-                stream=None):
+                ws=None, checkpoints_stored: bool = False, stream=None):
     """dL/df0 (planar float32) and dL/dmu for L with dL/dv_K = gv."""
     torch = _torch()
     _, Z, Y, X = f0.shape
     L = load()
-    need = L.tsf_gvf_adjoint_workspace_size(X, Y, Z, STORAGE[storage], int(iterations), int(checkpoint_every))
-    ws = workspace(need)
+    ws = gvf_adjoint_workspace(f0, iterations, storage, checkpoint_every) if ws is None else ws
     gf = torch.empty((3, Z, Y, X), dtype=torch.float32, device=f0.device)
     dmu = C.c_double(0.0)
     _check(L.tsf_gvf_adjoint(_ptr(f0), X, Y, Z, float(mu), int(iterations), STORAGE[storage], _ptr(gv), _ptr(gf),
-                             C.byref(dmu), int(checkpoint_every), _ptr(ws), ws.numel(), _stream(stream)))
+                             C.byref(dmu), int(checkpoint_every), 1 if checkpoints_stored else 0, _ptr(ws),
+                             ws.numel(), _stream(stream)))
     return gf, dmu.value
 
 
