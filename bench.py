@@ -75,6 +75,22 @@ def mem_peaks():
         return None
 
 
+def reduce_max(value: float, world: int, device="cuda") -> float:
+    """The largest value over the ranks (the timed region of the slowest rank)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput of `world` independent replicas: all ranks' units
+    over the slowest rank's time."""
+    return world * units_per_rank / seconds_max
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -251,12 +267,8 @@ def run_tsf(args, rank, world):
     launches = T.kernel_launches() - l0
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * (N * args.iters) / (ms * 1e-3) / 1e9
+    ms = reduce_max(e0.elapsed_time(e1) / args.steps, world)
+    value = replica_throughput(N * args.iters, ms * 1e-3, world) / 1e9
 
     # ---- per-stage times (one instrumented step) ------------------------------------
     evs = []
@@ -325,12 +337,8 @@ def run_tsf(args, rank, world):
     for _ in range(args.steps):
         nvs.append(e2e_step())
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * (N * args.iters) / e2e_s / 1e9
+    e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, world)
+    e2e_value = replica_throughput(N * args.iters, e2e_s, world) / 1e9
     h2d = N * 4
     d2h = N * 4 * 2 + int(np.mean(nvs)) * 12
 

@@ -300,6 +300,11 @@ static int launch_gvf_plain(int st, const void *d_f0, const void *src, void *dst
     return TSF_OK;
 }
 
+// One iteration from src to dst (distinct buffers).
+int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s) {
+    return launch_gvf_plain(st, d_f0, src, dst, X, Y, Z, mu, s);
+}
+
 // Runs `iterations` Jacobi iterations in place on d_v.  mode: 0 = choose,
 // 1 = one iteration per launch only, 2 = temporal blocking where possible.
 int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st,

@@ -27,6 +27,7 @@ namespace tsf {
 int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st, void *ws,
             size_t ws_bytes, int mode, cudaStream_t s);
 size_t gvf_workspace_size(int X, int Y, int Z, int st);
+int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s);
 
 // folded cotangent at (x, y, z): sum of lambda' over the voxels that mirror to it
 __device__ __forceinline__ float fold_at(const float *__restrict__ lp, int x, int y, int z, int X, int Y, int Z) {
@@ -64,16 +65,11 @@ __global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__re
                                                                const typename Store<ST>::T *__restrict__ f,
                                                                float *__restrict__ lam_out, float *__restrict__ gf,
                                                                double *__restrict__ dmu_block, int X, int Y, int Z,
-                                                               float mu, int skip_fast) {
+                                                               float mu) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    bool in = x < X && y < Y && z < Z;
-    if (skip_fast) {
-        // voxels of the 4-voxel vectors that gvf_adjoint_vec_kernel handled
-        const int x0 = x & ~3;
-        if (y >= 3 && y <= Y - 4 && z >= 3 && z <= Z - 4 && x0 >= 4 && x0 + 4 <= X - 4) in = false;
-    }
+    const bool in = x < X && y < Y && z < Z;
     const int64_t n = (int64_t)X * Y * Z;
     double dmu = 0.0;
     if (in) {
@@ -129,19 +125,44 @@ __global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__re
     }
 }
 
-// Interior fast path of the adjoint step: every thread owns 4 consecutive
-// voxels of a row whose whole stencil lies at least 3 voxels inside every
-// face, where the folded cotangent equals lambda' itself.  Vector loads of
-// lambda' (FP32) and of the stored states, x-neighbours by shuffles, the
-// same formulas as gvf_adjoint_step_kernel.  Threads with any voxel near a
-// face write nothing; gvf_adjoint_step_kernel (skip_fast) covers those voxels.
+// In-place fold of the cotangent along one axis: the mirror rule sends the
+// update computed at 2 to index 0 and the one at size-3 to size-1, so
+// g[2] += g[0], g[size-3] += g[size-1], and g[0] = g[size-1] = 0.  Applied to
+// x, then y, then z it turns lambda' into fold(lambda') (the rule is separable).
+// One thread per (component, face position); only the boundary planes move.
+__global__ void fold_axis_kernel(float *__restrict__ g, int X, int Y, int Z, int axis) {
+    const int64_t n = (int64_t)X * Y * Z;
+    int A, B;                       // extents of the face
+    int64_t sa, sb, sn;             // strides: face coordinates, folded axis
+    int E;                          // folded extent
+    if (axis == 0) { A = Y; B = Z; sa = X; sb = (int64_t)X * Y; sn = 1; E = X; }
+    else if (axis == 1) { A = X; B = Z; sa = 1; sb = (int64_t)X * Y; sn = X; E = Y; }
+    else { A = X; B = Y; sa = 1; sb = X; sn = (int64_t)X * Y; E = Z; }
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)3 * A * B) return;
+    const int c = (int)(t / ((int64_t)A * B));
+    const int64_t r = t % ((int64_t)A * B);
+    const int a = (int)(r % A), b = (int)(r / A);
+    float *p = g + c * n + a * sa + b * sb;
+    const float g0 = p[0], gl = p[(E - 1) * sn];
+    p[2 * sn] += g0;
+    p[(E - 3) * sn] += gl;
+    p[0] = 0.0f;
+    p[(E - 1) * sn] = 0.0f;
+}
+
+// Adjoint stencil on the folded cotangent g (zero outside [1, size-2] per
+// axis), 4 consecutive voxels per thread, FP32 cotangents in 16-byte vectors,
+// x-neighbours by shuffles, neighbours outside the volume read as 0:
+//     lambda = g (1 - 6 mu - s) + mu sum_6 g,   gf += g s - 2 f sum_d g_d (v_d - f_d),
+//     dmu += sum_c g_c L(v_c)   (L with clamped reads: g = 0 wherever L would clamp).
 template <int ST>
-__global__ void __launch_bounds__(256) gvf_adjoint_vec_kernel(const float *__restrict__ lam_in,
-                                                              const typename Store<ST>::T *__restrict__ v,
-                                                              const typename Store<ST>::T *__restrict__ f,
-                                                              float *__restrict__ lam_out, float *__restrict__ gf,
-                                                              double *__restrict__ dmu_block, int X, int Y, int Z,
-                                                              float mu) {
+__global__ void __launch_bounds__(256) gvf_adjoint_stencil_kernel(const float *__restrict__ gin,
+                                                                  const typename Store<ST>::T *__restrict__ v,
+                                                                  const typename Store<ST>::T *__restrict__ f,
+                                                                  float *__restrict__ lam_out, float *__restrict__ gf,
+                                                                  double *__restrict__ dmu_block, int X, int Y, int Z,
+                                                                  float mu) {
     using T = typename Store<ST>::T;
     constexpr int VX = 4;
     const int lane = threadIdx.x;
@@ -151,64 +172,73 @@ __global__ void __launch_bounds__(256) gvf_adjoint_vec_kernel(const float *__res
     const bool act = y < Y && x0 < X;
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
     const unsigned full = 0xffffffffu;
-    const bool fast = act && y >= 3 && y <= Y - 4 && z >= 3 && z <= Z - 4 && x0 >= 4 && x0 + VX <= X - 4;
+    const int64_t q = (int64_t)z * plane + (int64_t)(act ? y : 0) * X + (act ? x0 : 0);
+    const bool hy0 = y > 0, hy1 = y < Y - 1, hz0 = z > 0, hz1 = z < Z - 1;
     double dmu = 0.0;
-    const int64_t q = (int64_t)z * plane + (int64_t)y * X + x0;
-    auto ld4 = [](const float *p, float o[VX]) {
-        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
-        o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
-    };
-    auto ldv = [](const T *p, float o[VX]) {
+    float fv[3][VX], s[VX], gd[VX], gc[3][VX];
 #pragma unroll
-        for (int i = 0; i < VX; i++) o[i] = Store<ST>::load(p[i]);
-    };
-    float fv[3][VX], s[VX], gd[VX];
-    float gc[3][VX];
+    for (int c = 0; c < 3; c++)
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        if (act) ldv(f + c * n + q, fv[c]);
-        else for (int i = 0; i < VX; i++) fv[c][i] = 0.0f;
-    }
+        for (int i = 0; i < VX; i++) fv[c][i] = act ? Store<ST>::load(f[c * n + q + i]) : 0.0f;
 #pragma unroll
     for (int i = 0; i < VX; i++) {
         s[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
         gd[i] = 0.0f;
     }
+    auto ld4 = [&](const float *p, bool ok, float o[VX]) {
+        if (ok) {
+            const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+            o[0] = t.x; o[1] = t.y; o[2] = t.z; o[3] = t.w;
+        } else {
+            o[0] = o[1] = o[2] = o[3] = 0.0f;
+        }
+    };
+    auto ldv = [&](const T *p, bool ok, float o[VX]) {
+#pragma unroll
+        for (int i = 0; i < VX; i++) o[i] = ok ? Store<ST>::load(p[i]) : 0.0f;
+    };
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const float *lp = lam_in + c * n + q;
+        const float *gp = gin + c * n + q;
         const T *vp = v + c * n + q;
         float g[VX], gyp[VX], gym[VX], gzp[VX], gzm[VX], vv[VX], vyp[VX], vym[VX], vzp[VX], vzm[VX];
-        if (act) {
-            ld4(lp, g); ld4(lp + X, gyp); ld4(lp - X, gym); ld4(lp + plane, gzp); ld4(lp - plane, gzm);
-            ldv(vp, vv);
-            if (fast) { ldv(vp + X, vyp); ldv(vp - X, vym); ldv(vp + plane, vzp); ldv(vp - plane, vzm); }
-        } else {
-            for (int i = 0; i < VX; i++) g[i] = gyp[i] = gym[i] = gzp[i] = gzm[i] = vv[i] = 0.0f;
-        }
+        ld4(gp, act, g);
+        ld4(gp + X, act && hy1, gyp);
+        ld4(gp - X, act && hy0, gym);
+        ld4(gp + plane, act && hz1, gzp);
+        ld4(gp - plane, act && hz0, gzm);
+        ldv(vp, act, vv);
+        ldv(vp + X, act && hy1, vyp);
+        ldv(vp - X, act && hy0, vym);
+        ldv(vp + plane, act && hz1, vzp);
+        ldv(vp - plane, act && hz0, vzm);
         float gl = __shfl_up_sync(full, g[VX - 1], 1), gr = __shfl_down_sync(full, g[0], 1);
         float vl = __shfl_up_sync(full, vv[VX - 1], 1), vr = __shfl_down_sync(full, vv[0], 1);
-        if (fast && lane == 0) { gl = lp[-1]; vl = Store<ST>::load(vp[-1]); }
-        if (fast && lane == 31) { gr = lp[VX]; vr = Store<ST>::load(vp[VX]); }
-        if (fast) {
-            float out[VX];
-#pragma unroll
-            for (int i = 0; i < VX; i++) {
-                const float xp = i == VX - 1 ? gr : g[i + 1 < VX ? i + 1 : i];
-                const float xm = i == 0 ? gl : g[i > 0 ? i - 1 : 0];
-                const float nb = ((((xp + xm) + gyp[i]) + gym[i]) + gzp[i]) + gzm[i];
-                out[i] = g[i] * (1.0f - 6.0f * mu - s[i]) + mu * nb;
-                const float vxp = i == VX - 1 ? vr : vv[i + 1 < VX ? i + 1 : i];
-                const float vxm = i == 0 ? vl : vv[i > 0 ? i - 1 : 0];
-                const float L = (((((vxp + vxm) + vyp[i]) + vym[i]) + vzp[i]) + vzm[i]) - 6.0f * vv[i];
-                dmu += (double)(g[i] * L);
-                gd[i] += g[i] * (vv[i] - fv[c][i]);
-                gc[c][i] = g[i];
-            }
-            *reinterpret_cast<float4 *>(lam_out + c * n + q) = make_float4(out[0], out[1], out[2], out[3]);
+        if (lane == 0) {
+            gl = (act && x0 > 0) ? gp[-1] : 0.0f;
+            vl = (act && x0 > 0) ? Store<ST>::load(vp[-1]) : 0.0f;
         }
+        if (lane == 31 || x0 + VX >= X) {
+            gr = (act && x0 + VX < X) ? gp[VX] : 0.0f;
+            vr = (act && x0 + VX < X) ? Store<ST>::load(vp[VX]) : 0.0f;
+        }
+        float out[VX];
+#pragma unroll
+        for (int i = 0; i < VX; i++) {
+            const float xp = i == VX - 1 ? gr : g[i + 1 < VX ? i + 1 : i];
+            const float xm = i == 0 ? gl : g[i > 0 ? i - 1 : 0];
+            const float nb = ((((xp + xm) + gyp[i]) + gym[i]) + gzp[i]) + gzm[i];
+            out[i] = g[i] * (1.0f - 6.0f * mu - s[i]) + mu * nb;
+            const float vxp = i == VX - 1 ? vr : vv[i + 1 < VX ? i + 1 : i];
+            const float vxm = i == 0 ? vl : vv[i > 0 ? i - 1 : 0];
+            const float L = (((((vxp + vxm) + vyp[i]) + vym[i]) + vzp[i]) + vzm[i]) - 6.0f * vv[i];
+            dmu += (double)(g[i] * L);
+            gd[i] += g[i] * (vv[i] - fv[c][i]);
+            gc[c][i] = g[i];
+        }
+        if (act) *reinterpret_cast<float4 *>(lam_out + c * n + q) = make_float4(out[0], out[1], out[2], out[3]);
     }
-    if (fast) {
+    if (act) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             float4 *gp = reinterpret_cast<float4 *>(gf + c * n + q);
@@ -220,7 +250,6 @@ __global__ void __launch_bounds__(256) gvf_adjoint_vec_kernel(const float *__res
             *gp = a;
         }
     }
-    // per-block FP64 partial of dL/dmu, accumulated over the steps in a fixed order
     __shared__ double red[8];
     const int t = threadIdx.x + blockDim.x * threadIdx.y;
 #pragma unroll
@@ -368,28 +397,41 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
         // states k0 .. k1-1 into the segment buffer
         for (int k = k0; k < k1; k++) {
             void *dstate = w + L.seg + (size_t)(k - k0) * L.state;
-            const void *from = k == k0 ? (const void *)(w + L.ck + (size_t)seg * L.state)
-                                       : (const void *)(w + L.seg + (size_t)(k - k0 - 1) * L.state);
-            TSF_TRY_CUDA(cudaMemcpyAsync(dstate, from, state_bytes, cudaMemcpyDeviceToDevice, s));
-            if (k > k0) {
-                r = run_gvf(d_f0, dstate, X, Y, Z, mu, 1, st, gws, gws_bytes, 1, s);
+            if (k == k0) {
+                TSF_TRY_CUDA(cudaMemcpyAsync(dstate, w + L.ck + (size_t)seg * L.state, state_bytes,
+                                             cudaMemcpyDeviceToDevice, s));
+            } else {
+                r = gvf_step(st, d_f0, w + L.seg + (size_t)(k - k0 - 1) * L.state, dstate, X, Y, Z, mu, s);
                 if (r) return r;
             }
         }
+        // the stencil kernel moves cotangents in 16-byte vectors
+        const bool vec = adj_vec(X) && ((uintptr_t)d_gf0 & 15) == 0 && ((uintptr_t)w & 15) == 0;
         for (int k = k1 - 1; k >= k0; k--) {
             const void *vk = w + L.seg + (size_t)(k - k0) * L.state;
             const dim3 g = adj_grid(X, Y, Z);
             double *dmu_v = dmu_b + (int64_t)g.x * g.y * g.z;
-            const bool vec = adj_vec(X);
-            TSF_DISPATCH_STORAGE(st, ST, {
-                using T = typename Store<ST>::T;
-                if (vec)
-                    gvf_adjoint_vec_kernel<ST><<<adjv_grid(X, Y, Z), adjv_block(), 0, s>>>(
+            if (vec) {
+                // fold lambda' in place (boundary planes only), then the stencil
+                for (int axis = 0; axis < 3; axis++) {
+                    const int64_t faces = 3 * (axis == 0 ? (int64_t)Y * Z : axis == 1 ? (int64_t)X * Z : (int64_t)X * Y);
+                    fold_axis_kernel<<<(unsigned)((faces + 255) / 256), 256, 0, s>>>(lam, X, Y, Z, axis);
+                }
+                TSF_CHECK_LAUNCHES("fold_axis_kernel", 3);
+                TSF_DISPATCH_STORAGE(st, ST, {
+                    using T = typename Store<ST>::T;
+                    gvf_adjoint_stencil_kernel<ST><<<adjv_grid(X, Y, Z), adjv_block(), 0, s>>>(
                         lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu);
-                gvf_adjoint_step_kernel<ST><<<g, adj_block(), 0, s>>>(lam, (const T *)vk, (const T *)d_f0, lam2,
-                                                                     d_gf0, dmu_b, X, Y, Z, mu, vec ? 1 : 0);
-            });
-            TSF_CHECK_LAUNCHES("gvf_adjoint_step_kernel", vec ? 2 : 1);
+                });
+                TSF_CHECK_LAUNCH("gvf_adjoint_stencil_kernel");
+            } else {
+                TSF_DISPATCH_STORAGE(st, ST, {
+                    using T = typename Store<ST>::T;
+                    gvf_adjoint_step_kernel<ST><<<g, adj_block(), 0, s>>>(lam, (const T *)vk, (const T *)d_f0, lam2,
+                                                                         d_gf0, dmu_b, X, Y, Z, mu);
+                });
+                TSF_CHECK_LAUNCH("gvf_adjoint_step_kernel");
+            }
             float *t = lam; lam = lam2; lam2 = t;
         }
     }
