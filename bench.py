@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
+    ap.add_argument("--summarize-ncu-csv", metavar="CSV",
+                    help="print a per-kernel table (launches, total time, share) of an ncu "
+                         "--metrics gpu__time_duration.sum --csv launch list and exit")
     return ap.parse_args()
 
 
@@ -259,11 +262,13 @@ def run_tsf(args, rank, world):
     l0 = T.kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.profiler.start()           # a profiler started with collection off records only this region
     e0.record()
     for _ in range(args.steps):
         pipe.step()
     e1.record()
     torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     launches = T.kernel_launches() - l0
     barrier()
     clk = clocks.stop()
@@ -432,6 +437,32 @@ def fwd_adjoint_timing(torch, pipe, args):
             "checkpoint_every": int(np.ceil(np.sqrt(args.iters))),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
+
+
+def summarize_ncu_csv(path):
+    """Per-kernel launches, total device time and share of an ncu launch list."""
+    import csv
+    import collections
+    import re
+    rows = list(csv.reader(open(path)))
+    hi = next(i for i, r in enumerate(rows) if "Kernel Name" in r and "Metric Value" in r)
+    K, V, U = (rows[hi].index(c) for c in ("Kernel Name", "Metric Value", "Metric Unit"))
+    scale = {"ns": 1e-6, "nsecond": 1e-6, "us": 1e-3, "usecond": 1e-3, "ms": 1.0, "msecond": 1.0,
+             "s": 1e3, "second": 1e3}
+    tot, cnt = collections.defaultdict(float), collections.Counter()
+    for r in rows[hi + 1:]:
+        if len(r) <= V:
+            continue
+        name = re.sub(r"^void ", "", re.sub(r"\(.*", "", r[K]).strip())
+        name = re.sub(r"<.*", "", name).replace("tsf::", "")
+        tot[name] += float(r[V].replace(",", "")) * scale.get(r[U], 1.0)
+        cnt[name] += 1
+    total = sum(tot.values())
+    lines = ["| kernel | launches | total ms | share |", "|---|---|---|---|"]
+    for k, v in sorted(tot.items(), key=lambda kv: -kv[1]):
+        lines.append("| `%s` | %d | %.3f | %.1f %% |" % (k, cnt[k], v, 100 * v / total))
+    lines.append("| total | %d | %.3f | 100 %% |" % (sum(cnt.values()), total))
+    return "\n".join(lines)
 
 
 def _traffic_from_profile(storage):
@@ -624,6 +655,9 @@ def run_fmg_workload(args):
 
 def main():
     args = parse()
+    if args.summarize_ncu_csv:
+        print(summarize_ncu_csv(args.summarize_ncu_csv))
+        return
     if args.fmg:
         print(json.dumps(run_fmg_workload(args)))
         return
