@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time the forward + adjoint (gradient) pass alone and print its JSON line")
     ap.add_argument("--summarize-ncu-csv", metavar="CSV",
                     help="print a per-kernel table (launches, total time, share) of an ncu "
                          "--metrics gpu__time_duration.sum --csv launch list and exit")
@@ -174,11 +176,12 @@ class Pipeline:
         self.max_vertices = 1 << 16
         self.verts = torch.zeros((self.max_vertices, 3), dtype=torch.int32, device=dev)
         self.last = None
+        self.gvf_mode = 0                   # 0: default kernel choice; 1: register-vector kernel
 
     def gvf_only(self):
         T = self.T
         self.v.copy_(self.f0)
-        T.gvf(self.f0, self.mu, self.iters, self.storage, v=self.v, ws=self.gvf_ws)
+        T.gvf(self.f0, self.mu, self.iters, self.storage, v=self.v, ws=self.gvf_ws, mode=self.gvf_mode)
 
     def step(self, events=None):
         T, P, s = self.T, PARAMS, self.storage
@@ -284,8 +287,9 @@ def run_tsf(args, rank, world):
         stages[b] = round(ea.elapsed_time(eb), 4)
 
     # ---- GVF kernel: average launch duration, both storage formats ------------------
-    def gvf_kernel_stats(storage, mu):
+    def gvf_kernel_stats(storage, mu, mode=0):
         p = pipe if storage == args.storage else Pipeline(T, torch, shape, storage, args.iters, mu)
+        p.gvf_mode = mode
         if p is not pipe:
             p.vol.copy_(pipe.vol)
             T.blur(p.vol, PARAMS["large_blur"], out=p.blurred)
@@ -305,11 +309,13 @@ def run_tsf(args, rank, world):
         nl = (T.kernel_launches() - la) / reps
         gvf_ms = a.elapsed_time(b) / reps
         p.mu = args.mu
+        p.gvf_mode = 0
         return gvf_ms, nl
 
     gvf_ms, gvf_launches = gvf_kernel_stats(args.storage, args.mu)
     gvf_ms_mu01, _ = gvf_kernel_stats(args.storage, 0.1)
     f32_ms, _ = gvf_kernel_stats("f32", args.mu)
+    vec_ms, _ = gvf_kernel_stats(args.storage, args.mu, mode=1)
     s_bytes = 4 if args.storage == "f32" else 2
     iters_per_launch = args.iters / gvf_launches
     launch_s = gvf_ms * 1e-3 / gvf_launches
@@ -363,7 +369,9 @@ def run_tsf(args, rank, world):
                 "launches": gvf_launches, "iterations_per_launch": iters_per_launch,
                 "gvox_iter_s_mu_0_1": round(N * args.iters / (gvf_ms_mu01 * 1e-3) / 1e9, 2),
                 "f32_store_gvox_iter_s": round(N * args.iters / (f32_ms * 1e-3) / 1e9, 2),
-                "speedup_vs_f32_store": round(f32_ms / gvf_ms, 3)},
+                "speedup_vs_f32_store": round(f32_ms / gvf_ms, 3),
+                "register_vector_kernel_gvox_iter_s": round(N * args.iters / (vec_ms * 1e-3) / 1e9, 2),
+                "device_error": T.gvf_device_error()},
         "candidates": pipe.last,
         "roofline": {"bound": "hbm", "kernel": "GVF iteration", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -437,6 +445,18 @@ def fwd_adjoint_timing(torch, pipe, args):
             "checkpoint_every": int(np.ceil(np.sqrt(args.iters))),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
+
+
+def run_adjoint(args):
+    """Forward + adjoint timing alone on the vessel-tree volume (the same
+    measurement the default run reports under fwd_adjoint)."""
+    import types
+    import torch
+    import synthetic
+    n = args.size
+    vol = torch.from_numpy(synthetic.vascular_tree((n, n, n), seed=args.seed)).cuda()
+    return {"workload": "vessel tree %d^3, GVF %d iterations, forward + adjoint" % (n, args.iters),
+            "fwd_adjoint": fwd_adjoint_timing(torch, types.SimpleNamespace(vol=vol), args)}
 
 
 def summarize_ncu_csv(path):
@@ -657,6 +677,9 @@ def main():
     args = parse()
     if args.summarize_ncu_csv:
         print(summarize_ncu_csv(args.summarize_ncu_csv))
+        return
+    if args.adjoint:
+        print(json.dumps(run_adjoint(args)))
         return
     if args.fmg:
         print(json.dumps(run_fmg_workload(args)))

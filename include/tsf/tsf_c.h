@@ -130,20 +130,28 @@ size_t tsf_gvf_workspace_size(int X, int Y, int Z, int storage);
  * kernel (kernels.cl:1464-1493).  d_f0 is the planar initial field f0 (the
  * data term, read only); d_v holds the planar start value on entry (normally
  * a copy of f0, as GVF3DInit makes) and the result after exactly `iterations`
- * iterations on return.  mu is the GVF regularisation constant.  Several
- * iterations run per launch (temporal blocking); every iteration's result is
- * still rounded to `storage`, so the result equals one-iteration-per-launch.
+ * iterations on return.  mu is the GVF regularisation constant.  One
+ * iteration per launch; every iteration's result is rounded to `storage`.
  * Note: the reference's host loop returns the result of iterations - 1 when
  * `iterations` is odd; the C++ layer (run()) reproduces that, this call does
  * not. */
 int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
             int storage, void *d_workspace, size_t workspace_bytes, void *stream);
 
-/* tsf_gvf with the kernel forced: mode 1 = one iteration per launch,
- * mode 2 = temporal blocking wherever the iteration count allows, 0 = the
- * default choice of tsf_gvf.  All modes give bit-identical results. */
+/* tsf_gvf with the kernel chosen: 0 = the default of tsf_gvf (the
+ * z-streaming kernel fed by TMA copies wherever rows are a multiple of 16
+ * bytes and the buffers 16-byte aligned, else the register-vector kernel),
+ * 1 = the register-vector (or per-voxel) kernel only, 2 = same as 0.  All
+ * modes give bit-identical results. */
 int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                  int storage, void *d_workspace, size_t workspace_bytes, int mode, void *stream);
+
+/* Device-side error word of the streaming GVF kernel: 0 = none, bit 0 = a
+ * shared-memory copy did not complete within its wait limit (the kernel then
+ * stops early and its output is invalid); -1 if the word could not be read.
+ * clear != 0 resets the word.  Synchronises with the device.  No counterpart
+ * in the reference (OpenCL reports no such condition). */
+int tsf_gvf_device_error(int clear);
 
 /* tsf_gvf for callers that cannot allocate device memory.  No counterpart in
  * the reference: it exists for hosts that can neither call cudaMalloc nor

@@ -65,18 +65,23 @@ def test_vector_field_bitexact(torch_dev, tsf, oracle, synth, storage, vsign):
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("mu,iters", [(0.05, 17), (0.1, 8)])
 @pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130), (9, 10, 256)])
-def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape):
-    """Odd x extents take the one-thread-per-voxel kernel, the others the
-    vectorised kernel: 16- or 8-byte vectors, full rows (X = 256) and ragged
-    ones (several warps per row, a last warp with few lanes, the smallest
-    rows), and X = 130, which goes back to the per-voxel kernel."""
+@pytest.mark.parametrize("mode", [0, 1])
+def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape, mode):
+    """mode 0: the z-streaming TMA kernel wherever rows are a multiple of 16
+    bytes -- tiles shifted back inside at the +x / +y edges (X = 136, 264;
+    Y = 9, 22), rows shorter than a tile (X = 8, 40), z ranges split into
+    several chunks (Z = 19, 35), the thinnest volumes (Z = 5); X = 33 and, for
+    the 16-bit formats, X = 130 take the other kernels.  mode 1: the
+    register-vector kernel (16- or 8-byte vectors, ragged last warps) or, for
+    odd rows, the one-thread-per-voxel kernel."""
     torch = torch_dev
     vol = oracle.blur(_vol(synth, shape, 4), 0.5)
     ref4 = oracle.vector_field(vol, 0.2, 1, storage)
     p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
-    v = tsf.gvf(p, mu, iters, storage)
+    v = tsf.gvf(p, mu, iters, storage, mode=mode)
     ov = oracle.gvf(ref4, mu, iters, storage)
     assert np.array_equal(_np_stored(v, storage), ov)
+    assert tsf.gvf_device_error() == 0
     # the finish pass
     f4 = tsf.gvf_finish(v, storage)
     assert np.array_equal(_np_stored(f4, storage), oracle.gvf_finish(ov, storage))
@@ -84,7 +89,8 @@ def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape):
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 def test_gvf_modes_identical(torch_dev, tsf, synth, oracle, storage):
-    """One iteration per launch and temporal blocking give the same bits."""
+    """The register-vector kernel (mode 1) and the streaming kernel (mode 2)
+    give the same bits."""
     torch = torch_dev
     vol = oracle.blur(_vol(synth, (40, 36, 44), 5), 0.5)
     p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)

@@ -8,16 +8,14 @@
 // recomputed from the stored f0 each time, exactly like the reference (which
 // keeps f0z in v.w and f0x,f0y in an RG image).
 //
-// Two kernels compute the same iteration:
-//  * gvf_plain_kernel: one iteration per launch, one thread per voxel, all
-//    seven stencil reads through L1/L2.  HBM-bound at 9s B / voxel-iteration.
-//  * gvf_tb_kernel: TB iterations per launch (temporal blocking).  A CTA owns
-//    an x-y tile and streams through z; each time level keeps one z-plane of
-//    the tile (with a halo that shrinks by one voxel per level) in shared
-//    memory and its z-1 / z+1 neighbours in registers.  Intermediate levels
-//    are rounded to the storage format exactly as a stored iteration would
-//    be, so both kernels give bit-identical results.
-#include "tsf_common.cuh"
+// Three kernels compute the same iteration, bit for bit:
+//  * gvf_zs_kernel (gvf_zs.cu): z-streaming with TMA copies into a shared
+//    memory ring of planes; the default wherever rows are a multiple of 16
+//    bytes and the buffers 16-byte aligned.
+//  * gvf_vec_kernel: one thread per 8- or 16-byte vector of a row, all loads
+//    held in registers; rows that split into such vectors.
+//  * gvf_plain_kernel: one thread per voxel; any shape.
+#include "packed.cuh"
 
 namespace tsf {
 
@@ -73,72 +71,6 @@ __global__ void __launch_bounds__(256) gvf_plain_kernel(const typename Store<ST>
 // and the last chunk is shifted to end at Z, so those pairs never straddle a
 // chunk).  Per voxel the arithmetic is exactly gvf_plain_kernel's.
 // ---------------------------------------------------------------------------
-// BYTES (8 or 16) bytes of stored components -- 4 or 8 voxels of a 16-bit
-// format, 2 or 4 of FP32 -- unpacked / packed two at a time with the paired
-// conversion intrinsics.
-template <int ST, int BYTES> struct PackedV {
-    using T = typename Store<ST>::T;
-    static constexpr int VX = BYTES / (int)sizeof(T);
-    static constexpr int W = BYTES / 4;              // 32-bit words
-    struct Raw { unsigned u[W]; };
-    static __device__ __forceinline__ Raw load(const T *p) {
-        Raw r;
-        if constexpr (BYTES == 16) {
-            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-            r.u[0] = v.x; r.u[1] = v.y; r.u[2] = v.z; r.u[3] = v.w;
-        } else {
-            const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
-            r.u[0] = v.x; r.u[1] = v.y;
-        }
-        return r;
-    }
-    static __device__ __forceinline__ Raw zero() {
-        Raw r;
-#pragma unroll
-        for (int i = 0; i < W; i++) r.u[i] = 0u;
-        return r;
-    }
-    static __device__ __forceinline__ void unpack(const Raw &raw, float o[VX]) {
-#pragma unroll
-        for (int k = 0; k < W; k++) {
-            const unsigned u = raw.u[k];
-            if constexpr (ST == TSF_STORE_F32) {
-                o[k] = __uint_as_float(u);
-            } else if constexpr (ST == TSF_STORE_F16) {
-                const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u));
-                o[2 * k] = a.x; o[2 * k + 1] = a.y;
-            } else if constexpr (ST == TSF_STORE_BF16) {
-                o[2 * k] = __uint_as_float(u << 16);
-                o[2 * k + 1] = __uint_as_float(u & 0xffff0000u);
-            } else {
-                o[2 * k] = Store<ST>::load((int16_t)(u & 0xffffu));
-                o[2 * k + 1] = Store<ST>::load((int16_t)(u >> 16));
-            }
-        }
-    }
-    // rounds to the storage format (the only rounding of an iteration's result)
-    static __device__ __forceinline__ void store(T *p, const float o[VX]) {
-        unsigned u[W];
-#pragma unroll
-        for (int k = 0; k < W; k++) {
-            if constexpr (ST == TSF_STORE_F32) {
-                u[k] = __float_as_uint(o[k]);
-            } else if constexpr (ST == TSF_STORE_F16) {
-                const __half2 h = __floats2half2_rn(o[2 * k], o[2 * k + 1]);
-                u[k] = *reinterpret_cast<const unsigned *>(&h);
-            } else if constexpr (ST == TSF_STORE_BF16) {
-                const __nv_bfloat162 h = __floats2bfloat162_rn(o[2 * k], o[2 * k + 1]);
-                u[k] = *reinterpret_cast<const unsigned *>(&h);
-            } else {
-                const int16_t lo = Store<ST>::store(o[2 * k]), hi = Store<ST>::store(o[2 * k + 1]);
-                u[k] = (unsigned)(uint16_t)lo | ((unsigned)(uint16_t)hi << 16);
-            }
-        }
-        if constexpr (BYTES == 16) *reinterpret_cast<uint4 *>(p) = make_uint4(u[0], u[1], u[2], u[3]);
-        else *reinterpret_cast<uint2 *>(p) = make_uint2(u[0], u[1]);
-    }
-};
-
 // One thread = the VX voxels of one vector (BYTES bytes) of one row of one
 // plane.  All loads of a thread are independent and issued together -- per
 // component the centre vector and its y+-1 and z+-1 neighbours, plus the f0
@@ -247,11 +179,9 @@ __global__ void gvf_finish_kernel(const typename Store<ST>::T *__restrict__ v, v
     store4<ST>(field4, i, x, y, z, l > 0.0f ? l : 1.0f);
 }
 
-// Temporal blocking is not enabled yet: every launch runs one iteration.
-static int gvf_tb_levels(int) { return 1; }
-static int launch_gvf_tb(int, const void *, const void *, void *, int, int, int, float, int, cudaStream_t) {
-    return fail(TSF_ERR_INVALID_ARG, "temporal blocking unavailable");
-}
+bool gvf_zs_eligible(int st, const void *d_f0, const void *a, const void *b, int X, int Y, int Z);
+int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
+                  cudaStream_t s);
 
 size_t gvf_workspace_size(int X, int Y, int Z, int st) {
     return (size_t)3 * (size_t)X * (size_t)Y * (size_t)Z * storage_bytes(st);
@@ -300,13 +230,17 @@ static int launch_gvf_plain(int st, const void *d_f0, const void *src, void *dst
     return TSF_OK;
 }
 
-// One iteration from src to dst (distinct buffers).
+// One iteration from src to dst (distinct buffers); the streaming kernel
+// where it applies.
 int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s) {
+    if (gvf_zs_eligible(st, d_f0, src, dst, X, Y, Z)) return launch_gvf_zs(st, d_f0, src, dst, X, Y, Z, mu, s);
     return launch_gvf_plain(st, d_f0, src, dst, X, Y, Z, mu, s);
 }
 
-// Runs `iterations` Jacobi iterations in place on d_v.  mode: 0 = choose,
-// 1 = one iteration per launch only, 2 = temporal blocking where possible.
+// Runs `iterations` Jacobi iterations in place on d_v, one iteration per
+// launch, ping-ponging with the workspace.  mode: 0 = default (the streaming
+// kernel gvf_zs_kernel where it applies, else gvf_vec_kernel), 1 = the
+// register-vector kernels only, 2 = same as 0.  All give identical results.
 int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st,
             void *ws, size_t ws_bytes, int mode, cudaStream_t s) {
     int r = check_dims(X, Y, Z);
@@ -314,22 +248,16 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
     if (!valid_storage(st)) return fail(TSF_ERR_INVALID_ARG, "unknown storage format");
     if (!d_f0 || !d_v) return fail(TSF_ERR_INVALID_ARG, "null buffer");
     if (iterations < 0) return fail(TSF_ERR_INVALID_ARG, "iterations must be >= 0");
+    if (mode < 0 || mode > 2) return fail(TSF_ERR_INVALID_ARG, "unknown GVF mode");
     if (iterations == 0) return TSF_OK;
     const size_t need = gvf_workspace_size(X, Y, Z, st);
     if (!ws || ws_bytes < need) return fail(TSF_ERR_WORKSPACE, "GVF workspace too small");
     void *a = d_v, *b = ws;
-    int left = iterations;
-    const int tb = (mode == 1) ? 1 : gvf_tb_levels(st);
-    while (left > 0) {
-        int k = left >= tb ? tb : left;
-        if (k > 1) {
-            r = launch_gvf_tb(st, d_f0, a, b, X, Y, Z, mu, k, s);
-        } else {
-            r = launch_gvf_plain(st, d_f0, a, b, X, Y, Z, mu, s);
-        }
+    const bool zs = mode != 1 && gvf_zs_eligible(st, d_f0, a, b, X, Y, Z);
+    for (int left = iterations; left > 0; left--) {
+        r = zs ? launch_gvf_zs(st, d_f0, a, b, X, Y, Z, mu, s) : launch_gvf_plain(st, d_f0, a, b, X, Y, Z, mu, s);
         if (r) return r;
         void *t = a; a = b; b = t;
-        left -= k;
     }
     if (a != d_v) {
         TSF_TRY_CUDA(cudaMemcpyAsync(d_v, a, need, cudaMemcpyDeviceToDevice, s));

@@ -1,0 +1,323 @@
+// gvf_zs.cu -- one GVF Jacobi iteration (reference GVF3DIteration,
+// kernels.cl:1464-1493) as a z-streaming kernel fed by tensor-memory-access
+// (TMA) copies into a shared-memory ring of planes.
+//
+// Why: the register-vector kernel (gvf_vec_kernel) issues all of a thread's
+// loads, waits, computes and exits; the resident blocks of an SM move through
+// those phases together, so HBM idles while they compute and the issue slots
+// idle while they wait.  Here a CTA owns an x-y tile and a run of z planes;
+// one thread keeps the copies of the next planes in flight while all threads
+// compute the current one, so memory traffic and arithmetic overlap.
+//
+// Work: tile TX x TY outputs (TX = 128; TY = 8 for the 16-bit formats, 4 for
+// FP32), one warp per tile row, 4 consecutive voxels per lane.  The tiles of
+// a row / column that would run past the volume are shifted back inside it
+// (they overlap their neighbour and write identical values).  Each tile's z
+// range of evaluation planes [1, Z-2] is split into K chunks, K chosen so that
+// tiles x chunks fills the resident-CTA slots once; CTAs of neighbouring tiles
+// stream the same planes at the same time and share their halo rows in L2.
+//
+// Per evaluation plane q the CTA needs planes q-1, q, q+1 of v (box: TX + 2H
+// columns, H = 16 bytes of halo each side, TY + 2 rows, 3 components) and
+// plane q of f0 (TX x TY x 3).  v planes live in a ring of RV slots, f0 planes
+// in a ring of RF slots; slot i of a ring is reused every RV (RF) planes and
+// its mbarrier phase parity is (load index / ring size) & 1.
+//
+// Mirror rule (v'[w] = U(m(w)), m: 0 -> 2, size-1 -> size-3 per axis): a
+// lane's rows are evaluated at mirror(y) (inside the loaded box because edge
+// tiles are shifted inward); in x the vector holding x = 0 / X-1 copies the
+// result of x = 2 / X-3; the plane q = 2 (Z-3) is also written to plane 0
+// (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's, so the
+// result is bit-identical to the other GVF kernels.
+#include <mutex>
+
+#include "packed.cuh"
+#include "tma.cuh"
+
+namespace tsf {
+
+template <int ST> struct ZsCfg {
+    using T = typename Store<ST>::T;
+    static constexpr int ES = (int)sizeof(T);
+    static constexpr int TX = 128;
+    static constexpr int TY = ES == 2 ? 8 : 4;
+    static constexpr int H = 16 / ES;                      // x halo, elements
+    static constexpr int BW = TX + 2 * H;                  // v box width
+    static constexpr int RV = 5, RF = 4;                   // ring slots
+    static constexpr int VBOX = BW * (TY + 2) * 3 * ES;    // bytes of one v box
+    static constexpr int FBOX = TX * TY * 3 * ES;
+    static constexpr int VSLOT = (VBOX + 127) / 128 * 128;
+    static constexpr int FSLOT = (FBOX + 127) / 128 * 128;
+    static constexpr int SMEM = RV * VSLOT + RF * FSLOT + (RV + RF) * 8 + 16;
+    static constexpr int THREADS = 32 * TY;
+    static constexpr int BYTES = 4 * ES;                   // one lane's 4 voxels
+};
+
+// Device-side error word: bit 0 = a copy did not land within kWaitCycles.
+__device__ int g_gvf_zs_error;
+
+// one box copy: announce its bytes on the slot's barrier, then start it
+__device__ __forceinline__ void zs_issue(unsigned char *slot, uint64_t *bar, int bytes, const CUtensorMap *map,
+                                         int x, int y, int z) {
+    mbar_arrive_expect_tx(bar, (uint32_t)bytes);
+    tma_load_4d(slot, map, bar, x, y, z, 0);
+}
+
+template <int ST>
+__global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
+                                                                   const __grid_constant__ CUtensorMap tf,
+                                                                   typename Store<ST>::T *__restrict__ dst, int X,
+                                                                   int Y, int Z, float mu, int ntx, int K) {
+    using C = ZsCfg<ST>;
+    using T = typename Store<ST>::T;
+    using P = PackedV<ST, C::BYTES>;
+    constexpr int TX = C::TX, TY = C::TY, H = C::H, BW = C::BW, RV = C::RV, RF = C::RF;
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char *vring = smem;
+    unsigned char *fring = smem + RV * C::VSLOT;
+    uint64_t *vbar = reinterpret_cast<uint64_t *>(fring + RF * C::FSLOT);
+    uint64_t *fbar = vbar + RV;
+
+    // this CTA's tile and plane range
+    const int col = blockIdx.x / K, chunk = blockIdx.x % K;
+    const int tx = col % ntx, ty = col / ntx;
+    const int x0 = X >= TX ? min(tx * TX, X - TX) : 0;
+    const int y0 = Y >= TY ? min(ty * TY, Y - TY) : 0;
+    const int ZI = Z - 2;
+    const int qa = 1 + (int)((int64_t)ZI * chunk / K), qb = (int)((int64_t)ZI * (chunk + 1) / K);
+    const int nf = qb - qa + 1, nv = nf + 2;               // f planes qa..qb, v planes qa-1..qb+1
+    const int tid = threadIdx.x;
+
+    // v load j = plane qa-1+j into slot j % RV; f load j = plane qa+j into slot j % RF
+    int issued_v = 0, issued_f = 0;                       // meaningful in thread 0 only
+    if (tid == 0) {
+        tma_prefetch_desc(&tv);
+        tma_prefetch_desc(&tf);
+        for (int i = 0; i < RV; i++) mbar_init(vbar + i, 1);
+        for (int i = 0; i < RF; i++) mbar_init(fbar + i, 1);
+        fence_mbar_init();
+        for (; issued_v < RV && issued_v < nv; issued_v++)
+            zs_issue(vring + issued_v * C::VSLOT, vbar + issued_v, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + issued_v);
+        for (; issued_f < RF && issued_f < nf; issued_f++)
+            zs_issue(fring + issued_f * C::FSLOT, fbar + issued_f, C::FBOX, &tf, x0, y0, qa + issued_f);
+    }
+    __syncthreads();
+
+    const int lane = tid & 31, r = tid >> 5;
+    const int xc = x0 + 4 * lane, y = y0 + r;
+    const bool out_ok = xc < X && y < Y;
+    const int ey = mirror(y, Y);
+    const int lr = ey - y0 + 1, fr = ey - y0;            // row in the v box / f box
+    const int e = H + 4 * lane;                           // column of xc in the v box
+    const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
+    const int64_t orow = (int64_t)y * X + xc;
+    bool ok = true;
+
+    for (int k = 0; k < nf; k++) {
+        const int q = qa + k;
+        if (k == 0) {
+            ok &= mbar_wait(vbar + 0, 0);
+            ok &= mbar_wait(vbar + 1 % RV, (1 / RV) & 1);
+        }
+        ok &= mbar_wait(vbar + (k + 2) % RV, ((k + 2) / RV) & 1);
+        ok &= mbar_wait(fbar + k % RF, (k / RF) & 1);
+        const T *vm = reinterpret_cast<const T *>(vring + (k % RV) * C::VSLOT);
+        const T *vc = reinterpret_cast<const T *>(vring + ((k + 1) % RV) * C::VSLOT);
+        const T *vp = reinterpret_cast<const T *>(vring + ((k + 2) % RV) * C::VSLOT);
+        const T *fs = reinterpret_cast<const T *>(fring + (k % RF) * C::FSLOT);
+
+        float fv[3][4], sqr[4];
+#pragma unroll
+        for (int c = 0; c < 3; c++) P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), fv[c]);
+#pragma unroll
+        for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const int off = (c * (TY + 2) + lr) * BW + e;
+            float cc[4], yp[4], ym[4], zp[4], zm[4];
+            P::unpack(P::load_plain(vc + off), cc);
+            P::unpack(P::load_plain(vc + off + BW), yp);
+            P::unpack(P::load_plain(vc + off - BW), ym);
+            P::unpack(P::load_plain(vp + off), zp);
+            P::unpack(P::load_plain(vm + off), zm);
+            const float xr = Store<ST>::load(vc[off + 4]);
+            const float xl = Store<ST>::load(vc[off - 1]);
+            float res[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float v = cc[i];
+                float lap = -6.0f * v;
+                lap = lap + (i == 3 ? xr : cc[i < 3 ? i + 1 : i]);
+                lap = lap + (i == 0 ? xl : cc[i > 0 ? i - 1 : 0]);
+                lap = lap + yp[i];
+                lap = lap + ym[i];
+                lap = lap + zp[i];
+                lap = lap + zm[i];
+                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+                res[i] = v + upd;
+            }
+            if (xc == 0) res[0] = res[2];
+            if (xc + 4 == X) res[3] = res[1];
+            if (out_ok) {
+                T *o = dst + c * n + orow;
+                P::store(o + (int64_t)q * plane, res);
+                if (q == 2) P::store(o, res);
+                if (q == Z - 3) P::store(o + (int64_t)(Z - 1) * plane, res);
+            }
+        }
+        // slots k % RV (v) and k % RF (f) are free once every thread is here
+        if (__syncthreads_or(!ok)) {
+            ok = false;
+            break;
+        }
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            if (issued_v < nv) {                          // issued_v == k + RV: the slot just freed
+                const int sl = issued_v % RV;
+                zs_issue(vring + sl * C::VSLOT, vbar + sl, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + issued_v);
+                issued_v++;
+            }
+            if (issued_f < nf) {
+                const int sl = issued_f % RF;
+                zs_issue(fring + sl * C::FSLOT, fbar + sl, C::FBOX, &tf, x0, y0, qa + issued_f);
+                issued_f++;
+            }
+        }
+    }
+    if (!ok && tid == 0) {
+        // record the failure and wait (bounded) for this CTA's copies in flight
+        atomicOr(&g_gvf_zs_error, 1);
+        for (int s = 0; s < RV; s++) {
+            int j = issued_v - 1 - ((issued_v - 1 - s) % RV + RV) % RV;
+            if (j >= 0) mbar_wait(vbar + s, (j / RV) & 1);
+        }
+        for (int s = 0; s < RF; s++) {
+            int j = issued_f - 1 - ((issued_f - 1 - s) % RF + RF) % RF;
+            if (j >= 0) mbar_wait(fbar + s, (j / RF) & 1);
+        }
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// 4-D map (x, y, z, component) over a planar field, box (bx, by, 1, 3).
+static bool encode_planar(CUtensorMap *m, const void *base, int X, int Y, int Z, int es, int bx, int by) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, 3};
+    const cuuint64_t strides[3] = {(cuuint64_t)X * es, (cuuint64_t)X * Y * es, (cuuint64_t)X * Y * Z * es};
+    const cuuint32_t box[4] = {(cuuint32_t)bx, (cuuint32_t)by, 1, 3};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(m, es == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                           const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+// Whether the streaming kernel can run this volume: rows a multiple of 16
+// bytes (TMA strides), 16-byte aligned buffers, a driver tensor-map encoder.
+bool gvf_zs_eligible(int st, const void *d_f0, const void *a, const void *b, int X, int Y, int Z) {
+    const int es = (int)storage_bytes(st);
+    if (es == 0 || (X * es) % 16 != 0) return false;
+    if (((uintptr_t)d_f0 | (uintptr_t)a | (uintptr_t)b) & 15) return false;
+    if ((int64_t)X * Y * Z * es * 3 >= ((int64_t)1 << 40)) return false;
+    return tensor_map_encoder() != nullptr;
+}
+
+template <int ST> struct ZsLaunch {
+    int grid = 0, ntx = 0, K = 0;
+};
+
+template <int ST>
+static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
+    using C = ZsCfg<ST>;
+    static int blocks_per_sm[4] = {-1, -1, -1, -1};
+    static int nsm = 0;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (blocks_per_sm[ST] < 0) {
+            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              C::SMEM));
+            int bps = 0;
+            TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST>, C::THREADS,
+                                                                       C::SMEM));
+            int dev = 0;
+            TSF_TRY_CUDA(cudaGetDevice(&dev));
+            TSF_TRY_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            blocks_per_sm[ST] = bps > 0 ? bps : 1;
+        }
+    }
+    g.ntx = (X + C::TX - 1) / C::TX;
+    const int nty = (Y + C::TY - 1) / C::TY;
+    const int64_t cols = (int64_t)g.ntx * nty;
+    const int64_t slots = (int64_t)blocks_per_sm[ST] * nsm;
+    int64_t K = slots / cols;
+    const int64_t kmax = (Z - 2) / 8 > 1 ? (Z - 2) / 8 : 1;   // chunks of at least 8 planes
+    if (K > kmax) K = kmax;
+    if (K < 1) K = 1;
+    if (cols * K > 0x7fffffff) return fail(TSF_ERR_INVALID_ARG, "volume too large for the streaming GVF kernel");
+    g.K = (int)K;
+    g.grid = (int)(cols * K);
+    return TSF_OK;
+}
+
+// One iteration src -> dst with the streaming kernel (caller checked
+// gvf_zs_eligible).
+int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
+                  cudaStream_t s) {
+    int r = TSF_OK;
+    TSF_DISPATCH_STORAGE(st, ST, {
+        using C = ZsCfg<ST>;
+        using T = typename Store<ST>::T;
+        ZsLaunch<ST> g;
+        r = zs_geometry<ST>(X, Y, Z, g);
+        if (r) return r;
+        CUtensorMap tv, tf;
+        if (!encode_planar(&tv, src, X, Y, Z, C::ES, C::BW, C::TY + 2) ||
+            !encode_planar(&tf, d_f0, X, Y, Z, C::ES, C::TX, C::TY))
+            return fail(TSF_ERR_CUDA, "tensor map encoding failed");
+        gvf_zs_kernel<ST><<<g.grid, C::THREADS, C::SMEM, s>>>(tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K);
+    });
+    TSF_CHECK_LAUNCH("gvf_zs_kernel");
+    return r;
+}
+
+// Reads (and optionally clears) the streaming kernel's device error word;
+// -1 if the read itself failed.
+int gvf_zs_error(int clear) {
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_gvf_zs_error, sizeof(int));
+    if (e != cudaSuccess) {
+        check_cuda(e, "read GVF device error word");
+        return -1;
+    }
+    if (clear && v) {
+        const int z = 0;
+        e = cudaMemcpyToSymbol(g_gvf_zs_error, &z, sizeof(int));
+        if (e != cudaSuccess) {
+            check_cuda(e, "clear GVF device error word");
+            return -1;
+        }
+    }
+    return v;
+}
+
+}  // namespace tsf
+
+extern "C" int tsf_gvf_device_error(int clear) { return tsf::gvf_zs_error(clear); }

@@ -69,6 +69,7 @@ def _declare(L):
         "tsf_gvf_workspace_size": (_sz, [_i, _i, _i, _i]),
         "tsf_gvf": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
         "tsf_gvf_mode": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _i, _p]),
+        "tsf_gvf_device_error": (_i, [_i]),
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
         "tsf_gvf_adjoint_workspace_size": (_sz, [_i, _i, _i, _i, _i, _i]),
@@ -100,6 +101,15 @@ def _declare(L):
 
 def kernel_launches() -> int:
     return int(load().tsf_kernel_launches())
+
+
+def gvf_device_error(clear: bool = True) -> int:
+    """The streaming GVF kernel's device error word (0 = none); raises if it
+    cannot be read."""
+    v = int(load().tsf_gvf_device_error(int(clear)))
+    if v < 0:
+        raise TSFError(2, load().tsf_last_error_string().decode())
+    return v
 
 
 def _check(code):
