@@ -27,8 +27,9 @@
 // lane's rows are evaluated at mirror(y) (inside the loaded box because edge
 // tiles are shifted inward); in x the vector holding x = 0 / X-1 copies the
 // result of x = 2 / X-3; the plane q = 2 (Z-3) is also written to plane 0
-// (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's, so the
-// result is bit-identical to the other GVF kernels.
+// (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's -- the same
+// operations in the same order, two voxels per packed f32x2 instruction --
+// so the result is bit-identical to the other GVF kernels.
 #include <mutex>
 
 #include "packed.cuh"
@@ -112,6 +113,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
     const int64_t orow = (int64_t)y * X + xc;
     bool ok = true;
+    // The lane's z column: centre values of planes q-1 and q (carried from
+    // the previous plane, so each stored value is converted once as a centre),
+    // as the voxel pairs (0, 2) and (1, 3) of the lane's 4 voxels.
+    float cm[3][4], cc[3][4];
+    const F2 m6 = f2(-6.0f, -6.0f), mu2 = f2(mu, mu);
 
     for (int k = 0; k < nf; k++) {
         const int q = qa + k;
@@ -121,41 +127,59 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
         }
         ok &= mbar_wait(vbar + (k + 2) % RV, ((k + 2) / RV) & 1);
         ok &= mbar_wait(fbar + k % RF, (k / RF) & 1);
-        const T *vm = reinterpret_cast<const T *>(vring + (k % RV) * C::VSLOT);
         const T *vc = reinterpret_cast<const T *>(vring + ((k + 1) % RV) * C::VSLOT);
         const T *vp = reinterpret_cast<const T *>(vring + ((k + 2) % RV) * C::VSLOT);
         const T *fs = reinterpret_cast<const T *>(fring + (k % RF) * C::FSLOT);
+        if (k == 0) {
+            const T *vm = reinterpret_cast<const T *>(vring);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int off = (c * (TY + 2) + lr) * BW + e;
+                P::unpack(P::load_plain(vm + off), cm[c]);
+                P::unpack(P::load_plain(vc + off), cc[c]);
+            }
+        }
 
-        float fv[3][4], sqr[4];
+        F2 fp[3][2], sq[2];
 #pragma unroll
-        for (int c = 0; c < 3; c++) P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), fv[c]);
+        for (int c = 0; c < 3; c++) {
+            float t[4];
+            P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), t);
+            fp[c][0] = f2(t[0], t[2]);
+            fp[c][1] = f2(t[1], t[3]);
+        }
 #pragma unroll
-        for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+        for (int h = 0; h < 2; h++)       // (f0*f0 + f1*f1) + f2*f2
+            sq[h] = add2(add2(mul2(fp[0][h], fp[0][h]), mul2(fp[1][h], fp[1][h])), mul2(fp[2][h], fp[2][h]));
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const int off = (c * (TY + 2) + lr) * BW + e;
-            float cc[4], yp[4], ym[4], zp[4], zm[4];
-            P::unpack(P::load_plain(vc + off), cc);
+            float yp[4], ym[4], zp[4];
+            P::unpack(P::load_plain(vp + off), zp);
             P::unpack(P::load_plain(vc + off + BW), yp);
             P::unpack(P::load_plain(vc + off - BW), ym);
-            P::unpack(P::load_plain(vp + off), zp);
-            P::unpack(P::load_plain(vm + off), zm);
             const float xr = Store<ST>::load(vc[off + 4]);
             const float xl = Store<ST>::load(vc[off - 1]);
-            float res[4];
-#pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const float v = cc[i];
-                float lap = -6.0f * v;
-                lap = lap + (i == 3 ? xr : cc[i < 3 ? i + 1 : i]);
-                lap = lap + (i == 0 ? xl : cc[i > 0 ? i - 1 : 0]);
-                lap = lap + yp[i];
-                lap = lap + ym[i];
-                lap = lap + zp[i];
-                lap = lap + zm[i];
-                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
-                res[i] = v + upd;
-            }
+            const float *v = cc[c];
+            const F2 v0 = f2(v[0], v[2]), v1 = f2(v[1], v[3]);
+            // lap = -6 v + v[x+1] + v[x-1] + v[y+1] + v[y-1] + v[z+1] + v[z-1], in this order
+            F2 l0 = mul2(m6, v0), l1 = mul2(m6, v1);
+            l0 = add2(l0, v1);
+            l1 = add2(l1, f2(v[2], xr));
+            l0 = add2(l0, f2(xl, v[1]));
+            l1 = add2(l1, v0);
+            l0 = add2(l0, f2(yp[0], yp[2]));
+            l1 = add2(l1, f2(yp[1], yp[3]));
+            l0 = add2(l0, f2(ym[0], ym[2]));
+            l1 = add2(l1, f2(ym[1], ym[3]));
+            l0 = add2(l0, f2(zp[0], zp[2]));
+            l1 = add2(l1, f2(zp[1], zp[3]));
+            l0 = add2(l0, f2(cm[c][0], cm[c][2]));
+            l1 = add2(l1, f2(cm[c][1], cm[c][3]));
+            // v + (mu * lap - (v - f) * |f|^2)
+            const F2 r0 = add2(v0, sub2(mul2(mu2, l0), mul2(sub2(v0, fp[c][0]), sq[0])));
+            const F2 r1 = add2(v1, sub2(mul2(mu2, l1), mul2(sub2(v1, fp[c][1]), sq[1])));
+            float res[4] = {f2lo(r0), f2lo(r1), f2hi(r0), f2hi(r1)};
             if (xc == 0) res[0] = res[2];
             if (xc + 4 == X) res[3] = res[1];
             if (out_ok) {
@@ -163,6 +187,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
                 P::store(o + (int64_t)q * plane, res);
                 if (q == 2) P::store(o, res);
                 if (q == Z - 3) P::store(o + (int64_t)(Z - 1) * plane, res);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                cm[c][i] = cc[c][i];
+                cc[c][i] = zp[i];
             }
         }
         // slots k % RV (v) and k % RF (f) are free once every thread is here

@@ -85,4 +85,43 @@ template <int ST, int BYTES> struct PackedV {
 };
 
 
+// Two FP32 values in one 64-bit register pair, with the packed FP32
+// arithmetic of the sm_100 family (add/sub/mul .rn .f32x2).  Each half is
+// rounded exactly like the scalar instruction (round to nearest, no
+// contraction, subnormals kept), so packed and scalar code give the same bits;
+// one instruction does the work of two.
+struct F2 {
+    unsigned long long r;
+};
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+    F2 o;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(o.r) : "f"(lo), "f"(hi));
+    return o;
+}
+__device__ __forceinline__ float f2lo(F2 a) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.r));
+    return lo;
+}
+__device__ __forceinline__ float f2hi(F2 a) {
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.r));
+    return hi;
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+    F2 o;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+    return o;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+    F2 o;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+    return o;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+    F2 o;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
+    return o;
+}
+
 }  // namespace tsf
