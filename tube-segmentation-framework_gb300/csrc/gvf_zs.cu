@@ -28,8 +28,8 @@
 // tiles are shifted inward); in x the vector holding x = 0 / X-1 copies the
 // result of x = 2 / X-3; the plane q = 2 (Z-3) is also written to plane 0
 // (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's -- the same
-// operations in the same order, two voxels per packed f32x2 instruction --
-// so the result is bit-identical to the other GVF kernels.
+// operations in the same order, sums two voxels per packed f32x2 instruction,
+// products scalar -- so the result is bit-identical to the other GVF kernels.
 #include <mutex>
 
 #include "packed.cuh"
@@ -117,7 +117,6 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
     // the previous plane, so each stored value is converted once as a centre),
     // as the voxel pairs (0, 2) and (1, 3) of the lane's 4 voxels.
     float cm[3][4], cc[3][4];
-    const F2 m6 = f2(-6.0f, -6.0f), mu2 = f2(mu, mu);
 
     for (int k = 0; k < nf; k++) {
         const int q = qa + k;
@@ -140,17 +139,20 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
             }
         }
 
+        float fv[3][4];
         F2 fp[3][2], sq[2];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            float t[4];
-            P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), t);
-            fp[c][0] = f2(t[0], t[2]);
-            fp[c][1] = f2(t[1], t[3]);
+            P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), fv[c]);
+            fp[c][0] = f2(fv[c][0], fv[c][2]);
+            fp[c][1] = f2(fv[c][1], fv[c][3]);
         }
 #pragma unroll
-        for (int h = 0; h < 2; h++)       // (f0*f0 + f1*f1) + f2*f2
-            sq[h] = add2(add2(mul2(fp[0][h], fp[0][h]), mul2(fp[1][h], fp[1][h])), mul2(fp[2][h], fp[2][h]));
+        for (int h = 0; h < 2; h++) {     // (f0*f0 + f1*f1) + f2*f2
+            const int i = h, j = h + 2;
+            sq[h] = add2(add2(f2(fv[0][i] * fv[0][i], fv[0][j] * fv[0][j]), f2(fv[1][i] * fv[1][i], fv[1][j] * fv[1][j])),
+                         f2(fv[2][i] * fv[2][i], fv[2][j] * fv[2][j]));
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const int off = (c * (TY + 2) + lr) * BW + e;
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
             const float *v = cc[c];
             const F2 v0 = f2(v[0], v[2]), v1 = f2(v[1], v[3]);
             // lap = -6 v + v[x+1] + v[x-1] + v[y+1] + v[y-1] + v[z+1] + v[z-1], in this order
-            F2 l0 = mul2(m6, v0), l1 = mul2(m6, v1);
+            F2 l0 = f2(-6.0f * v[0], -6.0f * v[2]), l1 = f2(-6.0f * v[1], -6.0f * v[3]);
             l0 = add2(l0, v1);
             l1 = add2(l1, f2(v[2], xr));
             l0 = add2(l0, f2(xl, v[1]));
@@ -176,9 +178,13 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
             l1 = add2(l1, f2(zp[1], zp[3]));
             l0 = add2(l0, f2(cm[c][0], cm[c][2]));
             l1 = add2(l1, f2(cm[c][1], cm[c][3]));
-            // v + (mu * lap - (v - f) * |f|^2)
-            const F2 r0 = add2(v0, sub2(mul2(mu2, l0), mul2(sub2(v0, fp[c][0]), sq[0])));
-            const F2 r1 = add2(v1, sub2(mul2(mu2, l1), mul2(sub2(v1, fp[c][1]), sq[1])));
+            // v + (mu * lap - (v - f) * |f|^2), products scalar
+            const F2 d0 = sub2(v0, fp[c][0]), d1 = sub2(v1, fp[c][1]);
+            const F2 a0 = f2(mu * f2lo(l0), mu * f2hi(l0)), a1 = f2(mu * f2lo(l1), mu * f2hi(l1));
+            const F2 b0 = f2(f2lo(d0) * f2lo(sq[0]), f2hi(d0) * f2hi(sq[0]));
+            const F2 b1 = f2(f2lo(d1) * f2lo(sq[1]), f2hi(d1) * f2hi(sq[1]));
+            const F2 r0 = add2(v0, sub2(a0, b0));
+            const F2 r1 = add2(v1, sub2(a1, b1));
             float res[4] = {f2lo(r0), f2lo(r1), f2hi(r0), f2hi(r1)};
             if (xc == 0) res[0] = res[2];
             if (xc + 4 == X) res[3] = res[1];
