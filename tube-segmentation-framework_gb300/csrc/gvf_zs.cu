@@ -9,8 +9,8 @@
 // one thread keeps the copies of the next planes in flight while all threads
 // compute the current one, so memory traffic and arithmetic overlap.
 //
-// Work: tile TX x TY outputs (TX = 128; TY = 8 for the 16-bit formats, 4 for
-// FP32), one warp per tile row, 4 consecutive voxels per lane.  The tiles of
+// Work: tile TX x TY = 128 x 8 outputs, one warp per tile row, 4 consecutive
+// voxels per lane.  The tiles of
 // a row / column that would run past the volume are shifted back inside it
 // (they overlap their neighbour and write identical values).  Each tile's z
 // range of evaluation planes [1, Z-2] is split into K chunks, K chosen so that
@@ -27,9 +27,10 @@
 // lane's rows are evaluated at mirror(y) (inside the loaded box because edge
 // tiles are shifted inward); in x the vector holding x = 0 / X-1 copies the
 // result of x = 2 / X-3; the plane q = 2 (Z-3) is also written to plane 0
-// (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's -- the same
-// operations in the same order, sums two voxels per packed f32x2 instruction,
-// products scalar -- so the result is bit-identical to the other GVF kernels.
+// (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's, so the
+// result is bit-identical to the other GVF kernels.  Packed f32x2 sums were
+// tried and lost: they do not raise FP32 throughput here, and the assembler
+// fuses packed multiply-add pairs, which changes the rounding.
 #include <mutex>
 
 #include "packed.cuh"
@@ -41,10 +42,11 @@ template <int ST> struct ZsCfg {
     using T = typename Store<ST>::T;
     static constexpr int ES = (int)sizeof(T);
     static constexpr int TX = 128;
-    static constexpr int TY = ES == 2 ? 8 : 4;
+    static constexpr int TY = 8;
     static constexpr int H = 16 / ES;                      // x halo, elements
     static constexpr int BW = TX + 2 * H;                  // v box width
-    static constexpr int RV = 5, RF = 4;                   // ring slots
+    // ring slots: 16-bit formats 68 KB per CTA (3 per SM), FP32 102 KB (2 per SM)
+    static constexpr int RV = ES == 2 ? 5 : 4, RF = ES == 2 ? 4 : 3;
     static constexpr int VBOX = BW * (TY + 2) * 3 * ES;    // bytes of one v box
     static constexpr int FBOX = TX * TY * 3 * ES;
     static constexpr int VSLOT = (VBOX + 127) / 128 * 128;
@@ -107,92 +109,73 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
     const int lane = tid & 31, r = tid >> 5;
     const int xc = x0 + 4 * lane, y = y0 + r;
     const bool out_ok = xc < X && y < Y;
+    const bool fix_lo = xc == 0, fix_hi = xc + 4 == X;   // vectors holding x = 0 / X-1
     const int ey = mirror(y, Y);
     const int lr = ey - y0 + 1, fr = ey - y0;            // row in the v box / f box
     const int e = H + 4 * lane;                           // column of xc in the v box
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
-    const int64_t orow = (int64_t)y * X + xc;
+    T *o = dst + (int64_t)y * X + xc + (int64_t)qa * plane;   // component 0, plane q
+    const int voff = lr * BW + e, vstride = (TY + 2) * BW;    // component c at voff + c * vstride
+    const int foff = fr * TX + 4 * lane;
     bool ok = true;
-    // The lane's z column: centre values of planes q-1 and q (carried from
-    // the previous plane, so each stored value is converted once as a centre),
-    // as the voxel pairs (0, 2) and (1, 3) of the lane's 4 voxels.
+    // The lane's z column: centre values of planes q-1 and q, carried from
+    // the previous plane so each stored value is loaded and converted once as
+    // a centre.
     float cm[3][4], cc[3][4];
+    int sc = 1, sp = 2, sf = 0;                           // slots of v planes q, q+1 and f plane q
+    uint32_t pp = 0, pf = 0;                              // phase parity of the waits on sp, sf
+    ok &= mbar_wait(vbar + 0, 0);
+    ok &= mbar_wait(vbar + 1, 0);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        P::unpack(P::load_plain(reinterpret_cast<const T *>(vring) + voff + c * vstride), cm[c]);
+        P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), cc[c]);
+    }
 
     for (int k = 0; k < nf; k++) {
         const int q = qa + k;
-        if (k == 0) {
-            ok &= mbar_wait(vbar + 0, 0);
-            ok &= mbar_wait(vbar + 1 % RV, (1 / RV) & 1);
-        }
-        ok &= mbar_wait(vbar + (k + 2) % RV, ((k + 2) / RV) & 1);
-        ok &= mbar_wait(fbar + k % RF, (k / RF) & 1);
-        const T *vc = reinterpret_cast<const T *>(vring + ((k + 1) % RV) * C::VSLOT);
-        const T *vp = reinterpret_cast<const T *>(vring + ((k + 2) % RV) * C::VSLOT);
-        const T *fs = reinterpret_cast<const T *>(fring + (k % RF) * C::FSLOT);
-        if (k == 0) {
-            const T *vm = reinterpret_cast<const T *>(vring);
-#pragma unroll
-            for (int c = 0; c < 3; c++) {
-                const int off = (c * (TY + 2) + lr) * BW + e;
-                P::unpack(P::load_plain(vm + off), cm[c]);
-                P::unpack(P::load_plain(vc + off), cc[c]);
-            }
-        }
+        ok &= mbar_wait(vbar + sp, pp);
+        ok &= mbar_wait(fbar + sf, pf);
+        const T *vc = reinterpret_cast<const T *>(vring + sc * C::VSLOT) + voff;
+        const T *vp = reinterpret_cast<const T *>(vring + sp * C::VSLOT) + voff;
+        const T *fs = reinterpret_cast<const T *>(fring + sf * C::FSLOT) + foff;
+        const bool dup_lo = q == 2, dup_hi = q == Z - 3;
 
-        float fv[3][4];
-        F2 fp[3][2], sq[2];
+        float fv[3][4], sqr[4];
+#pragma unroll
+        for (int c = 0; c < 3; c++) P::unpack(P::load_plain(fs + c * TY * TX), fv[c]);
+#pragma unroll
+        for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            P::unpack(P::load_plain(fs + (c * TY + fr) * TX + 4 * lane), fv[c]);
-            fp[c][0] = f2(fv[c][0], fv[c][2]);
-            fp[c][1] = f2(fv[c][1], fv[c][3]);
-        }
-#pragma unroll
-        for (int h = 0; h < 2; h++) {     // (f0*f0 + f1*f1) + f2*f2
-            const int i = h, j = h + 2;
-            sq[h] = add2(add2(f2(fv[0][i] * fv[0][i], fv[0][j] * fv[0][j]), f2(fv[1][i] * fv[1][i], fv[1][j] * fv[1][j])),
-                         f2(fv[2][i] * fv[2][i], fv[2][j] * fv[2][j]));
-        }
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const int off = (c * (TY + 2) + lr) * BW + e;
+            const T *pc = vc + c * vstride;
             float yp[4], ym[4], zp[4];
-            P::unpack(P::load_plain(vp + off), zp);
-            P::unpack(P::load_plain(vc + off + BW), yp);
-            P::unpack(P::load_plain(vc + off - BW), ym);
-            const float xr = Store<ST>::load(vc[off + 4]);
-            const float xl = Store<ST>::load(vc[off - 1]);
-            const float *v = cc[c];
-            const F2 v0 = f2(v[0], v[2]), v1 = f2(v[1], v[3]);
-            // lap = -6 v + v[x+1] + v[x-1] + v[y+1] + v[y-1] + v[z+1] + v[z-1], in this order
-            F2 l0 = f2(-6.0f * v[0], -6.0f * v[2]), l1 = f2(-6.0f * v[1], -6.0f * v[3]);
-            l0 = add2(l0, v1);
-            l1 = add2(l1, f2(v[2], xr));
-            l0 = add2(l0, f2(xl, v[1]));
-            l1 = add2(l1, v0);
-            l0 = add2(l0, f2(yp[0], yp[2]));
-            l1 = add2(l1, f2(yp[1], yp[3]));
-            l0 = add2(l0, f2(ym[0], ym[2]));
-            l1 = add2(l1, f2(ym[1], ym[3]));
-            l0 = add2(l0, f2(zp[0], zp[2]));
-            l1 = add2(l1, f2(zp[1], zp[3]));
-            l0 = add2(l0, f2(cm[c][0], cm[c][2]));
-            l1 = add2(l1, f2(cm[c][1], cm[c][3]));
-            // v + (mu * lap - (v - f) * |f|^2), products scalar
-            const F2 d0 = sub2(v0, fp[c][0]), d1 = sub2(v1, fp[c][1]);
-            const F2 a0 = f2(mu * f2lo(l0), mu * f2hi(l0)), a1 = f2(mu * f2lo(l1), mu * f2hi(l1));
-            const F2 b0 = f2(f2lo(d0) * f2lo(sq[0]), f2hi(d0) * f2hi(sq[0]));
-            const F2 b1 = f2(f2lo(d1) * f2lo(sq[1]), f2hi(d1) * f2hi(sq[1]));
-            const F2 r0 = add2(v0, sub2(a0, b0));
-            const F2 r1 = add2(v1, sub2(a1, b1));
-            float res[4] = {f2lo(r0), f2lo(r1), f2hi(r0), f2hi(r1)};
-            if (xc == 0) res[0] = res[2];
-            if (xc + 4 == X) res[3] = res[1];
+            P::unpack(P::load_plain(vp + c * vstride), zp);
+            P::unpack(P::load_plain(pc + BW), yp);
+            P::unpack(P::load_plain(pc - BW), ym);
+            const float xr = Store<ST>::load(pc[4]);
+            const float xl = Store<ST>::load(pc[-1]);
+            float res[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const float v = cc[c][i];
+                float lap = -6.0f * v;
+                lap = lap + (i == 3 ? xr : cc[c][i < 3 ? i + 1 : i]);
+                lap = lap + (i == 0 ? xl : cc[c][i > 0 ? i - 1 : 0]);
+                lap = lap + yp[i];
+                lap = lap + ym[i];
+                lap = lap + zp[i];
+                lap = lap + cm[c][i];
+                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+                res[i] = v + upd;
+            }
+            if (fix_lo) res[0] = res[2];
+            if (fix_hi) res[3] = res[1];
             if (out_ok) {
-                T *o = dst + c * n + orow;
-                P::store(o + (int64_t)q * plane, res);
-                if (q == 2) P::store(o, res);
-                if (q == Z - 3) P::store(o + (int64_t)(Z - 1) * plane, res);
+                T *oc = o + c * n;
+                P::store(oc, res);
+                if (dup_lo) P::store(oc - 2 * plane, res);
+                if (dup_hi) P::store(oc + 2 * plane, res);
             }
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -200,6 +183,12 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
                 cc[c][i] = zp[i];
             }
         }
+        o += plane;
+        sc = sp;
+        sp = sp + 1 == RV ? 0 : sp + 1;
+        pp ^= sp == 0;
+        sf = sf + 1 == RF ? 0 : sf + 1;
+        pf ^= sf == 0;
         // slots k % RV (v) and k % RF (f) are free once every thread is here
         if (__syncthreads_or(!ok)) {
             ok = false;

@@ -85,40 +85,4 @@ template <int ST, int BYTES> struct PackedV {
 };
 
 
-// Two FP32 values in one 64-bit register pair, with the packed FP32 adds and
-// subtracts of the sm_100 family (add/sub .rn .f32x2).  Each half is rounded
-// exactly like the scalar instruction, so packed and scalar sums give the same
-// bits and one instruction does the work of two.  Products stay scalar: the
-// assembler contracts a packed multiply feeding a packed add into a packed
-// fused multiply-add (one rounding) even under -fmad=false, with an explicit
-// .rn, in volatile asm, or written as fma(a, b, -0); a scalar product feeding
-// a packed add is left alone (measured on GB300 over 2^20 operand pairs).
-struct F2 {
-    unsigned long long r;
-};
-__device__ __forceinline__ F2 f2(float lo, float hi) {
-    F2 o;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(o.r) : "f"(lo), "f"(hi));
-    return o;
-}
-__device__ __forceinline__ float f2lo(F2 a) {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.r));
-    return lo;
-}
-__device__ __forceinline__ float f2hi(F2 a) {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.r));
-    return hi;
-}
-__device__ __forceinline__ F2 add2(F2 a, F2 b) {
-    F2 o;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
-    return o;
-}
-__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
-    F2 o;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(o.r) : "l"(a.r), "l"(b.r));
-    return o;
-}
 }  // namespace tsf
