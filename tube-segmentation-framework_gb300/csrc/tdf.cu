@@ -69,14 +69,19 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 //
 // With one voxel per lane, a warp runs as many radii as its slowest voxel
 // needs (about half the voxels stop at the first radius, others go on to 3-6),
-// which left ~60 % of the lanes idle.  Here a warp owns a row segment of
-// kSeg voxels: it first decomposes all their Hessians (one voxel per lane,
-// kSeg / 32 rounds) into shared memory, then treats each voxel's sweep as a
-// task: a lane evaluates one radius (its 32 samples, in order) per round and,
-// when its voxel's sweep ends, takes the next unstarted voxel of the segment,
-// in lane order.  Lanes stay busy until the segment's queue drains, the samples
-// of neighbouring lanes stay spatially close (L1 hits), and each voxel's
-// arithmetic is exactly that of tdf_circle_kernel.
+// which left ~60 % of the lanes idle.  Here a warp owns kSeg = 128 voxels: it
+// first decomposes all their Hessians (one voxel per lane, 4 rounds) into
+// shared memory, then treats each voxel's sweep as a task: a lane evaluates
+// one radius (its 32 samples, in order) per round and, when its voxel's sweep
+// ends, takes the next unstarted voxel, in lane order.  Lanes stay busy until
+// the queue drains, and each voxel's arithmetic is exactly that of
+// tdf_circle_kernel.
+//
+// Locality: a warp's voxels form an 8 x 4 x 4 block and a CTA's four warps an
+// 8 x 8 x 8 brick, so the circles sampled by a CTA stay within a
+// (8 + 2 rmax)^3 neighbourhood that L1 can hold (row segments of 128 voxels
+// touched ~5x more distinct lines and missed L1 for about a quarter of the
+// trilinear corners).
 constexpr int kSeg = 128;
 constexpr int kTdfWarps = 4;
 
@@ -84,21 +89,25 @@ template <int ST, bool NORM, bool UNORM>
 __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                                     float rmin, float rmax, float rstep,
                                                                     const CircleTable tab, void *T,
-                                                                    float *__restrict__ Rout, int nseg_x) {
+                                                                    float *__restrict__ Rout) {
+    static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t seg = (int64_t)blockIdx.x * kTdfWarps + w;
-    const int64_t nseg = (int64_t)nseg_x * Y * Z;
-    if (seg >= nseg) return;                         // whole warp
-    const int sx = (int)(seg % nseg_x);
-    const int y = (int)((seg / nseg_x) % Y);
-    const int z = (int)(seg / ((int64_t)nseg_x * Y));
-    const int xb = sx * kSeg;
-    const int ntask = min(kSeg, X - xb);
-    // phase 1: eigenvectors of the segment's voxels
+    // brick of this CTA, block of this warp: task t -> (t & 7, (t >> 3) & 3, t >> 5)
+    const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
+    const int b = blockIdx.x;
+    const int bx0 = (b % nbx) * 8, by0 = ((b / nbx) % nby) * 8 + (w & 1) * 4;
+    const int bz0 = (b / (nbx * nby)) * 8 + (w >> 1) * 4;
+    const int ntask = kSeg;
+    auto tx = [&](int t) { return bx0 + (t & 7); };
+    auto ty = [&](int t) { return by0 + ((t >> 3) & 3); };
+    auto tz = [&](int t) { return bz0 + (t >> 5); };
+    auto inside = [&](int t) { return tx(t) < X && ty(t) < Y && tz(t) < Z; };
+    // phase 1: eigenvectors of the block's voxels
     for (int t = lane; t < ntask; t += 32) {
+        if (!inside(t)) continue;
         float H[3][3], V[3][3], d[3];
-        hessian<ST, NORM>(F, X, Y, Z, xb + t, y, z, H);
+        hessian<ST, NORM>(F, X, Y, Z, tx(t), ty(t), tz(t), H);
         eig3<float>(H, V, d);
         se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
         se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
@@ -112,10 +121,10 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
     int nr = 0;
     while (__any_sync(full, task >= 0)) {
         bool done = true;
-        if (task >= 0) {
+        if (task >= 0 && inside(task)) {
             const float e2x = se[w][0][task], e2y = se[w][1][task], e2z = se[w][2][task];
             const float e3x = se[w][3][task], e3y = se[w][4][task], e3z = se[w][5][task];
-            const float fx = (float)(xb + task), fy = (float)y, fz = (float)z;
+            const float fx = (float)tx(task), fy = (float)ty(task), fz = (float)tz(task);
             if (radius <= rmax && nr < kMaxRadii) {
                 float rs = 0.0f;
 #pragma unroll 4
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                 }
             }
             if (done) {
-                const int64_t i = lin(xb + task, y, z, X, Y);
+                const int64_t i = lin(tx(task), ty(task), tz(task), X, Y);
                 if (UNORM) reinterpret_cast<uint16_t *>(T)[i] = to_unorm16(maxSum);
                 else reinterpret_cast<float *>(T)[i] = maxSum;
                 Rout[i] = maxRadius;
@@ -184,15 +193,13 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
     const CircleTable tab = host_circle_table();
     const dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
     const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
-    const int nseg_x = (X + kSeg - 1) / kSeg;
-    const int64_t nseg = (int64_t)nseg_x * Y * Z;
-    const unsigned qblocks = (unsigned)((nseg + kTdfWarps - 1) / kTdfWarps);
+    const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
     const bool queue = tdf_mode != 1;
 #define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
     do {                                                                                                             \
         if (queue)                                                                                                   \
             tdf_queue_kernel<ST, NORM, UN><<<qblocks, 32 * kTdfWarps, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, \
-                                                                              tab, d_T, d_R, nseg_x);                \
+                                                                              tab, d_T, d_R);                        \
         else                                                                                                         \
             tdf_circle_kernel<ST, NORM, UN><<<g, b, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R);    \
     } while (0)
