@@ -432,7 +432,8 @@ def fwd_adjoint_timing(torch, pipe, args):
     mark()
     g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, "f32")
     mark()
-    g_f0, _ = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, "f32", ws=state["gvf_ws"], checkpoints_stored=True)
+    g_f0, _ = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, "f32", state["checkpoint_every"],
+                            ws=state["gvf_ws"], checkpoints_stored=True)
     mark()
     gI2 = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
     g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)
@@ -442,7 +443,8 @@ def fwd_adjoint_timing(torch, pipe, args):
     names = ["tdf_small_backward", "tdf_large_backward", "gvf_adjoint", "vector_field_and_blur_backward"]
     bw = {k: round(marks[i].elapsed_time(marks[i + 1]), 3) for i, k in enumerate(names)}
     return {"storage": "f32", "iterations": args.iters, "volume": list(vol.shape), "backward_ms": bw,
-            "checkpoint_every": int(np.ceil(np.sqrt(args.iters))),
+            "checkpoint_every": int(state["checkpoint_every"]),
+            "adjoint_workspace_gb": round(state["gvf_ws"].numel() / 1e9, 2),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
 

@@ -172,13 +172,20 @@ int tsf_gvf_static(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, i
 size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iterations,
                                       int checkpoint_every);
 
+/* Smallest checkpoint interval whose tsf_gvf_adjoint workspace fits in
+ * budget_bytes: 1 keeps every forward state and recomputes nothing; 0 if no
+ * interval fits.  No counterpart in the reference. */
+int tsf_gvf_adjoint_checkpoint_interval(int X, int Y, int Z, int storage, int iterations,
+                                        size_t budget_bytes);
+
 /* Reverse-mode derivative of `iterations` GVF Jacobi iterations started from
  * v_0 = f0 (no counterpart in the reference, which has no derivatives).
  * Given d_gv = dL/dv_K (planar FP32), writes dL/df0 (planar FP32, all paths
  * through the data term, |f0|^2 and v_0) to d_gf0 and dL/dmu to *dmu (host,
  * FP64; NULL to skip -- otherwise the call synchronises `stream`).  Forward
- * states are recomputed from checkpoints kept every `checkpoint_every`
- * iterations (<= 0: ceil(sqrt(iterations))); memory (K/C + C) states.
+ * states are recomputed from checkpoints kept every C = `checkpoint_every`
+ * iterations (<= 0: ceil(sqrt(iterations))); the workspace holds about
+ * K/C + C states (C = 1: all K-1 states, no recomputation).
  * flags bit 0: the checkpoints are already in the workspace
  * (tsf_gvf_checkpointed ran with the same arguments). */
 int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,

@@ -34,6 +34,29 @@ def test_workspace_queries(tsf):
     assert L.tsf_gvf_fmg_workspace_size(64, 64, 64, 1) > 3 * n * 2
 
 
+def test_adjoint_checkpoint_interval(tsf):
+    """The smallest interval whose workspace fits the budget: every state
+    when there is room, about sqrt(K) when memory is tight, 0 when nothing
+    fits."""
+    L = tsf.load()
+    X = Y = Z = 64
+    K = 100
+    ws = lambda C: L.tsf_gvf_adjoint_workspace_size(X, Y, Z, 0, K, C)
+    state = 3 * X * Y * Z * 4
+    assert ws(1) >= (K - 1) * state and ws(1) < (K + 2) * state
+    assert L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, ws(1)) == 1
+    assert L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, 1 << 50) == 1
+    assert L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, ws(1) - 1) > 1
+    best = min(ws(C) for C in range(1, K + 1))
+    C = L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, best)
+    assert C > 1 and ws(C) == best and all(ws(c) > best for c in range(1, C))
+    assert L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, best - 1) == 0
+    for budget in (ws(1) // 2, ws(1) // 5, ws(1) // 9):
+        C = L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, budget)
+        assert C > 1 and ws(C) <= budget
+        assert all(ws(c) > budget for c in range(1, C))
+
+
 def test_blur_mask_matches_oracle(tsf, oracle):
     for sigma in (0.5, 1.0, 1.7, 3.0):
         m, mask = tsf.blur_mask(sigma)

@@ -74,12 +74,21 @@ def _field(tsf, synth, shape, seed):
     return f0
 
 
-@pytest.mark.parametrize("shape,K,C", [((16, 18, 20), 12, 0), ((13, 9, 24), 10, 3), ((8, 8, 8), 7, 7)])
+@pytest.mark.parametrize("shape,K,C", [((16, 18, 20), 12, 0), ((13, 9, 24), 10, 3), ((8, 8, 8), 7, 7),
+                                       ((12, 10, 16), 9, 1), ((12, 10, 16), 1, 0), ((12, 10, 16), 8, 20)])
 def test_adjoint_matches_fp64_autograd(torch_dev, tsf, synth, shape, K, C):
+    """C = 0: sqrt(K) checkpoints; C = 1: every state kept; C = 3: a short
+    last segment; C >= K: one segment, all states from the forward pass."""
     torch = torch_dev
     f0 = _field(tsf, synth, shape, 3)
     gv = torch.randn(f0.shape, generator=torch.Generator().manual_seed(1)).float().cuda()
     gf, dmu = tsf.gvf_adjoint(f0, 0.05, K, gv, "f32", checkpoint_every=C)
+    # the same through a checkpointed forward whose states the adjoint reuses
+    ws = tsf.gvf_adjoint_workspace(f0, K, "f32", C)
+    vK = tsf.gvf_checkpointed(f0, 0.05, K, ws, "f32", C)
+    assert torch.equal(vK, tsf.gvf(f0, 0.05, K, "f32"))
+    gf2, dmu2 = tsf.gvf_adjoint(f0, 0.05, K, gv, "f32", C, ws=ws, checkpoints_stored=True)
+    assert torch.equal(gf, gf2) and dmu == dmu2
     f64 = f0.double().cpu().requires_grad_(True)
     mu64 = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
     v = torch_gvf(f64, mu64, K)

@@ -21,6 +21,10 @@ import tsf_gb300 as T
 
 
 class Params:
+    """checkpoint_every: GVF adjoint checkpoint interval; 0 = the smallest
+    interval whose workspace fits in 60 % of the free device memory (1, no
+    recomputation, whenever all states fit), else sqrt(K)."""
+
     def __init__(self, mu=0.05, sigma=0.5, iterations=300, fmax=0.2, vsign=1, rmin=1.0, rmax=7.0, rstep=0.5,
                  checkpoint_every=0):
         self.mu, self.sigma, self.iterations = mu, sigma, iterations
@@ -38,13 +42,14 @@ def forward(vol, p: Params):
     Ts, Rs = T.tdf_circle(f_s, p.rmin, 3.0, 0.5, st)
     b = T.blur(vol, p.sigma)
     f0, _ = T.vector_field(b, p.fmax, p.vsign, st, planar=True, field4=False)
-    ws = T.gvf_adjoint_workspace(f0, p.iterations, st, p.checkpoint_every)
-    v = T.gvf_checkpointed(f0, p.mu, p.iterations, ws, st, p.checkpoint_every)
+    C = p.checkpoint_every if p.checkpoint_every > 0 else T.gvf_adjoint_interval(f0, p.iterations, st)
+    ws = T.gvf_adjoint_workspace(f0, p.iterations, st, C)
+    v = T.gvf_checkpointed(f0, p.mu, p.iterations, ws, st, C)
     F = T.gvf_finish(v, st)
     Tl, Rl = T.tdf_circle(F, max(2.5, p.rmin), p.rmax, p.rstep, st)
     small = Ts > Tl                       # combine (kernels.cl:561-572): T_l < T_s -> take T_s
     Tc = torch.where(small, Ts, Tl)
-    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small, gvf_ws=ws)
+    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small, gvf_ws=ws, checkpoint_every=C)
     return Tc, s
 
 
@@ -61,8 +66,8 @@ def backward(state, gT, p: Params):
     gI = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
     # large pass -> GVF -> vector field -> blur
     g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, st)
-    g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, p.checkpoint_every, ws=state["gvf_ws"],
-                              checkpoints_stored=True)
+    g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, state["checkpoint_every"],
+                              ws=state["gvf_ws"], checkpoints_stored=True)
     g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)
     gI, dsigma = T.blur_backward(vol, g_b, p.sigma, gin=gI)
     return gI, dmu, dsigma

@@ -14,19 +14,19 @@
 // and, since v_0 = f0 (GVF3DInit), dL/df0 += lambda_0 at the end.
 // Storage rounding of the forward states is treated as the identity.
 //
-// Checkpointing: the forward states v_0, v_C, v_2C, ... are kept (C =
+// Checkpointing: the forward states v_C, v_2C, ... are kept (v_0 is f0; C =
 // checkpoint interval, ceil(sqrt(K)) by default); each segment is recomputed
-// from its checkpoint into a C-state buffer and then reversed, so the memory is
-// (K/C + C) states and the extra work one forward pass.  Cotangents are FP32;
+// from its checkpoint into a (C-1)-state buffer and then reversed, so the
+// memory is about K/C + C states and the extra work at most one forward pass.
+// The last segment's states are left in the buffer by the forward pass, and
+// C = 1 (every state kept, K-1 states: 100 GB for 500 FP32 iterations at
+// 256^3, which fits GB300's HBM) recomputes nothing.  Cotangents are FP32;
 // the mu derivative is accumulated in FP64, per block in a fixed order, so the
 // result does not depend on scheduling.
 #include "tsf_common.cuh"
 
 namespace tsf {
 
-int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st, void *ws,
-            size_t ws_bytes, int mode, cudaStream_t s);
-size_t gvf_workspace_size(int X, int Y, int Z, int st);
 int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s);
 
 // folded cotangent at (x, y, z): sum of lambda' over the voxels that mirror to it
@@ -157,7 +157,7 @@ __global__ void fold_axis_kernel(float *__restrict__ g, int X, int Y, int Z, int
 //     lambda = g (1 - 6 mu - s) + mu sum_6 g,   gf += g s - 2 f sum_d g_d (v_d - f_d),
 //     dmu += sum_c g_c L(v_c)   (L with clamped reads: g = 0 wherever L would clamp).
 template <int ST>
-__global__ void __launch_bounds__(256) gvf_adjoint_stencil_kernel(const float *__restrict__ gin,
+__global__ void __launch_bounds__(256, 3) gvf_adjoint_stencil_kernel(const float *__restrict__ gin,
                                                                   const typename Store<ST>::T *__restrict__ v,
                                                                   const typename Store<ST>::T *__restrict__ f,
                                                                   float *__restrict__ lam_out, float *__restrict__ gf,
@@ -287,7 +287,7 @@ static size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 struct AdjLayout {
     int C, nck;
-    size_t state, ck, seg, lam0, lam1, dmu, dmu_out, gvf_ws, bytes;
+    size_t state, ck, seg, lam0, lam1, dmu, dmu_out, bytes;
     int64_t nblocks;
 };
 
@@ -297,12 +297,18 @@ static dim3 adj_grid(int X, int Y, int Z) { return dim3((X + 31) / 32, (Y + 3) /
 static dim3 adjv_block() { return dim3(32, 8, 1); }
 static dim3 adjv_grid(int X, int Y, int Z) { return dim3((X / 4 + 31) / 32, (Y + 7) / 8, Z); }
 
+static int default_interval(int K) {
+    int C = 1;
+    while (C * C < K) C++;
+    return C;
+}
+
+// Workspace: checkpoints v_C, v_2C, ... (v_0 is f0 itself), a segment buffer
+// for the C - 1 states after a checkpoint, two cotangent buffers and the mu
+// partials.  C = 1 keeps every state and recomputes nothing.
 static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
     AdjLayout L;
-    if (C <= 0) {
-        C = 1;
-        while (C * C < K) C++;
-    }
+    if (C <= 0) C = default_interval(K);
     L.C = C;
     L.nck = K > 0 ? (K + C - 1) / C : 0;
     const size_t n = (size_t)X * Y * Z;
@@ -310,13 +316,12 @@ static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
     const dim3 g = adj_grid(X, Y, Z), gv = adjv_grid(X, Y, Z);
     L.nblocks = (int64_t)g.x * g.y * g.z + (adj_vec(X) ? (int64_t)gv.x * gv.y * gv.z : 0);
     size_t off = 0;
-    L.ck = off; off += L.state * (size_t)L.nck;
-    L.seg = off; off += L.state * (size_t)C;
+    L.ck = off; off += L.state * (size_t)(L.nck > 1 ? L.nck - 1 : 0);
+    L.seg = off; off += L.state * (size_t)(C - 1);
     L.lam0 = off; off += al256(3 * n * sizeof(float));
     L.lam1 = off; off += al256(3 * n * sizeof(float));
     L.dmu = off; off += al256(sizeof(double) * (size_t)L.nblocks);
     L.dmu_out = off; off += 256;
-    L.gvf_ws = off; off += al256(gvf_workspace_size(X, Y, Z, st));
     L.bytes = off;
     return L;
 }
@@ -325,8 +330,28 @@ size_t gvf_adjoint_workspace_size(int X, int Y, int Z, int st, int K, int C) {
     return adj_layout(X, Y, Z, st, K, C).bytes;
 }
 
-// Forward pass keeping the checkpoints v_0, v_C, ... in the adjoint workspace;
-// the result v_K goes to d_v (may be NULL).
+// Smallest checkpoint interval whose workspace fits `budget` bytes (1 = keep
+// every state); 0 if even the smallest workspace does not fit.
+int gvf_adjoint_interval(int X, int Y, int Z, int st, int K, size_t budget) {
+    if (K <= 0) return 1;
+    for (int C = 1; C <= K; C++) {
+        if (adj_layout(X, Y, Z, st, K, C).bytes <= budget) return C;
+        if ((int64_t)C * C > 4 * (int64_t)K) break;   // past the minimum near sqrt(K)
+    }
+    return 0;
+}
+
+// state k of the segment that starts at checkpoint i (k = i*C + t)
+static inline const void *ck_state(const AdjLayout &L, const void *d_f0, char *w, int i) {
+    return i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
+}
+static inline void *seg_state(const AdjLayout &L, char *w, int t) {   // t = 1 .. C-1
+    return w + L.seg + (size_t)(t - 1) * L.state;
+}
+
+// Forward pass storing the checkpoints v_C, v_2C, ... and the states of the
+// last segment; v_K goes to d_v (may be NULL).  Every state is written once,
+// straight into its slot.
 int run_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int K, int st, int C, void *ws,
                          size_t ws_bytes, cudaStream_t s) {
     int r = check_dims(X, Y, Z);
@@ -338,24 +363,22 @@ int run_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float
     if (!ws || ws_bytes < L.bytes) return fail(TSF_ERR_WORKSPACE, "GVF adjoint workspace too small");
     char *w = (char *)ws;
     const size_t state_bytes = 3 * (size_t)X * Y * Z * storage_bytes(st);
-    void *gws = w + L.gvf_ws;
-    const size_t gws_bytes = gvf_workspace_size(X, Y, Z, st);
     for (int i = 0; i < L.nck; i++) {
-        void *ck = w + L.ck + (size_t)i * L.state;
-        const void *prev = i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
-        TSF_TRY_CUDA(cudaMemcpyAsync(ck, prev, state_bytes, cudaMemcpyDeviceToDevice, s));
-        if (i > 0) {
-            r = run_gvf(d_f0, ck, X, Y, Z, mu, L.C, st, gws, gws_bytes, 0, s);
+        const int k0 = i * L.C, k1 = (k0 + L.C < K) ? k0 + L.C : K;
+        const bool last = i == L.nck - 1;
+        const void *src = ck_state(L, d_f0, w, i);
+        for (int k = k0 + 1; k <= k1; k++) {
+            void *dst;
+            if (k < k1) dst = seg_state(L, w, k - k0);          // inside the segment
+            else if (!last) dst = (void *)ck_state(L, d_f0, w, i + 1);
+            else if (d_v) dst = d_v;                            // v_K
+            else break;
+            r = gvf_step(st, d_f0, src, dst, X, Y, Z, mu, s);
             if (r) return r;
+            src = dst;
         }
     }
-    if (d_v) {
-        const void *last = L.nck > 0 ? (const void *)(w + L.ck + (size_t)(L.nck - 1) * L.state) : d_f0;
-        TSF_TRY_CUDA(cudaMemcpyAsync(d_v, last, state_bytes, cudaMemcpyDeviceToDevice, s));
-        const int done = L.nck > 0 ? (L.nck - 1) * L.C : 0;
-        r = run_gvf(d_f0, d_v, X, Y, Z, mu, K - done, st, gws, gws_bytes, 0, s);
-        if (r) return r;
-    }
+    if (d_v && L.nck == 0) TSF_TRY_CUDA(cudaMemcpyAsync(d_v, d_f0, state_bytes, cudaMemcpyDeviceToDevice, s));
     return TSF_OK;
 }
 
@@ -370,47 +393,38 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
     if (!ws || ws_bytes < L.bytes) return fail(TSF_ERR_WORKSPACE, "GVF adjoint workspace too small");
     char *w = (char *)ws;
     const int64_t n = (int64_t)X * Y * Z;
-    const size_t sb = storage_bytes(st);
-    const size_t state_bytes = 3 * (size_t)n * sb;
     float *lam = (float *)(w + L.lam0), *lam2 = (float *)(w + L.lam1);
     double *dmu_b = (double *)(w + L.dmu);
     TSF_TRY_CUDA(cudaMemsetAsync(d_gf0, 0, sizeof(float) * 3 * (size_t)n, s));
     TSF_TRY_CUDA(cudaMemsetAsync(dmu_b, 0, sizeof(double) * (size_t)L.nblocks, s));
     TSF_TRY_CUDA(cudaMemcpyAsync(lam, d_gv, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    void *gws = w + L.gvf_ws;
-    const size_t gws_bytes = gvf_workspace_size(X, Y, Z, st);
 
-    // forward pass keeping checkpoints v_0, v_C, ... (unless a checkpointed
-    // forward already stored them)
-    for (int i = 0; i < L.nck && !(flags & 1); i++) {
-        void *ck = w + L.ck + (size_t)i * L.state;
-        const void *prev = i == 0 ? d_f0 : (const void *)(w + L.ck + (size_t)(i - 1) * L.state);
-        TSF_TRY_CUDA(cudaMemcpyAsync(ck, prev, state_bytes, cudaMemcpyDeviceToDevice, s));
-        if (i > 0) {
-            r = run_gvf(d_f0, ck, X, Y, Z, mu, L.C, st, gws, gws_bytes, 1, s);
-            if (r) return r;
-        }
+    // forward pass storing the checkpoints and the last segment (unless a
+    // checkpointed forward with the same arguments already did)
+    if (!(flags & 1)) {
+        r = run_gvf_checkpointed(d_f0, nullptr, X, Y, Z, mu, K, st, L.C, ws, ws_bytes, s);
+        if (r) return r;
     }
+    // the cotangent kernels move 16-byte vectors
+    const bool vec = adj_vec(X) && ((uintptr_t)d_gf0 & 15) == 0 && ((uintptr_t)w & 15) == 0;
+    const dim3 g = adj_grid(X, Y, Z);
+    double *dmu_v = dmu_b + (int64_t)g.x * g.y * g.z;
     // reverse, one segment at a time
     for (int seg = L.nck - 1; seg >= 0; seg--) {
         const int k0 = seg * L.C, k1 = (k0 + L.C < K) ? k0 + L.C : K;
-        // states k0 .. k1-1 into the segment buffer
-        for (int k = k0; k < k1; k++) {
-            void *dstate = w + L.seg + (size_t)(k - k0) * L.state;
-            if (k == k0) {
-                TSF_TRY_CUDA(cudaMemcpyAsync(dstate, w + L.ck + (size_t)seg * L.state, state_bytes,
-                                             cudaMemcpyDeviceToDevice, s));
-            } else {
-                r = gvf_step(st, d_f0, w + L.seg + (size_t)(k - k0 - 1) * L.state, dstate, X, Y, Z, mu, s);
+        // states k0+1 .. k1-1 into the segment buffer (the last segment's are
+        // there from the forward pass)
+        if (seg != L.nck - 1) {
+            const void *src = ck_state(L, d_f0, w, seg);
+            for (int k = k0 + 1; k < k1; k++) {
+                void *dst = seg_state(L, w, k - k0);
+                r = gvf_step(st, d_f0, src, dst, X, Y, Z, mu, s);
                 if (r) return r;
+                src = dst;
             }
         }
-        // the stencil kernel moves cotangents in 16-byte vectors
-        const bool vec = adj_vec(X) && ((uintptr_t)d_gf0 & 15) == 0 && ((uintptr_t)w & 15) == 0;
         for (int k = k1 - 1; k >= k0; k--) {
-            const void *vk = w + L.seg + (size_t)(k - k0) * L.state;
-            const dim3 g = adj_grid(X, Y, Z);
-            double *dmu_v = dmu_b + (int64_t)g.x * g.y * g.z;
+            const void *vk = k == k0 ? ck_state(L, d_f0, w, seg) : (const void *)seg_state(L, w, k - k0);
             if (vec) {
                 // fold lambda' in place (boundary planes only), then the stencil
                 for (int axis = 0; axis < 3; axis++) {
@@ -455,6 +469,12 @@ extern "C" size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storag
                                                  int checkpoint_every) {
     if (!tsf::valid_storage(storage) || X <= 0 || Y <= 0 || Z <= 0 || iterations < 0) return 0;
     return tsf::gvf_adjoint_workspace_size(X, Y, Z, storage, iterations, checkpoint_every);
+}
+
+extern "C" int tsf_gvf_adjoint_checkpoint_interval(int X, int Y, int Z, int storage, int iterations,
+                                                   size_t budget_bytes) {
+    if (!tsf::valid_storage(storage) || X <= 0 || Y <= 0 || Z <= 0 || iterations < 0) return 0;
+    return tsf::gvf_adjoint_interval(X, Y, Z, storage, iterations, budget_bytes);
 }
 
 extern "C" int tsf_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int iterations, int storage,

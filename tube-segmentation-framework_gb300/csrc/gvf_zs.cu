@@ -132,7 +132,6 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
         P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), cc[c]);
     }
 
-#pragma unroll 3
     for (int k = 0; k < nf; k++) {
         const int q = qa + k;
         ok &= mbar_wait(vbar + sp, pp);

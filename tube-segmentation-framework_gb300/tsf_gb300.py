@@ -70,6 +70,7 @@ def _declare(L):
         "tsf_gvf": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
         "tsf_gvf_mode": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _i, _p]),
         "tsf_gvf_device_error": (_i, [_i]),
+        "tsf_gvf_adjoint_checkpoint_interval": (_i, [_i, _i, _i, _i, _i, _sz]),
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
         "tsf_gvf_adjoint_workspace_size": (_sz, [_i, _i, _i, _i, _i, _i]),
@@ -200,6 +201,18 @@ def gvf(f0, mu: float, iterations: int, storage: str = "f32", v=None, ws=None, m
     _check(L.tsf_gvf_mode(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
                           _ptr(ws), ws.numel(), int(mode), _stream(stream)))
     return v
+
+
+def gvf_adjoint_interval(f0, iterations: int, storage: str = "f32", budget_bytes: int = None) -> int:
+    """Smallest checkpoint interval whose adjoint workspace fits budget_bytes
+    (default: 60 % of the device memory free now); 0 means the default
+    sqrt(K) interval."""
+    if budget_bytes is None:
+        free, _ = _torch().cuda.mem_get_info(f0.device)
+        budget_bytes = int(0.6 * free)
+    _, Z, Y, X = f0.shape
+    return int(load().tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, STORAGE[storage], int(iterations),
+                                                          int(budget_bytes)))
 
 
 def gvf_adjoint_workspace(f0, iterations: int, storage: str = "f32", checkpoint_every: int = 0):
