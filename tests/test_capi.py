@@ -51,7 +51,7 @@ def test_adjoint_checkpoint_interval(tsf):
     C = L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, best)
     assert C > 1 and ws(C) == best and all(ws(c) > best for c in range(1, C))
     assert L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, best - 1) == 0
-    for budget in (ws(1) // 2, ws(1) // 5, ws(1) // 9):
+    for budget in (ws(1) // 2, ws(1) // 4, (best + ws(1) // 4) // 2):
         C = L.tsf_gvf_adjoint_checkpoint_interval(X, Y, Z, 0, K, budget)
         assert C > 1 and ws(C) <= budget
         assert all(ws(c) > budget for c in range(1, C))
