@@ -316,6 +316,23 @@ def run_tsf(args, rank, world):
     gvf_ms_mu01, _ = gvf_kernel_stats(args.storage, 0.1)
     f32_ms, _ = gvf_kernel_stats("f32", args.mu)
     vec_ms, _ = gvf_kernel_stats(args.storage, args.mu, mode=1)
+
+    # ---- the whole path with FP32 storage (same volume, same steps) -------------------
+    path32_ms = None
+    if args.storage != "f32":
+        p32 = Pipeline(T, torch, shape, "f32", args.iters, args.mu)
+        p32.vol.copy_(pipe.vol)
+        p32.step()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(2):
+            p32.step()
+        b.record()
+        torch.cuda.synchronize()
+        path32_ms = a.elapsed_time(b) / 2
+        del p32
     s_bytes = 4 if args.storage == "f32" else 2
     iters_per_launch = args.iters / gvf_launches
     launch_s = gvf_ms * 1e-3 / gvf_launches
@@ -373,6 +390,9 @@ def run_tsf(args, rank, world):
                 "register_vector_kernel_gvox_iter_s": round(N * args.iters / (vec_ms * 1e-3) / 1e9, 2),
                 "device_error": T.gvf_device_error()},
         "candidates": pipe.last,
+        "f32_path": None if path32_ms is None else {
+            "ms_per_step": round(path32_ms, 3),
+            "speedup_of_%s_path" % args.storage: round(path32_ms / ms, 3)},
         "roofline": {"bound": "hbm", "kernel": "GVF iteration", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": "measured" if peaks else "fallback",
