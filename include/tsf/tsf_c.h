@@ -146,9 +146,10 @@ int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
 int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                  int storage, void *d_workspace, size_t workspace_bytes, int mode, void *stream);
 
-/* Device-side error word of the streaming GVF kernel: 0 = none, bit 0 = a
- * shared-memory copy did not complete within its wait limit (the kernel then
- * stops early and its output is invalid); -1 if the word could not be read.
+/* Device-side error word of the streaming GVF kernels: 0 = none; bit 0 (the
+ * forward kernel) or bit 1 (the adjoint kernel) = a shared-memory copy did not
+ * complete within its wait limit (the kernel then stops early and its output
+ * is invalid); -1 if the word could not be read.
  * clear != 0 resets the word.  Synchronises with the device.  No counterpart
  * in the reference (OpenCL reports no such condition). */
 int tsf_gvf_device_error(int clear);

@@ -89,6 +89,7 @@ def test_adjoint_matches_fp64_autograd(torch_dev, tsf, synth, shape, K, C):
     assert torch.equal(vK, tsf.gvf(f0, 0.05, K, "f32"))
     gf2, dmu2 = tsf.gvf_adjoint(f0, 0.05, K, gv, "f32", C, ws=ws, checkpoints_stored=True)
     assert torch.equal(gf, gf2) and dmu == dmu2
+    assert tsf.gvf_device_error() == 0
     f64 = f0.double().cpu().requires_grad_(True)
     mu64 = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
     v = torch_gvf(f64, mu64, K)
@@ -98,6 +99,33 @@ def test_adjoint_matches_fp64_autograd(torch_dev, tsf, synth, shape, K, C):
     scale = np.abs(ref).max()
     assert np.abs(got - ref).max() <= 1e-4 * scale
     assert abs(dmu - mu64.grad.item()) <= 1e-4 * max(1.0, abs(mu64.grad.item()))
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16", "snorm16"])
+@pytest.mark.parametrize("shape", [(12, 10, 16), (9, 11, 20)])
+def test_adjoint_16bit_storage(torch_dev, tsf, synth, storage, shape):
+    """16-bit forward states (X = 16: the streaming adjoint kernel; X = 20: the
+    vector kernel).  The adjoint treats the storage rounding as the identity,
+    so it is compared with FP64 autograd of the FP32 method at the rounding
+    error of the stored states."""
+    torch = torch_dev
+    vol = synth.vascular_tree(shape, seed=7)
+    b = tsf.blur(torch.from_numpy(vol).cuda(), 0.5)
+    f16, _ = tsf.vector_field(b, 0.2, 1, storage)
+    K = 9
+    gv = torch.randn((3,) + shape, generator=torch.Generator().manual_seed(2)).float().cuda()
+    gf, dmu = tsf.gvf_adjoint(f16, 0.05, K, gv, storage, checkpoint_every=3)
+    assert tsf.gvf_device_error() == 0
+    a = f16.detach().cpu()
+    if storage == "snorm16":
+        a = torch.clamp(a.float() / 32767.0, min=-1.0)
+    f64 = a.double().requires_grad_(True)
+    mu64 = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
+    (torch_gvf(f64, mu64, K) * gv.double().cpu()).sum().backward()
+    ref = f64.grad.numpy()
+    tol = {"f16": 2e-3, "snorm16": 2e-3, "bf16": 2e-2}[storage]
+    assert np.abs(gf.cpu().numpy() - ref).max() <= tol * np.abs(ref).max()
+    assert abs(dmu - mu64.grad.item()) <= tol * max(1.0, abs(mu64.grad.item()))
 
 
 def test_adjoint_matches_fp64_finite_differences(torch_dev, tsf, oracle, synth):

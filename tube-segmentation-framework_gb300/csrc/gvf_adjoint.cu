@@ -28,6 +28,11 @@
 namespace tsf {
 
 int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu, cudaStream_t s);
+bool gvf_adjoint_zs_eligible(int st, const void *g, const void *v, const void *f, const void *gf, const void *lam,
+                             int X);
+int gvf_adjoint_zs_max_grid();
+int launch_gvf_adjoint_zs(int st, const float *g, const void *v, const void *f, float *lam_out, float *gf,
+                          double *dmu_block, int X, int Y, int Z, float mu, cudaStream_t s);
 
 // folded cotangent at (x, y, z): sum of lambda' over the voxels that mirror to it
 __device__ __forceinline__ float fold_at(const float *__restrict__ lp, int x, int y, int z, int X, int Y, int Z) {
@@ -314,7 +319,9 @@ static AdjLayout adj_layout(int X, int Y, int Z, int st, int K, int C) {
     const size_t n = (size_t)X * Y * Z;
     L.state = al256(3 * n * storage_bytes(st));
     const dim3 g = adj_grid(X, Y, Z), gv = adjv_grid(X, Y, Z);
-    L.nblocks = (int64_t)g.x * g.y * g.z + (adj_vec(X) ? (int64_t)gv.x * gv.y * gv.z : 0);
+    // partials: the per-voxel kernel's blocks, then the vector or streaming kernel's
+    const int64_t nv = adj_vec(X) ? (int64_t)gv.x * gv.y * gv.z : 0, nz = gvf_adjoint_zs_max_grid();
+    L.nblocks = (int64_t)g.x * g.y * g.z + (nv > nz ? nv : nz);
     size_t off = 0;
     L.ck = off; off += L.state * (size_t)(L.nck > 1 ? L.nck - 1 : 0);
     L.seg = off; off += L.state * (size_t)(C - 1);
@@ -407,6 +414,8 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
     }
     // the cotangent kernels move 16-byte vectors
     const bool vec = adj_vec(X) && ((uintptr_t)d_gf0 & 15) == 0 && ((uintptr_t)w & 15) == 0;
+    const bool zs = vec && gvf_adjoint_zs_eligible(st, lam, d_f0, d_f0, d_gf0, lam2, X) &&
+                    ((uintptr_t)(w + L.ck) & 15) == 0 && ((uintptr_t)(w + L.seg) & 15) == 0;
     const dim3 g = adj_grid(X, Y, Z);
     double *dmu_v = dmu_b + (int64_t)g.x * g.y * g.z;
     // reverse, one segment at a time
@@ -432,12 +441,17 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
                     fold_axis_kernel<<<(unsigned)((faces + 255) / 256), 256, 0, s>>>(lam, X, Y, Z, axis);
                 }
                 TSF_CHECK_LAUNCHES("fold_axis_kernel", 3);
-                TSF_DISPATCH_STORAGE(st, ST, {
-                    using T = typename Store<ST>::T;
-                    gvf_adjoint_stencil_kernel<ST><<<adjv_grid(X, Y, Z), adjv_block(), 0, s>>>(
-                        lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu);
-                });
-                TSF_CHECK_LAUNCH("gvf_adjoint_stencil_kernel");
+                if (zs) {
+                    r = launch_gvf_adjoint_zs(st, lam, vk, d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu, s);
+                    if (r) return r;
+                } else {
+                    TSF_DISPATCH_STORAGE(st, ST, {
+                        using T = typename Store<ST>::T;
+                        gvf_adjoint_stencil_kernel<ST><<<adjv_grid(X, Y, Z), adjv_block(), 0, s>>>(
+                            lam, (const T *)vk, (const T *)d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu);
+                    });
+                    TSF_CHECK_LAUNCH("gvf_adjoint_stencil_kernel");
+                }
             } else {
                 TSF_DISPATCH_STORAGE(st, ST, {
                     using T = typename Store<ST>::T;

@@ -239,7 +239,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // 4-D map (x, y, z, component) over a planar field, box (bx, by, 1, 3).
-static bool encode_planar(CUtensorMap *m, const void *base, int X, int Y, int Z, int es, int bx, int by) {
+bool encode_planar(CUtensorMap *m, const void *base, int X, int Y, int Z, int es, int bx, int by) {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint64_t dims[4] = {(cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, 3};
@@ -344,4 +344,12 @@ int gvf_zs_error(int clear) {
 
 }  // namespace tsf
 
-extern "C" int tsf_gvf_device_error(int clear) { return tsf::gvf_zs_error(clear); }
+namespace tsf {
+int gvf_adjoint_zs_error(int clear);
+}
+
+extern "C" int tsf_gvf_device_error(int clear) {
+    const int a = tsf::gvf_zs_error(clear), b = tsf::gvf_adjoint_zs_error(clear);
+    if (a < 0 || b < 0) return -1;
+    return (a ? 1 : 0) | (b ? 2 : 0);
+}

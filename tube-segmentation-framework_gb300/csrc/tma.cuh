@@ -83,4 +83,9 @@ __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *map) {
 // Host: cuTensorMapEncodeTiled from the driver (NULL if unavailable).
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 
+// Host: 4-D map (x, y, z, component) over a planar field of three X*Y*Z
+// planes with es-byte elements, box (bx, by, 1, 3).  False if the driver
+// rejects it (strides must be multiples of 16 bytes).
+bool encode_planar(CUtensorMap *m, const void *base, int X, int Y, int Z, int es, int bx, int by);
+
 }  // namespace tsf
