@@ -427,6 +427,7 @@ def fwd_adjoint_timing(torch, pipe, args):
     Tc, state = CAL.forward(vol, p)
     ev[1].record()
     torch.cuda.synchronize()
+    del Tc, state
     ev[2].record()
     Tc, state = CAL.forward(vol, p)
     gT = ((2.0 / Tc.numel()) * (Tc - G)).contiguous()
@@ -435,6 +436,8 @@ def fwd_adjoint_timing(torch, pipe, args):
     torch.cuda.synchronize()
     fwd = ev[0].elapsed_time(ev[1])
     both = ev[2].elapsed_time(ev[3])
+    # (the timed forward + adjoint reuses the cached workspace of the forward
+    # before it: that state is released first)
     # breakdown of the backward stages
     import tsf_gb300 as T
     small = state["small"]
@@ -448,9 +451,9 @@ def fwd_adjoint_timing(torch, pipe, args):
         marks.append(e)
 
     mark()
-    g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, "f32")
+    g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, "f32", T=state["Ts"], R=state["Rs"])
     mark()
-    g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, "f32")
+    g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, "f32", T=state["Tl"], R=state["Rl"])
     mark()
     g_f0, _ = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, "f32", state["checkpoint_every"],
                             ws=state["gvf_ws"], checkpoints_stored=True)

@@ -238,11 +238,15 @@ int tsf_tdf_combine(const void *d_T_small, const float *d_R_small, void *d_T_lar
  * radius, through the sample directions (eigenvectors of the Hessian, by
  * first-order eigenvector perturbation) and through the Hessian's central
  * differences (of v/|v| when rmax >= 4, w taken as |v|).  The arg-max radius
- * is held fixed (sub-gradient of the max over radii). */
+ * is held fixed (sub-gradient of the max over radii).  d_T, d_R: the float
+ * response and radius tsf_tdf_circle wrote for this field and radius range
+ * (then the sweep is not repeated), or both NULL (the sweep is recomputed).
+ * Scatters use atomics, so the last bits vary between runs. */
 size_t tsf_tdf_backward_workspace_size(int X, int Y, int Z);
 int tsf_tdf_circle_backward(const void *d_field4, int X, int Y, int Z, int storage, float rmin,
-                            float rmax, float rstep, const float *d_gT, float *d_gfield,
-                            void *d_workspace, size_t workspace_bytes, void *stream);
+                            float rmax, float rstep, const float *d_gT, const float *d_T,
+                            const float *d_R, float *d_gfield, void *d_workspace,
+                            size_t workspace_bytes, void *stream);
 
 /* Reverse-mode derivative of tsf_vector_field with respect to its input
  * volume: ADDS to d_gin the gradient from d_gf (planar FP32 dL/df). */

@@ -76,7 +76,12 @@ def test_tdf_backward_directional(torch_dev, tsf, oracle, synth, rng_):
         z, y, x = cand[rng.integers(len(cand))]
         gT = np.zeros(T0.shape, np.float32)
         gT[z, y, x] = 1.0
-        g = tsf.tdf_backward(d4, *rng_, torch.from_numpy(gT).cuda()).cpu().numpy()
+        gT_d = torch.from_numpy(gT).cuda()
+        g = tsf.tdf_backward(d4, *rng_, gT_d).cpu().numpy()
+        # the same at the forward's arg-max radius, without repeating the sweep
+        Tf, Rf = tsf.tdf_circle(d4, *rng_, storage="f32")
+        g2 = tsf.tdf_backward(d4, *rng_, gT_d, T=Tf, R=Rf).cpu().numpy()
+        assert np.allclose(g, g2, rtol=1e-5, atol=1e-7 * np.abs(g).max())
         g = np.moveaxis(g, 0, -1).astype(np.float64)
         D = rng.normal(size=f64.shape[:3] + (3,))
 

@@ -8,8 +8,9 @@ tube-segmentation.cpp:212-939):
                 T_l = TDF(F; max(2.5, rmin)..rmax, rstep)
     T = combine(T_s, T_l)                (the larger response per voxel)
 Loss: L = mean((T - G)^2) for a target map G (e.g. a Gaussian centerline map).
-Backward: the library's adjoints (tsf_tdf_circle_backward, tsf_gvf_adjoint with
-sqrt(K) checkpointing, tsf_vector_field_backward, tsf_blur_backward) give
+Backward: the library's adjoints (tsf_tdf_circle_backward at the forward's
+arg-max radii, tsf_gvf_adjoint with memory-budgeted checkpointing,
+tsf_vector_field_backward, tsf_blur_backward) give
 dL/dI, dL/dmu and dL/dsigma; torch is only the glue (elementwise products and
 the combine mask).  FP32 storage and arithmetic.
 """
@@ -49,7 +50,8 @@ def forward(vol, p: Params):
     Tl, Rl = T.tdf_circle(F, max(2.5, p.rmin), p.rmax, p.rstep, st)
     small = Ts > Tl                       # combine (kernels.cl:561-572): T_l < T_s -> take T_s
     Tc = torch.where(small, Ts, Tl)
-    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small, gvf_ws=ws, checkpoint_every=C)
+    s.update(vol=vol, f_s=f_s, b=b, f0=f0, F=F, small=small, gvf_ws=ws, checkpoint_every=C, Ts=Ts, Rs=Rs, Tl=Tl,
+             Rl=Rl)
     return Tc, s
 
 
@@ -62,10 +64,10 @@ def backward(state, gT, p: Params):
     gTs = torch.where(small, gT, torch.zeros_like(gT)).contiguous()
     gTl = torch.where(small, torch.zeros_like(gT), gT).contiguous()
     # small pass -> the un-diffused field of I
-    g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, st)
+    g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, st, T=state["Ts"], R=state["Rs"])
     gI = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
     # large pass -> GVF -> vector field -> blur
-    g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, st)
+    g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, st, T=state["Tl"], R=state["Rl"])
     g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, state["checkpoint_every"],
                               ws=state["gvf_ws"], checkpoints_stored=True)
     g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)

@@ -435,12 +435,13 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
         for (int k = k1 - 1; k >= k0; k--) {
             const void *vk = k == k0 ? ck_state(L, d_f0, w, seg) : (const void *)seg_state(L, w, k - k0);
             if (vec) {
-                // fold lambda' in place (boundary planes only), then the stencil
-                for (int axis = 0; axis < 3; axis++) {
+                // fold lambda' in place (boundary planes only; the streaming
+                // kernel does the x part itself), then the stencil
+                for (int axis = zs ? 1 : 0; axis < 3; axis++) {
                     const int64_t faces = 3 * (axis == 0 ? (int64_t)Y * Z : axis == 1 ? (int64_t)X * Z : (int64_t)X * Y);
                     fold_axis_kernel<<<(unsigned)((faces + 255) / 256), 256, 0, s>>>(lam, X, Y, Z, axis);
                 }
-                TSF_CHECK_LAUNCHES("fold_axis_kernel", 3);
+                TSF_CHECK_LAUNCHES("fold_axis_kernel", zs ? 2 : 3);
                 if (zs) {
                     r = launch_gvf_adjoint_zs(st, lam, vk, d_f0, lam2, d_gf0, dmu_v, X, Y, Z, mu, s);
                     if (r) return r;

@@ -2,7 +2,9 @@
 // TMA copies (the transpose of GVF3DIteration, kernels.cl:1464-1493; no
 // counterpart in the reference, which has no derivatives).
 //
-// Given the folded cotangent g = fold(lambda') (zero outside the volume), the
+// Given the folded cotangent g = fold(lambda') (zero outside the volume; the
+// y and z parts of the fold are applied to lambda' beforehand, the x part by
+// this kernel as it loads), the
 // state v_k and the data term f0, per component c and voxel r:
 //     lambda_c = g_c (1 - 6 mu - s) + mu nb_c,   nb_c = sum of g_c over the 6 neighbours
 //     dL/df0_c += g_c s - 2 f_c sum_d g_d (v_d - f_d),   s = |f0|^2
@@ -140,6 +142,13 @@ __global__ void __launch_bounds__(AdjZsCfg<ST>::THREADS, 1)
         const int xc = x0 + 4 * lane, y = y0 + r;
         const bool act = xc < X && y < Y;
         const int goff = (r + 1) * BW + H + 4 * lane;      // component c at goff + c * (TY + 2) * BW
+        // the x part of the fold happens here, on every g vector a lane loads:
+        // its vector holds x = 0 and 2 (or X-3 and X-1) together
+        const bool fx_lo = xc == 0, fx_hi = xc + 4 == X;
+        auto xfold = [&](float a[4]) {
+            if (fx_lo) { a[2] = a[2] + a[0]; a[0] = 0.0f; }
+            if (fx_hi) { a[1] = a[1] + a[3]; a[3] = 0.0f; }
+        };
         const int toff = r * TX + 4 * lane;                // component c at toff + c * TY * TX
         float gm[3][4], gc[3][4];                          // g at planes q-1 and q (lane's column)
         ok &= mbar_wait(gbar + gbase % RG, (gbase / RG) & 1);
@@ -151,6 +160,8 @@ __global__ void __launch_bounds__(AdjZsCfg<ST>::THREADS, 1)
             for (int c = 0; c < 3; c++) {
                 PF::unpack(PF::load_plain(a + goff + c * (TY + 2) * BW), gm[c]);
                 PF::unpack(PF::load_plain(b + goff + c * (TY + 2) * BW), gc[c]);
+                xfold(gm[c]);
+                xfold(gc[c]);
             }
         }
         float *lo = lam_out + (int64_t)y * X + xc + (int64_t)s.qa * plane;
@@ -184,6 +195,11 @@ __global__ void __launch_bounds__(AdjZsCfg<ST>::THREADS, 1)
                 PF::unpack(PF::load_plain(gp + c * (TY + 2) * BW), zp);
                 PF::unpack(PF::load_plain(pc + BW), yp);
                 PF::unpack(PF::load_plain(pc - BW), ym);
+                xfold(zp);
+                xfold(yp);
+                xfold(ym);
+                // x-neighbours outside the lane's vector are never fold targets
+                // (x = -1 / X read as 0; x = 3 / X-4 are unchanged by the fold)
                 const float xr = pc[4], xl = pc[-1];
                 const float *g = gc[c];
                 float out[4];

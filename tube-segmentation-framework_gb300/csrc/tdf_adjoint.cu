@@ -30,16 +30,24 @@ namespace tsf {
 
 constexpr int kMaxRadiiBwd = 4096;
 
-template <int ST, bool NORM>
+// One thread per voxel; a CTA of 128 threads is an 8 x 4 x 4 block, so the
+// gathers and scatters of neighbouring threads stay close.  GIVEN: the
+// forward's response T and arg-max radius R are read instead of re-running the
+// sweep (the forward computed them with the same arithmetic).
+template <int ST, bool NORM, bool GIVEN>
 __global__ void __launch_bounds__(128) tdf_backward_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                            float rmin, float rmax, float rstep, const CircleTable tab,
-                                                           const float *__restrict__ gT, float4 *__restrict__ gV) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+                                                           const float *__restrict__ gT, const float *__restrict__ Tin,
+                                                           const float *__restrict__ Rin, float4 *__restrict__ gV) {
+    const int t = threadIdx.x;
+    const int x = blockIdx.x * 8 + (t & 7);
+    const int y = blockIdx.y * 4 + ((t >> 3) & 3);
+    const int z = blockIdx.z * 4 + (t >> 5);
     if (x >= X || y >= Y || z >= Z) return;
-    const float g = gT[lin(x, y, z, X, Y)];
+    const int64_t vi = lin(x, y, z, X, Y);
+    const float g = gT[vi];
     if (g == 0.0f) return;
+    if (GIVEN && !(Tin[vi] > 0.0f)) return;
     float H[3][3], V[3][3], d[3];
     hessian<ST, NORM>(F, X, Y, Z, x, y, z, H);
     eig3<float>(H, V, d);
@@ -47,9 +55,9 @@ __global__ void __launch_bounds__(128) tdf_backward_kernel(const void *__restric
     const float e3[3] = {V[0][2], V[1][2], V[2][2]};
     const float fx = (float)x, fy = (float)y, fz = (float)z;
     // forward sweep: the arg-max radius
-    float maxSum = 0.0f, rstar = 0.0f;
+    float maxSum = GIVEN ? Tin[vi] : 0.0f, rstar = GIVEN ? Rin[vi] : 0.0f;
     int nr = 0;
-    for (float radius = rmin; radius <= rmax && nr < kMaxRadiiBwd; radius = radius + rstep, nr++) {
+    for (float radius = rmin; !GIVEN && radius <= rmax && nr < kMaxRadiiBwd; radius = radius + rstep, nr++) {
         float rs = 0.0f;
         for (int j = 0; j < 32; j++) {
             const float c = tab.c[j], s = tab.s[j];
@@ -270,7 +278,8 @@ static size_t a256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t tdf_backward_workspace_size(int X, int Y, int Z) { return a256(sizeof(float4) * (size_t)X * Y * Z); }
 
 int run_tdf_backward(const void *F, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                     const float *gT, float *gfield, void *ws, size_t ws_bytes, cudaStream_t s) {
+                     const float *gT, const float *Tin, const float *Rin, float *gfield, void *ws, size_t ws_bytes,
+                     cudaStream_t s) {
     int r = check_dims(X, Y, Z);
     if (r) return r;
     if (!F || !gT || !gfield) return fail(TSF_ERR_INVALID_ARG, "null buffer");
@@ -279,12 +288,20 @@ int run_tdf_backward(const void *F, int X, int Y, int Z, int st, float rmin, flo
     float4 *acc = (float4 *)ws;
     TSF_TRY_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * (size_t)n, s));
     const CircleTable tab = host_circle_table();
-    const dim3 b(32, 2, 2), g((X + 31) / 32, (Y + 1) / 2, (Z + 1) / 2);
+    const dim3 b(128), g((X + 7) / 8, (Y + 3) / 4, (Z + 3) / 4);
     const bool norm = !(rmax < 4.0f);
+    if ((Tin == nullptr) != (Rin == nullptr)) return fail(TSF_ERR_INVALID_ARG, "give both T and R, or neither");
+    const bool given = Tin != nullptr;
+#define TSF_TDFB(NORM_, GIVEN_) \
+    tdf_backward_kernel<ST, NORM_, GIVEN_><<<g, b, 0, s>>>(F, X, Y, Z, rmin, rmax, rstep, tab, gT, Tin, Rin, acc)
     TSF_DISPATCH_STORAGE(st, ST, {
-        if (norm) tdf_backward_kernel<ST, true><<<g, b, 0, s>>>(F, X, Y, Z, rmin, rmax, rstep, tab, gT, acc);
-        else tdf_backward_kernel<ST, false><<<g, b, 0, s>>>(F, X, Y, Z, rmin, rmax, rstep, tab, gT, acc);
+        if (norm) {
+            if (given) TSF_TDFB(true, true); else TSF_TDFB(true, false);
+        } else {
+            if (given) TSF_TDFB(false, true); else TSF_TDFB(false, false);
+        }
     });
+#undef TSF_TDFB
     TSF_CHECK_LAUNCH("tdf_backward_kernel");
     aos4_to_planar_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(acc, gfield, n);
     TSF_CHECK_LAUNCH("aos4_to_planar_add_kernel");
@@ -356,10 +373,10 @@ extern "C" size_t tsf_tdf_backward_workspace_size(int X, int Y, int Z) {
 }
 
 extern "C" int tsf_tdf_circle_backward(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
-                                       float rstep, const float *d_gT, float *d_gfield, void *d_workspace,
-                                       size_t workspace_bytes, void *stream) {
-    return tsf::run_tdf_backward(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_gT, d_gfield, d_workspace,
-                                 workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
+                                       float rstep, const float *d_gT, const float *d_T, const float *d_R,
+                                       float *d_gfield, void *d_workspace, size_t workspace_bytes, void *stream) {
+    return tsf::run_tdf_backward(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_gT, d_T, d_R, d_gfield,
+                                 d_workspace, workspace_bytes, reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tsf_vector_field_backward(const float *d_in, const float *d_gf, int X, int Y, int Z, float fmax,

@@ -77,7 +77,7 @@ def _declare(L):
         "tsf_gvf_adjoint": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _p, _i, _i, _p, _sz, _p]),
         "tsf_gvf_checkpointed": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _sz, _p]),
         "tsf_tdf_backward_workspace_size": (_sz, [_i, _i, _i]),
-        "tsf_tdf_circle_backward": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _p, _sz, _p]),
+        "tsf_tdf_circle_backward": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _p, _p, _p, _sz, _p]),
         "tsf_vector_field_backward": (_i, [_p, _p, _i, _i, _i, _f, _i, _p, _p]),
         "tsf_blur_backward_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_blur_backward": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, _p, _sz, _p]),
@@ -246,15 +246,18 @@ def gvf_adjoint(f0, mu: float, iterations: int, gv, storage: str = "f32", checkp
     return gf, dmu.value
 
 
-def tdf_backward(field4, rmin, rmax, rstep, gT, storage: str = "f32", gfield=None, stream=None):
-    """Adds dL/d(field xyz) (planar float32) for dL/dT = gT; returns gfield."""
+def tdf_backward(field4, rmin, rmax, rstep, gT, storage: str = "f32", gfield=None, T=None, R=None, stream=None):
+    """Adds dL/d(field xyz) (planar float32) for dL/dT = gT; returns gfield.
+    T, R: the forward's float response and radius (the sweep is then not
+    repeated)."""
     torch = _torch()
     Z, Y, X = field4.shape[:3]
     L = load()
     gfield = torch.zeros((3, Z, Y, X), dtype=torch.float32, device=field4.device) if gfield is None else gfield
     ws = workspace(L.tsf_tdf_backward_workspace_size(X, Y, Z))
     _check(L.tsf_tdf_circle_backward(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax), float(rstep),
-                                     _ptr(gT), _ptr(gfield), _ptr(ws), ws.numel(), _stream(stream)))
+                                     _ptr(gT), _ptr(T), _ptr(R), _ptr(gfield), _ptr(ws), ws.numel(),
+                                     _stream(stream)))
     return gfield
 
 
