@@ -89,9 +89,11 @@ template <int ST, bool NORM, bool UNORM>
 __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                                     float rmin, float rmax, float rstep,
                                                                     const CircleTable tab, void *T,
-                                                                    float *__restrict__ Rout) {
+                                                                    float *__restrict__ Rout, int fast_ok) {
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
+    __shared__ unsigned char sin_[kTdfWarps][kSeg];      // samples stay inside: unclamped sampler
+    const int XY = X * Y, margin = sample_margin(rmax);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     // brick of this CTA, block of this warp: task t -> (t & 7, (t >> 3) & 3, t >> 5)
     const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
@@ -111,6 +113,8 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
         eig3<float>(H, V, d);
         se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
         se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
+        const float e2[3] = {V[0][1], V[1][1], V[2][1]}, e3[3] = {V[0][2], V[1][2], V[2][2]};
+        sin_[w][t] = fast_ok && samples_inside(tx(t), ty(t), tz(t), X, Y, Z, margin, e2, e3);
     }
     __syncwarp();
     // phase 2: radius sweeps as tasks
@@ -127,16 +131,30 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
             const float fx = (float)tx(task), fy = (float)ty(task), fz = (float)tz(task);
             if (radius <= rmax && nr < kMaxRadii) {
                 float rs = 0.0f;
+                if (sin_[w][task]) {
 #pragma unroll 4
-                for (int j = 0; j < 32; j++) {
-                    const float c = tab.c[j], s = tab.s[j];
-                    const float va0 = c * e3x + s * e2x;
-                    const float va1 = c * e3y + s * e2y;
-                    const float va2 = c * e3z + s * e2z;
-                    const float3 smp =
-                        sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
-                    const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
-                    rs = rs + dt;
+                    for (int j = 0; j < 32; j++) {
+                        const float c = tab.c[j], s = tab.s[j];
+                        const float va0 = c * e3x + s * e2x;
+                        const float va1 = c * e3y + s * e2y;
+                        const float va2 = c * e3z + s * e2z;
+                        const float3 smp =
+                            sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1, fz + radius * va2);
+                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                        rs = rs + dt;
+                    }
+                } else {
+#pragma unroll 4
+                    for (int j = 0; j < 32; j++) {
+                        const float c = tab.c[j], s = tab.s[j];
+                        const float va0 = c * e3x + s * e2x;
+                        const float va1 = c * e3y + s * e2y;
+                        const float va2 = c * e3z + s * e2z;
+                        const float3 smp =
+                            sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
+                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                        rs = rs + dt;
+                    }
                 }
                 rs = rs / 32.0f;
                 if (rs > maxSum) {
@@ -195,11 +213,12 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
     const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
     const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
     const bool queue = tdf_mode != 1;
+    const int fast_ok = (int64_t)X * Y * Z < ((int64_t)1 << 31) - 1;   // 32-bit texel offsets
 #define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
     do {                                                                                                             \
         if (queue)                                                                                                   \
             tdf_queue_kernel<ST, NORM, UN><<<qblocks, 32 * kTdfWarps, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, \
-                                                                              tab, d_T, d_R);                        \
+                                                                              tab, d_T, d_R, fast_ok);               \
         else                                                                                                         \
             tdf_circle_kernel<ST, NORM, UN><<<g, b, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R);    \
     } while (0)

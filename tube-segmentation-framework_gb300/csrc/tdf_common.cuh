@@ -94,4 +94,49 @@ __device__ __forceinline__ float3 sample_linear(const void *F, int X, int Y, int
     return o;
 }
 
+// sample_linear for a point whose 8 corners are all inside the volume (the
+// caller guarantees it): the clamps are no-ops there and are skipped, and the
+// corners are addressed from one 32-bit base (X*Y*Z < 2^31).  Same weights
+// and the same sums in the same order, so the same bits as sample_linear.
+template <int ST>
+__device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY, float u, float v, float w) {
+    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
+    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
+    const float a = uu - fu, b = vv - fv, c = ww - fw;
+    const int base = (int)fu + X * (int)fv + XY * (int)fw;
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
+    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    const float4 t000 = Vec4Load<ST>::load(F, base), t100 = Vec4Load<ST>::load(F, base + 1);
+    const float4 t010 = Vec4Load<ST>::load(F, base + X), t110 = Vec4Load<ST>::load(F, base + X + 1);
+    const float4 t001 = Vec4Load<ST>::load(F, base + XY), t101 = Vec4Load<ST>::load(F, base + XY + 1);
+    const float4 t011 = Vec4Load<ST>::load(F, base + XY + X), t111 = Vec4Load<ST>::load(F, base + XY + X + 1);
+    float3 o;
+    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
+    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
+    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
+    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
+    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
+    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
+    return o;
+}
+
+// Margin m such that every trilinear corner of a sample at distance <= r
+// from a voxel lies within m - 1 voxels of it, for sample directions
+// a = cos e3 + sin e2 with |e2|, |e3| <= 1.00005 and |e2 . e3| <= 1e-3
+// (then |a| <= 1.0012; corners lie within ceil(|a| r + 0.5) of the voxel).
+__host__ __device__ __forceinline__ int sample_margin(float rmax) { return (int)ceilf(rmax * 1.002f + 0.5f) + 2; }
+
+// Whether a voxel's samples can take sample_linear_in: the margin box lies in
+// the volume and the eigenvectors are finite, unit and orthogonal up to
+// rounding (false for NaN / inf, which then take the clamped sampler).
+__device__ __forceinline__ bool samples_inside(int x, int y, int z, int X, int Y, int Z, int m, const float e2[3],
+                                               const float e3[3]) {
+    if (x < m || y < m || z < m || x + m >= X || y + m >= Y || z + m >= Z) return false;
+    const float n2 = (e2[0] * e2[0] + e2[1] * e2[1]) + e2[2] * e2[2];
+    const float n3 = (e3[0] * e3[0] + e3[1] * e3[1]) + e3[2] * e3[2];
+    const float d = (e2[0] * e3[0] + e2[1] * e3[1]) + e2[2] * e3[2];
+    return n2 <= 1.0001f && n3 <= 1.0001f && d >= -1e-3f && d <= 1e-3f;
+}
+
 }  // namespace tsf
