@@ -173,7 +173,6 @@ class Pipeline:
         self.Rl = torch.empty_like(self.Ts)
         self.gvf_ws = T.workspace(L.tsf_gvf_workspace_size(X, Y, Z, st))
         self.cand_ws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
-        self.tdf_ws = T.workspace(L.tsf_tdf_circle_workspace_size(X, Y, Z, st))
         self.max_vertices = 1 << 16
         self.verts = torch.zeros((self.max_vertices, 3), dtype=torch.int32, device=dev)
         self.last = None
@@ -191,18 +190,16 @@ class Pipeline:
         T.blur(self.vol, P["large_blur"], out=self.blurred)
         # small-radius pass on the un-diffused field of the unblurred volume (small-blur 0)
         self._vf(self.vol, None, self.f4_small)
-        T._check(T.load().tsf_tdf_circle_ws(T._ptr(self.f4_small), *self._xyz(), T.STORAGE[s], P["rmin"], 3.0, 0.5,
-                                            T._ptr(self.Ts), 0, T._ptr(self.Rs), T._ptr(self.tdf_ws),
-                                            self.tdf_ws.numel(), T._stream()))
+        T._check(T.load().tsf_tdf_circle(T._ptr(self.f4_small), *self._xyz(), T.STORAGE[s], P["rmin"], 3.0, 0.5,
+                                         T._ptr(self.Ts), 0, T._ptr(self.Rs), T._stream()))
         rec("tdf_small")
         self._vf(self.blurred, self.f0, None)
         rec("vector_field")
         self.gvf_only()
         rec("gvf")
         T.gvf_finish(self.v, s, out=self.field)
-        T._check(T.load().tsf_tdf_circle_ws(T._ptr(self.field), *self._xyz(), T.STORAGE[s], max(2.5, P["rmin"]),
-                                            P["rmax"], P["rstep"], T._ptr(self.Tl), 0, T._ptr(self.Rl),
-                                            T._ptr(self.tdf_ws), self.tdf_ws.numel(), T._stream()))
+        T._check(T.load().tsf_tdf_circle(T._ptr(self.field), *self._xyz(), T.STORAGE[s], max(2.5, P["rmin"]),
+                                         P["rmax"], P["rstep"], T._ptr(self.Tl), 0, T._ptr(self.Rl), T._stream()))
         T.tdf_combine(self.Ts, self.Rs, self.Tl, self.Rl)
         rec("tdf_large")
         self.last = self._candidates()
@@ -661,7 +658,6 @@ def run_fmg_workload(args):
     ws = T.workspace(L.tsf_gvf_fmg_workspace_size(X, Y, Z, T.STORAGE[st]))
     Ts = torch.empty_like(vol); Rs = torch.empty_like(vol); Tl = torch.empty_like(vol); Rl = torch.empty_like(vol)
     cws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
-    tws = T.workspace(L.tsf_tdf_circle_workspace_size(X, Y, Z, T.STORAGE[st]))
     verts = torch.zeros((1 << 16, 3), dtype=torch.int32, device="cuda")
     import ctypes as C
 
@@ -670,15 +666,13 @@ def run_fmg_workload(args):
             else (lambda: None)
         rec()
         T._check(L.tsf_vector_field(T._ptr(vol), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4s), T._stream()))
-        T._check(L.tsf_tdf_circle_ws(T._ptr(f4s), X, Y, Z, T.STORAGE[st], P["rmin"], 3.0, 0.5, T._ptr(Ts), 0,
-                                     T._ptr(Rs), T._ptr(tws), tws.numel(), T._stream()))
+        T._check(L.tsf_tdf_circle(T._ptr(f4s), X, Y, Z, T.STORAGE[st], P["rmin"], 3.0, 0.5, T._ptr(Ts), 0, T._ptr(Rs), T._stream()))
         T.blur(vol, P["blur"], out=b)
         T._check(L.tsf_vector_field(T._ptr(b), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4), T._stream()))
         rec()
         T._check(L.tsf_gvf_fmg(T._ptr(f4), T._ptr(out), X, Y, Z, 0.2, args.fmg_cycles, T.STORAGE[st], T._ptr(ws), ws.numel(), T._stream()))
         rec()
-        T._check(L.tsf_tdf_circle_ws(T._ptr(out), X, Y, Z, T.STORAGE[st], 2.5, P["rmax"], P["rstep"], T._ptr(Tl), 0,
-                                     T._ptr(Rl), T._ptr(tws), tws.numel(), T._stream()))
+        T._check(L.tsf_tdf_circle(T._ptr(out), X, Y, Z, T.STORAGE[st], 2.5, P["rmax"], P["rstep"], T._ptr(Tl), 0, T._ptr(Rl), T._stream()))
         T.tdf_combine(Ts, Rs, Tl, Rl)
         rec()
         nc, nv = C.c_int64(0), C.c_int64(0)

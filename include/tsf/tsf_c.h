@@ -220,16 +220,6 @@ int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int sto
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
                    float rstep, void *d_T, int tdf_unorm16, float *d_R, void *stream);
 
-/* tsf_tdf_circle with a workspace (size from tsf_tdf_circle_workspace_size;
- * 0 bytes for FP32 fields): for the 16-bit formats it holds a copy of the
- * field shifted by one texel, so the two x-corners of every trilinear sample
- * away from the faces come in one 16-byte load (halving the gathers).
- * Identical results to tsf_tdf_circle. */
-size_t tsf_tdf_circle_workspace_size(int X, int Y, int Z, int storage);
-int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, float rmin,
-                      float rmax, float rstep, void *d_T, int tdf_unorm16, float *d_R,
-                      void *d_workspace, size_t workspace_bytes, void *stream);
-
 /* tsf_tdf_circle with the kernel forced: mode 1 = one voxel per lane, 0 = the
  * default (radius sweeps load-balanced within each warp).  Identical results. */
 int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, float rmin,

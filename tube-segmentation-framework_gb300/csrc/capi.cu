@@ -35,10 +35,7 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
             size_t ws_bytes, int mode, cudaStream_t s);
 int launch_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int st, cudaStream_t s);
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, const void *d_shift);
-size_t tdf_circle_workspace_size(int X, int Y, int Z, int st);
-int launch_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                         void *d_T, int unorm, float *d_R, void *ws, size_t ws_bytes, cudaStream_t s);
+                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode);
 int launch_tdf_combine(const void *Ts, const float *Rs, void *Tl, float *Rl, int64_t n, int unorm, cudaStream_t s);
 size_t candidates_workspace_size(int X, int Y, int Z);
 size_t compact_workspace_size(int X, int Y, int Z);
@@ -105,27 +102,13 @@ int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int sto
 
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
                    void *d_T, int tdf_unorm16, float *d_R, void *stream) {
-    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), 0,
-                             nullptr);
+    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), 0);
 }
 
 // tsf_tdf_circle with the kernel forced (0 = default, 1 = one voxel per lane).
-size_t tsf_tdf_circle_workspace_size(int X, int Y, int Z, int storage) {
-    if (X <= 0 || Y <= 0 || Z <= 0) return 0;
-    return tdf_circle_workspace_size(X, Y, Z, storage);
-}
-
-int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
-                      void *d_T, int tdf_unorm16, float *d_R, void *d_workspace, size_t workspace_bytes,
-                      void *stream) {
-    return launch_tdf_circle_ws(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, d_workspace,
-                                workspace_bytes, S(stream));
-}
-
 int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
                         void *d_T, int tdf_unorm16, float *d_R, int mode, void *stream) {
-    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), mode,
-                             nullptr);
+    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), mode);
 }
 
 int tsf_tdf_combine(const void *d_T_small, const float *d_R_small, void *d_T_large, float *d_R_large, int64_t n,

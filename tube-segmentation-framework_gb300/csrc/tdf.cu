@@ -85,9 +85,8 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 constexpr int kSeg = 128;
 constexpr int kTdfWarps = 4;
 
-template <int ST, bool NORM, bool UNORM, bool PAIRS>
-__global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F,
-                                                                    const void *__restrict__ Fs, int X, int Y, int Z,
+template <int ST, bool NORM, bool UNORM>
+__global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                                     float rmin, float rmax, float rstep,
                                                                     const CircleTable tab, void *T,
                                                                     float *__restrict__ Rout, int fast_ok) {
@@ -139,13 +138,8 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                         const float va0 = c * e3x + s * e2x;
                         const float va1 = c * e3y + s * e2y;
                         const float va2 = c * e3z + s * e2z;
-                        float3 smp;
-                        if constexpr (PAIRS)
-                            smp = sample_linear_pair<ST>(F, Fs, X, XY, fx + radius * va0, fy + radius * va1,
-                                                         fz + radius * va2);
-                        else
-                            smp = sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1,
-                                                       fz + radius * va2);
+                        const float3 smp =
+                            sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1, fz + radius * va2);
                         const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
                         rs = rs + dt;
                     }
@@ -208,9 +202,8 @@ __global__ void combine_kernel(const void *__restrict__ Ts, const float *__restr
 }
 
 // tdf_mode: 0 = default (load-balanced sweeps), 1 = one voxel per lane.
-// d_shift: the field shifted by one texel (16-bit formats, X even), or NULL.
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, const void *d_shift) {
+                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode) {
     int r = check_dims(X, Y, Z);
     if (r) return r;
     if (!d_field4 || !d_T || !d_R) return fail(TSF_ERR_INVALID_ARG, "null buffer");
@@ -221,16 +214,11 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
     const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
     const bool queue = tdf_mode != 1;
     const int fast_ok = (int64_t)X * Y * Z < ((int64_t)1 << 31) - 1;   // 32-bit texel offsets
-    const bool pairs = d_shift && st != TSF_STORE_F32 && X % 2 == 0 && fast_ok &&
-                       (((uintptr_t)d_field4 | (uintptr_t)d_shift) & 15) == 0;
 #define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
     do {                                                                                                             \
-        if (queue && pairs && ST != TSF_STORE_F32)                                                                   \
-            tdf_queue_kernel<ST, NORM, UN, ST != TSF_STORE_F32><<<qblocks, 32 * kTdfWarps, 0, s>>>(                  \
-                d_field4, d_shift, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok);                              \
-        else if (queue)                                                                                              \
-            tdf_queue_kernel<ST, NORM, UN, false><<<qblocks, 32 * kTdfWarps, 0, s>>>(                                \
-                d_field4, nullptr, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok);                              \
+        if (queue)                                                                                                   \
+            tdf_queue_kernel<ST, NORM, UN><<<qblocks, 32 * kTdfWarps, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, \
+                                                                              tab, d_T, d_R, fast_ok);               \
         else                                                                                                         \
             tdf_circle_kernel<ST, NORM, UN><<<g, b, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R);    \
     } while (0)
@@ -244,26 +232,6 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
 #undef TSF_TDF_LAUNCH
     TSF_CHECK_LAUNCH("tdf_circle_kernel");
     return TSF_OK;
-}
-
-// Workspace of the paired sampler: the field shifted by one texel.
-size_t tdf_circle_workspace_size(int X, int Y, int Z, int st) {
-    if (st == TSF_STORE_F32 || !valid_storage(st)) return 0;
-    return ((size_t)X * Y * Z * 8 + 255) & ~(size_t)255;
-}
-
-int launch_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                         void *d_T, int unorm, float *d_R, void *ws, size_t ws_bytes, cudaStream_t s) {
-    int r = check_dims(X, Y, Z);
-    if (r) return r;
-    if (!d_field4) return fail(TSF_ERR_INVALID_ARG, "null buffer");
-    const size_t need = tdf_circle_workspace_size(X, Y, Z, st);
-    if (need == 0) return launch_tdf_circle(d_field4, X, Y, Z, st, rmin, rmax, rstep, d_T, unorm, d_R, s, 0, nullptr);
-    if (!ws || ws_bytes < need) return fail(TSF_ERR_WORKSPACE, "TDF workspace too small");
-    const size_t n = (size_t)X * Y * Z;
-    TSF_TRY_CUDA(cudaMemcpyAsync(ws, reinterpret_cast<const char *>(d_field4) + 8, (n - 1) * 8,
-                                 cudaMemcpyDeviceToDevice, s));
-    return launch_tdf_circle(d_field4, X, Y, Z, st, rmin, rmax, rstep, d_T, unorm, d_R, s, 0, ws);
 }
 
 int launch_tdf_combine(const void *Ts, const float *Rs, void *Tl, float *Rl, int64_t n, int unorm, cudaStream_t s) {

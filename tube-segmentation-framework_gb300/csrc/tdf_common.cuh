@@ -121,51 +121,6 @@ __device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY,
     return o;
 }
 
-// sample_linear_in for 16-bit formats with the x-corner pairs fetched as one
-// 16-byte load each: texels i and i+1 are the 16 bytes at byte 8i of the
-// field -- aligned when i is even; for odd i they are read from Fs, a copy of
-// the field shifted by one texel (Fs[k] = F[k+1]), where they start at the
-// even texel i-1.  X must be even, so all four corner rows of a sample share
-// the parity of their x index.  Same texel values, same bits.
-template <int ST>
-__device__ __forceinline__ float4 texel8(unsigned lo, unsigned hi) {
-    using T = typename Store<ST>::T;
-    T c[4];
-    memcpy(c, &lo, 4);
-    memcpy(c + 2, &hi, 4);
-    return make_float4(Store<ST>::load(c[0]), Store<ST>::load(c[1]), Store<ST>::load(c[2]), Store<ST>::load(c[3]));
-}
-
-template <int ST>
-__device__ __forceinline__ float3 sample_linear_pair(const void *F, const void *Fs, int X, int XY, float u, float v,
-                                                     float w) {
-    static_assert(ST != TSF_STORE_F32, "16-bit field4 texels only");
-    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
-    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
-    const float a = uu - fu, b = vv - fv, c = ww - fw;
-    const int base = (int)fu + X * (int)fv + XY * (int)fw;
-    const char *p = (base & 1) ? reinterpret_cast<const char *>(Fs) - 8 : reinterpret_cast<const char *>(F);
-    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
-    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
-    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
-    const uint4 r00 = __ldg(reinterpret_cast<const uint4 *>(p + 8 * (int64_t)base));
-    const uint4 r10 = __ldg(reinterpret_cast<const uint4 *>(p + 8 * (int64_t)(base + X)));
-    const uint4 r01 = __ldg(reinterpret_cast<const uint4 *>(p + 8 * (int64_t)(base + XY)));
-    const uint4 r11 = __ldg(reinterpret_cast<const uint4 *>(p + 8 * (int64_t)(base + XY + X)));
-    const float4 t000 = texel8<ST>(r00.x, r00.y), t100 = texel8<ST>(r00.z, r00.w);
-    const float4 t010 = texel8<ST>(r10.x, r10.y), t110 = texel8<ST>(r10.z, r10.w);
-    const float4 t001 = texel8<ST>(r01.x, r01.y), t101 = texel8<ST>(r01.z, r01.w);
-    const float4 t011 = texel8<ST>(r11.x, r11.y), t111 = texel8<ST>(r11.z, r11.w);
-    float3 o;
-    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
-    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
-    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
-    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
-    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
-    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
-    return o;
-}
-
 // Margin m such that every trilinear corner of a sample at distance <= r
 // from a voxel lies within m - 1 voxels of it, for sample directions
 // a = cos e3 + sin e2 with |e2|, |e3| <= 1.00005 and |e2 . e3| <= 1e-3

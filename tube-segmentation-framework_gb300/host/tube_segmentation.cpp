@@ -232,14 +232,7 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4small.p, S), "vector field");
         Ts.alloc(n * ts);
         Rs.alloc(n * 4);
-        {
-            const size_t tb = tsf_tdf_circle_workspace_size(X, Y, Z, st);
-            DevBuf tws(tb ? tb : 256);
-            check(tsf_tdf_circle_ws(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), tws.p, tb,
-                                    S),
-                  "TDF");
-            cudaStreamSynchronize(static_cast<cudaStream_t>(S));   // the workspace is freed at the end of this scope
-        }
+        check(tsf_tdf_circle(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), S), "TDF");
         if (rMax < 2.5f) {
             out.T.p = Ts.release();
             out.R.p = Rs.release();
@@ -280,14 +273,8 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
     }
     out.T.alloc(n * ts);
     out.R.alloc(n * 4);
-    {
-        const size_t tb = tsf_tdf_circle_workspace_size(X, Y, Z, st);
-        DevBuf tws(tb ? tb : 256);
-        check(tsf_tdf_circle_ws(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
-                                out.R.as<float>(), tws.p, tb, S),
-              "TDF");
-        cudaStreamSynchronize(static_cast<cudaStream_t>(S));
-    }
+    check(tsf_tdf_circle(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
+                         out.R.as<float>(), S), "TDF");
     if (rMin < 2.5f)
         check(tsf_tdf_combine(Ts.p, Rs.as<float>(), out.T.p, out.R.as<float>(), (int64_t)n, tdf16, S), "combine");
 }

@@ -82,8 +82,6 @@ def _declare(L):
         "tsf_blur_backward_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_blur_backward": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
-        "tsf_tdf_circle_workspace_size": (_sz, [_i, _i, _i, _i]),
-        "tsf_tdf_circle_ws": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p, _sz, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
         "tsf_tdf_circle_mode": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _i, _p]),
         "tsf_candidates_workspace_size": (_sz, [_i, _i, _i]),
@@ -292,24 +290,14 @@ def gvf_finish(v, storage: str = "f32", out=None, stream=None):
     return out
 
 
-def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, mode: int = 2,
+def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, mode: int = 0,
                stream=None):
-    """mode 2 (default): tsf_tdf_circle_ws (paired x-corner loads for 16-bit
-    fields); 0: tsf_tdf_circle's kernel without a workspace; 1: one voxel per
-    lane.  All identical."""
     torch = _torch()
     Z, Y, X = field4.shape[:3]
-    L = load()
     T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
     R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
-    if mode == 2:
-        ws = workspace(L.tsf_tdf_circle_workspace_size(X, Y, Z, STORAGE[storage]))
-        _check(L.tsf_tdf_circle_ws(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax), float(rstep),
-                                   _ptr(T), int(unorm16), _ptr(R), _ptr(ws) if ws.numel() else None, ws.numel(),
-                                   _stream(stream)))
-        return T, R
-    _check(L.tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
-                                 float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
+    _check(load().tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
+                                      float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
     return T, R
 
 
