@@ -34,8 +34,10 @@ class Params:
         self.checkpoint_every = checkpoint_every
 
 
-def forward(vol, p: Params):
-    """vol: float32 CUDA tensor [Z, Y, X].  Returns (T, state)."""
+def forward(vol, p: Params, reuse=None):
+    """vol: float32 CUDA tensor [Z, Y, X].  Returns (T, state).  reuse: a
+    previous state whose GVF adjoint workspace (possibly ~100 GB) is taken
+    over when the size matches, so repeated calls do not allocate."""
     import torch
     st = "f32"
     s = {}
@@ -43,8 +45,16 @@ def forward(vol, p: Params):
     Ts, Rs = T.tdf_circle(f_s, p.rmin, 3.0, 0.5, st)
     b = T.blur(vol, p.sigma)
     f0, _ = T.vector_field(b, p.fmax, p.vsign, st, planar=True, field4=False)
-    C = p.checkpoint_every if p.checkpoint_every > 0 else T.gvf_adjoint_interval(f0, p.iterations, st)
-    ws = T.gvf_adjoint_workspace(f0, p.iterations, st, C)
+    ws = None
+    if reuse is not None and reuse.get("gvf_ws") is not None and (
+            p.checkpoint_every <= 0 or p.checkpoint_every == reuse["checkpoint_every"]):
+        C = reuse["checkpoint_every"]
+        need = T.load().tsf_gvf_adjoint_workspace_size(*reversed(f0.shape[1:]), T.STORAGE[st], p.iterations, C)
+        if reuse["gvf_ws"].numel() >= need:
+            ws = reuse.pop("gvf_ws")
+    if ws is None:
+        C = p.checkpoint_every if p.checkpoint_every > 0 else T.gvf_adjoint_interval(f0, p.iterations, st)
+        ws = T.gvf_adjoint_workspace(f0, p.iterations, st, C)
     v = T.gvf_checkpointed(f0, p.mu, p.iterations, ws, st, C)
     F = T.gvf_finish(v, st)
     Tl, Rl = T.tdf_circle(F, max(2.5, p.rmin), p.rmax, p.rstep, st)
@@ -75,14 +85,14 @@ def backward(state, gT, p: Params):
     return gI, dmu, dsigma
 
 
-def loss_and_grad(vol, G, p: Params):
-    Tc, state = forward(vol, p)
+def loss_and_grad(vol, G, p: Params, reuse=None):
+    Tc, state = forward(vol, p, reuse)
     n = Tc.numel()
     diff = Tc - G
     L = float((diff.double() ** 2).sum() / n)
     gT = (2.0 / n) * diff
     gI, dmu, dsigma = backward(state, gT.float().contiguous(), p)
-    return L, gI, dmu, dsigma
+    return L, gI, dmu, dsigma, state
 
 
 def calibrate(vol, G, p: Params, steps=20, lr_mu=0.005, lr_sigma=0.05, log=None):
@@ -92,8 +102,9 @@ def calibrate(vol, G, p: Params, steps=20, lr_mu=0.005, lr_sigma=0.05, log=None)
     m = [0.0, 0.0]
     v2 = [0.0, 0.0]
     hist = []
+    state = None
     for t in range(1, steps + 1):
-        L, _, dmu, dsig = loss_and_grad(vol, G, p)
+        L, _, dmu, dsig, state = loss_and_grad(vol, G, p, state)
         hist.append({"step": t - 1, "loss": L, "mu": p.mu, "sigma": p.sigma, "dmu": dmu, "dsigma": dsig})
         if log:
             log(hist[-1])
@@ -104,6 +115,6 @@ def calibrate(vol, G, p: Params, steps=20, lr_mu=0.005, lr_sigma=0.05, log=None)
         vh = [v2[k] / (1 - b2 ** t) for k in range(2)]
         p.mu = min(max(p.mu - lr_mu * mh[0] / (math.sqrt(vh[0]) + eps), 1e-3), 1.0 / 12 - 1e-3)
         p.sigma = min(max(p.sigma - lr_sigma * mh[1] / (math.sqrt(vh[1]) + eps), 0.25), 5.0)
-    L, _, _, _ = loss_and_grad(vol, G, p)
+    L, _, _, _, _ = loss_and_grad(vol, G, p, state)
     hist.append({"step": steps, "loss": L, "mu": p.mu, "sigma": p.sigma})
     return p, hist
