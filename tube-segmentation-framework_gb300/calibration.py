@@ -65,23 +65,29 @@ def forward(vol, p: Params, reuse=None):
     return Tc, s
 
 
-def backward(state, gT, p: Params):
-    """dL/dI (tensor), dL/dmu, dL/dsigma for dL/dT = gT."""
+def backward(state, gT, p: Params, mark=None):
+    """dL/dI (tensor), dL/dmu, dL/dsigma for dL/dT = gT.  mark(name), if
+    given, is called after each stage (timing)."""
     import torch
     st = "f32"
+    mark = mark or (lambda name: None)
     vol = state["vol"]
     small = state["small"]
     gTs = torch.where(small, gT, torch.zeros_like(gT)).contiguous()
     gTl = torch.where(small, torch.zeros_like(gT), gT).contiguous()
     # small pass -> the un-diffused field of I
     g_fs = T.tdf_backward(state["f_s"], p.rmin, 3.0, 0.5, gTs, st, T=state["Ts"], R=state["Rs"])
+    mark("tdf_small_backward")
     gI = T.vector_field_backward(vol, g_fs, p.fmax, p.vsign)
     # large pass -> GVF -> vector field -> blur
     g_v = T.tdf_backward(state["F"], max(2.5, p.rmin), p.rmax, p.rstep, gTl, st, T=state["Tl"], R=state["Rl"])
+    mark("tdf_large_backward")
     g_f0, dmu = T.gvf_adjoint(state["f0"], p.mu, p.iterations, g_v, st, state["checkpoint_every"],
                               ws=state["gvf_ws"], checkpoints_stored=True)
+    mark("gvf_adjoint")
     g_b = T.vector_field_backward(state["b"], g_f0, p.fmax, p.vsign)
     gI, dsigma = T.blur_backward(vol, g_b, p.sigma, gin=gI)
+    mark("vector_field_and_blur_backward")
     return gI, dmu, dsigma
 
 
