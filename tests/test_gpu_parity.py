@@ -224,7 +224,7 @@ def test_candidates_count_range_error(torch_dev, tsf, oracle, synth):
 
 
 @pytest.mark.parametrize("storage", ["f32", "snorm16", "f16"])
-@pytest.mark.parametrize("shape", [(32, 32, 32), (28, 32, 36)])
+@pytest.mark.parametrize("shape", [(32, 32, 32), (28, 32, 36), (24, 20, 40)])
 def test_fmg_bitexact(torch_dev, tsf, oracle, synth, storage, shape):
     torch = torch_dev
     vol = oracle.blur(_vol(synth, shape, 10), 0.5)

@@ -17,7 +17,7 @@
 // All images of one run live in one workspace, laid out once; the restricted
 // |f|^2 images are computed once per run (the reference recomputes identical
 // ones in every cycle).
-#include "tsf_common.cuh"
+#include "packed.cuh"
 
 namespace tsf {
 
@@ -185,6 +185,202 @@ __global__ void fmg_finish_kernel(const ST_T<ST> *fx, const ST_T<ST> *fy, const 
 }
 
 // ---------------------------------------------------------------------------
+// vectorised level kernels: one thread per 16-byte vector of a row (8 voxels
+// of a 16-bit format, 4 of FP32), loads issued together, x-neighbours by
+// shuffles.  Rows evaluate at mirror(y), planes at mirror(z); the vector
+// holding x = 0 / X-1 copies the result of x = 2 / X-3.  Per voxel the
+// arithmetic is exactly the scalar kernels', so the results are identical.
+// ---------------------------------------------------------------------------
+template <int ST> struct FmgVec {
+    using P = PackedV<ST, 16>;
+    using Raw = typename P::Raw;
+    static constexpr int VX = P::VX;
+};
+
+// x-neighbours of a row vector c: xl = value at x0-1, xr = value at x0+VX
+template <int VX>
+__device__ __forceinline__ void fmg_xnb(const float c[VX], float el, float er, int lane, float &xl, float &xr) {
+    const unsigned full = 0xffffffffu;
+    xl = __shfl_up_sync(full, c[VX - 1], 1);
+    xr = __shfl_down_sync(full, c[0], 1);
+    if (lane == 0) xl = el;
+    if (lane == 31) xr = er;
+}
+
+#define FMG_VEC_PROLOGUE(d)                                                     \
+    using P = typename FmgVec<ST>::P;                                           \
+    constexpr int VX = FmgVec<ST>::VX;                                          \
+    const int lane = threadIdx.x;                                               \
+    const int y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;       \
+    if (y >= (d).y) return;                                                     \
+    const int x0 = (blockIdx.x * 32 + lane) * VX;                               \
+    const bool act = x0 < (d).x;                                                \
+    const int py = mirror(y, (d).y), pz = mirror(z, (d).z);                     \
+    const int64_t sy = (d).x, sz = (int64_t)(d).x * (d).y;                      \
+    const int64_t p = (int64_t)pz * sz + (int64_t)py * sy + (act ? x0 : 0);     \
+    const int64_t o = (int64_t)z * sz + (int64_t)y * sy + x0;
+
+template <int ST>
+__device__ __forceinline__ void fmg_load(const ST_T<ST> *a, int64_t i, bool act, float out[FmgVec<ST>::VX]) {
+    using P = typename FmgVec<ST>::P;
+    P::unpack(act ? P::load(a + i) : P::zero(), out);
+}
+
+// GVFgaussSeidel (RED) / GVFgaussSeidel2, vectorised.  RED: lanes on black
+// points write the source value, which no later pass reads (the reference
+// leaves them unwritten).
+template <int ST, bool RED>
+__global__ void __launch_bounds__(256) gs_vec_kernel(const ST_T<ST> *src, ST_T<ST> *dst, const ST_T<ST> *r,
+                                                     const ST_T<ST> *sq, Dim d, float two_mu, float twelve_mu,
+                                                     float hh, float two_hh) {
+    FMG_VEC_PROLOGUE(d);
+    float c[VX], yp[VX], ym[VX], zp[VX], zm[VX], rr[VX], qq[VX];
+    fmg_load<ST>(src, p, act, c);
+    fmg_load<ST>(src, p + sy, act, yp);
+    fmg_load<ST>(src, p - sy, act, ym);
+    fmg_load<ST>(src, p + sz, act, zp);
+    fmg_load<ST>(src, p - sz, act, zm);
+    fmg_load<ST>(r, p, act, rr);
+    fmg_load<ST>(sq, p, act, qq);
+    const float el = (act && x0 > 0) ? Store<ST>::load(src[p - 1]) : 0.0f;
+    const float er = (act && x0 + VX < d.x) ? Store<ST>::load(src[p + VX]) : 0.0f;
+    float xl, xr;
+    fmg_xnb<VX>(c, el, er, lane, xl, xr);
+    if (x0 + VX >= d.x) xr = er;                  // last vector of a row: no lane to the right
+    float res[VX];
+#pragma unroll
+    for (int i = 0; i < VX; i++) {
+        const bool red = ((x0 + i + py + pz) & 1) == 0;
+        if (RED != red) {
+            res[i] = c[i];
+        } else {
+            float s = i == VX - 1 ? xr : c[i + 1 < VX ? i + 1 : i];
+            s = s + (i == 0 ? xl : c[i > 0 ? i - 1 : 0]);
+            s = s + yp[i];
+            s = s + ym[i];
+            s = s + zp[i];
+            s = s + zm[i];
+            const float num = two_mu * s - two_hh * rr[i];
+            const float den = twelve_mu + hh * qq[i];
+            res[i] = num / den;
+        }
+    }
+    if (x0 == 0) res[0] = res[2];
+    if (x0 + VX == d.x) res[VX - 1] = res[VX - 3];
+    if (act) P::store(dst + o, res);
+}
+
+// residual (kernels.cl:1973-2006), vectorised
+template <int ST>
+__global__ void __launch_bounds__(256) residual_vec_kernel(const ST_T<ST> *r, const ST_T<ST> *v, const ST_T<ST> *sq,
+                                                           Dim d, float mu, float h, ST_T<ST> *out) {
+    FMG_VEC_PROLOGUE(d);
+    float c[VX], yp[VX], ym[VX], zp[VX], zm[VX], rr[VX], qq[VX];
+    fmg_load<ST>(v, p, act, c);
+    fmg_load<ST>(v, p + sy, act, yp);
+    fmg_load<ST>(v, p - sy, act, ym);
+    fmg_load<ST>(v, p + sz, act, zp);
+    fmg_load<ST>(v, p - sz, act, zm);
+    fmg_load<ST>(r, p, act, rr);
+    fmg_load<ST>(sq, p, act, qq);
+    const float el = (act && x0 > 0) ? Store<ST>::load(v[p - 1]) : 0.0f;
+    const float er = (act && x0 + VX < d.x) ? Store<ST>::load(v[p + VX]) : 0.0f;
+    float xl, xr;
+    fmg_xnb<VX>(c, el, er, lane, xl, xr);
+    if (x0 + VX >= d.x) xr = er;
+    float res[VX];
+#pragma unroll
+    for (int i = 0; i < VX; i++) {
+        float s = i == VX - 1 ? xr : c[i + 1 < VX ? i + 1 : i];
+        s = s + (i == 0 ? xl : c[i > 0 ? i - 1 : 0]);
+        s = s + yp[i];
+        s = s + ym[i];
+        s = s + zp[i];
+        s = s + zm[i];
+        s = s - 6.0f * c[i];
+        const float lap = (mu * s) / (h * h);
+        res[i] = rr[i] - (lap - qq[i] * c[i]);
+    }
+    if (x0 == 0) res[0] = res[2];
+    if (x0 + VX == d.x) res[VX - 1] = res[VX - 3];
+    if (act) P::store(out + o, res);
+}
+
+// fmgResidual (kernels.cl:2008-2053), spacing 1, vectorised
+template <int ST>
+__global__ void __launch_bounds__(256) fmg_residual_vec_kernel(const void *F, const ST_T<ST> *f, Dim d, int comp,
+                                                               float mu, ST_T<ST> *out) {
+    FMG_VEC_PROLOGUE(d);
+    float c[VX], yp[VX], ym[VX], zp[VX], zm[VX];
+    fmg_load<ST>(f, p, act, c);
+    fmg_load<ST>(f, p + sy, act, yp);
+    fmg_load<ST>(f, p - sy, act, ym);
+    fmg_load<ST>(f, p + sz, act, zp);
+    fmg_load<ST>(f, p - sz, act, zm);
+    const float el = (act && x0 > 0) ? Store<ST>::load(f[p - 1]) : 0.0f;
+    const float er = (act && x0 + VX < d.x) ? Store<ST>::load(f[p + VX]) : 0.0f;
+    float xl, xr;
+    fmg_xnb<VX>(c, el, er, lane, xl, xr);
+    if (x0 + VX >= d.x) xr = er;
+    float res[VX];
+#pragma unroll
+    for (int i = 0; i < VX; i++) {
+        const float4 q = act ? Vec4Load<ST>::load(F, p + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float v0 = comp == 0 ? q.x : (comp == 1 ? q.y : q.z);
+        const float sqm = (q.x * q.x + q.y * q.y) + q.z * q.z;
+        float s = i == VX - 1 ? xr : c[i + 1 < VX ? i + 1 : i];
+        s = s + (i == 0 ? xl : c[i > 0 ? i - 1 : 0]);
+        s = s + yp[i];
+        s = s + ym[i];
+        s = s + zp[i];
+        s = s + zm[i];
+        s = s - 6.0f * c[i];
+        const float rs = (mu * s) / (1.0f * 1.0f);
+        res[i] = (-sqm) * v0 - (rs - sqm * c[i]);
+    }
+    if (x0 == 0) res[0] = res[2];
+    if (x0 + VX == d.x) res[VX - 1] = res[VX - 3];
+    if (act) P::store(out + o, res);
+}
+
+// prolongate (ADD, in place on v) / prolongate2, vectorised: fine x0..x0+VX-1
+// take coarse x0/2 .. (x0+VX-1)/2 (0 outside the coarse image)
+template <int ST, bool ADD>
+__global__ void __launch_bounds__(256) prolong_vec_kernel(const ST_T<ST> *coarse, Dim fd, Dim cd, ST_T<ST> *v) {
+    using P = typename FmgVec<ST>::P;
+    constexpr int VX = FmgVec<ST>::VX;
+    const int lane = threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
+    if (y >= fd.y) return;
+    const int x0 = (blockIdx.x * 32 + lane) * VX;
+    if (x0 >= fd.x) return;
+    const int64_t o = ((int64_t)z * fd.y + y) * fd.x + x0;
+    float res[VX];
+    if (ADD) P::unpack(P::load(v + o), res);
+#pragma unroll
+    for (int i = 0; i < VX; i++) {
+        const float c = ld0<ST>(coarse, cd, (x0 + i) / 2, y / 2, z / 2);
+        res[i] = ADD ? res[i] + c : c;
+    }
+    P::store(v + o, res);
+}
+
+// addTwoImages, vectorised (n a multiple of VX)
+template <int ST>
+__global__ void __launch_bounds__(256) add_vec_kernel(ST_T<ST> *a, const ST_T<ST> *b, int64_t nvec) {
+    using P = typename FmgVec<ST>::P;
+    constexpr int VX = FmgVec<ST>::VX;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nvec) return;
+    float x[VX], y[VX];
+    P::unpack(P::load(a + i * VX), x);
+    P::unpack(P::load(b + i * VX), y);
+#pragma unroll
+    for (int k = 0; k < VX; k++) x[k] = x[k] + y[k];
+    P::store(a + i * VX, x);
+}
+
+// ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
 constexpr int kLevels = 3;  // l_max = 2 (gradientVectorFlow.cpp:750)
@@ -230,6 +426,11 @@ template <int ST> struct FmgRun {
     T *buf(size_t off) const { return reinterpret_cast<T *>(ws + off); }
     static dim3 blk() { return dim3(32, 4, 2); }
     static dim3 grd(Dim d) { return dim3((d.x + 31) / 32, (d.y + 3) / 4, (d.z + 1) / 2); }
+    // vectorised kernels: rows that split into at least two 16-byte vectors
+    static constexpr int VX = FmgVec<ST>::VX;
+    static bool vec(Dim d) { return d.x % VX == 0 && d.x >= 2 * VX; }
+    static dim3 vblk() { return dim3(32, 8, 1); }
+    static dim3 vgrd(Dim d) { return dim3((d.x / VX + 31) / 32, (d.y + 7) / 8, d.z); }
 
     int gs(int l, T *v, const T *r, float h, int iterations) {
         if (iterations <= 0) return TSF_OK;
@@ -238,8 +439,13 @@ template <int ST> struct FmgRun {
         const T *sq = buf(L.sq[l]);
         const float two_mu = 2.0f * mu, twelve_mu = 12.0f * mu, hh = h * h, two_hh = (2.0f * h) * h;
         for (int i = 0; i < iterations; i++) {
-            gs_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh);
-            gs_kernel<ST, false><<<grd(d), blk(), 0, s>>>(v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+            if (vec(d)) {
+                gs_vec_kernel<ST, true><<<vgrd(d), vblk(), 0, s>>>(v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+                gs_vec_kernel<ST, false><<<vgrd(d), vblk(), 0, s>>>(v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+            } else {
+                gs_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+                gs_kernel<ST, false><<<grd(d), blk(), 0, s>>>(v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+            }
         }
         TSF_CHECK_LAUNCHES("gs_kernel", 2 * iterations);
         return TSF_OK;
@@ -252,7 +458,8 @@ template <int ST> struct FmgRun {
         if (l < kLevels - 1) {
             const Dim d = L.d[l], nd = L.d[l + 1];
             T *p = buf(L.p[l]);
-            residual_kernel<ST><<<grd(d), blk(), 0, s>>>(r, v, buf(L.sq[l]), d, mu, h, p);
+            if (vec(d)) residual_vec_kernel<ST><<<vgrd(d), vblk(), 0, s>>>(r, v, buf(L.sq[l]), d, mu, h, p);
+            else residual_kernel<ST><<<grd(d), blk(), 0, s>>>(r, v, buf(L.sq[l]), d, mu, h, p);
             T *r1 = buf(L.r[l + 1]);
             restrict_kernel<ST><<<grd(nd), blk(), 0, s>>>(p, d, nd, r1);
             T *v1 = buf(L.v[l + 1]);
@@ -260,9 +467,14 @@ template <int ST> struct FmgRun {
             TSF_CHECK_LAUNCHES("residual/restrict", 2);
             e = vcycle(l + 1, r1, v1, h * 2.0f);
             if (e) return e;
-            prolong_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v1, d, nd, p);
-            TSF_CHECK_LAUNCH("prolong_kernel");
-            TSF_TRY_CUDA(cudaMemcpyAsync(v, p, sizeof(T) * (size_t)nvox(d), cudaMemcpyDeviceToDevice, s));
+            if (vec(d)) {
+                prolong_vec_kernel<ST, true><<<vgrd(d), vblk(), 0, s>>>(v1, d, nd, v);   // in place
+                TSF_CHECK_LAUNCH("prolong_vec_kernel");
+            } else {
+                prolong_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v1, d, nd, p);
+                TSF_CHECK_LAUNCH("prolong_kernel");
+                TSF_TRY_CUDA(cudaMemcpyAsync(v, p, sizeof(T) * (size_t)nvox(d), cudaMemcpyDeviceToDevice, s));
+            }
         }
         return gs(l, v, r, h, 2);
     }
@@ -277,7 +489,8 @@ template <int ST> struct FmgRun {
             TSF_CHECK_LAUNCH("restrict_kernel");
             int e = full(l + 1, h * 2.0f);
             if (e) return e;
-            prolong_kernel<ST, false><<<grd(d), blk(), 0, s>>>(nullptr, buf(L.v[l + 1]), d, nd, v);
+            if (vec(d)) prolong_vec_kernel<ST, false><<<vgrd(d), vblk(), 0, s>>>(buf(L.v[l + 1]), d, nd, v);
+            else prolong_kernel<ST, false><<<grd(d), blk(), 0, s>>>(nullptr, buf(L.v[l + 1]), d, nd, v);
             TSF_CHECK_LAUNCH("prolong_kernel");
         } else {
             TSF_TRY_CUDA(cudaMemsetAsync(v, 0, sizeof(T) * (size_t)nvox(d), s));
@@ -297,11 +510,17 @@ template <int ST> struct FmgRun {
             T *f = buf(L.comp[c]);
             TSF_TRY_CUDA(cudaMemsetAsync(f, 0, sizeof(T) * (size_t)n0, s));
             for (int it = 0; it < iterations; it++) {
-                fmg_residual_kernel<ST><<<grd(d0), blk(), 0, s>>>(F, f, d0, c, mu, buf(L.r[0]));
+                if (vec(d0)) fmg_residual_vec_kernel<ST><<<vgrd(d0), vblk(), 0, s>>>(F, f, d0, c, mu, buf(L.r[0]));
+                else fmg_residual_kernel<ST><<<grd(d0), blk(), 0, s>>>(F, f, d0, c, mu, buf(L.r[0]));
                 TSF_CHECK_LAUNCH("fmg_residual_kernel");
                 int e = full(0, 1.0f);
                 if (e) return e;
-                add_kernel<ST><<<nb, 256, 0, s>>>(f, buf(L.v[0]), n0);
+                if (vec(d0)) {
+                    const int64_t nvec = n0 / VX;
+                    add_vec_kernel<ST><<<(unsigned)((nvec + 255) / 256), 256, 0, s>>>(f, buf(L.v[0]), nvec);
+                } else {
+                    add_kernel<ST><<<nb, 256, 0, s>>>(f, buf(L.v[0]), n0);
+                }
                 TSF_CHECK_LAUNCH("add_kernel");
             }
         }
