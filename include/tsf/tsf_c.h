@@ -232,6 +232,66 @@ int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, 
 int tsf_tdf_combine(const void *d_T_small, const float *d_R_small, void *d_T_large,
                     float *d_R_large, int64_t n, int tdf_unorm16, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Centerline linking
+ * ------------------------------------------------------------------------- */
+
+/* runNewCenterlineAlg after the vertex list (parallelCenterlineExtraction.cpp:
+ * 911-1161; kernels linkLengths, compact, linkCenterpoints,
+ * removeDuplicateEdges, graphComponentLabeling, calculateTreeLength,
+ * kernels.cl:327-508, and the 2-D pyramid enumeration of the edge image).
+ * d_vertices: n_vertices x 3 int (x, y, z), n_vertices <= 16384; d_T: the TDF
+ * (float, or unorm16 when tdf_unorm16 != 0).  Writes the edges (pairs of
+ * vertex indices, at most 2 n_vertices, in the reference's pyramid order) to
+ * d_edges and their count to *n_edges (host; the call synchronises
+ * `stream`), each vertex's component label (the smallest vertex index of the
+ * component) to d_labels and the component sizes, indexed by label, to
+ * d_tree_sizes.  Candidate partners are listed in ascending index (the
+ * reference's atomic compaction leaves that order, and so the choice between
+ * pairs of equal length, to chance).  TSF_ERR_COUNT_RANGE ("No edges were
+ * found") when nothing links. */
+size_t tsf_link_workspace_size(int n_vertices);
+int tsf_link_centerpoints(const int *d_vertices, int n_vertices, const void *d_T, int tdf_unorm16,
+                          int X, int Y, int Z, float min_mean_tdf, float max_distance, int *d_edges,
+                          int *n_edges, int *d_labels, int *d_tree_sizes, void *d_workspace,
+                          size_t workspace_bytes, void *stream);
+
+/* removeSmallTrees (kernels.cl:510-534; the reference's GPU rasterisation,
+ * used when loop removal is off): sets d_centerlines (X*Y*Z int8, zeroed by
+ * the caller) to 1 along the edges of components of at least
+ * min_tree_length vertices. */
+int tsf_rasterize_trees(const int *d_vertices, const int *d_edges, int n_edges, const int *d_labels,
+                        const int *d_tree_sizes, int min_tree_length, int8_t *d_centerlines, int X,
+                        int Y, int Z, void *stream);
+
+/* Host functions (no device memory): the CPU part of runNewCenterlineAlg
+ * when loop removal or a VTK centerline file is requested
+ * (parallelCenterlineExtraction.cpp:1168-1247).
+ *
+ * tsf_centerline_graph: from the linked graph (vertices, edges, labels and
+ * tree sizes as tsf_link_centerpoints gives them, copied to the host) keeps
+ * the trees of at least min_tree_length vertices, splits edges longer than
+ * max_edge_distance (0 = no splitting; the reference splits only for the VTK
+ * file), removes loops (removeLoops, :129-285) and rasterises the result
+ * into centerlines (X*Y*Z int8, written) while replacing the radius along
+ * each edge by its mean (createCenterlineVoxels, :287-321; radius X*Y*Z
+ * float, updated).  The final graph goes to out_vertices (x, y, z) and
+ * out_edges; both counts are returned, and TSF_ERR_CAPACITY when either
+ * exceeds `capacity` (call again with more).  TSF_ERR_COUNT_RANGE when no
+ * vertex survives ("Centerline graph size is 0").
+ * tsf_remove_loops: removeLoops alone.
+ * tsf_write_centerline_vtk: writeToVtkFile (inputOutput.cpp:48-63). */
+int tsf_centerline_graph(const int *vertices, int n_vertices, const int *edges, int n_edges,
+                         const int *labels, const int *tree_sizes, int min_tree_length,
+                         int max_edge_distance, int X, int Y, int Z, float *radius,
+                         int8_t *centerlines, int *out_vertices, int *out_edges, int capacity,
+                         int *n_out_vertices, int *n_out_edges);
+int tsf_remove_loops(const int *vertices, int n_vertices, const int *edges, int n_edges, int X,
+                     int Y, int Z, int *out_vertices, int *out_edges, int capacity,
+                     int *n_out_vertices, int *n_out_edges);
+int tsf_write_centerline_vtk(const char *path, const int *vertices, int n_vertices,
+                             const int *edges, int n_edges);
+
 /* Reverse-mode derivative of tsf_tdf_circle (no counterpart in the
  * reference): given d_gT = dL/dT (float per voxel), ADDS dL/d(field x,y,z) to
  * d_gfield (planar FP32, 3N) -- through the trilinear samples at the arg-max

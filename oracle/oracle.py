@@ -64,6 +64,10 @@ def _declare(L):
     L.orc_blur_mask.argtypes = [_f, _p]
     L.orc_hp_compact.restype = _i64
     L.orc_hp_compact.argtypes = [_p, _i, _i, _i, _p, _i64]
+    L.orc_link_centerpoints.restype = _i
+    L.orc_link_centerpoints.argtypes = [_p, _i, _p, _i, _i, _i, _f, _f, _p, _p, _p]
+    L.orc_rasterize_trees.restype = None
+    L.orc_rasterize_trees.argtypes = [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i]
     L.orc_threshold_f32.argtypes = [_p, _i64, _f, _p]
     L.orc_set_threads.argtypes = [_i]
     L.orc_get_threads.restype = _i
@@ -293,6 +297,35 @@ def fmg_gvf(field4, mu: float, iterations: int, storage: str = "f32", f64: bool 
 
 
 # ---- composite: the candidate stage (runNewCenterlineAlg front half) --------
+
+def link_centerpoints(vertices, T, min_mean_tdf: float, max_distance: float):
+    """runNewCenterlineAlg back half (parallelCenterlineExtraction.cpp:911-1161,
+    kernels.cl:327-508): vertices (n, 3) int (x, y, z); T the TDF as read by
+    the linear sampler (float; unorm16 already divided by 65535).  Returns
+    (edges (m, 2) in the 2-D pyramid order, labels, tree sizes)."""
+    v = np.ascontiguousarray(vertices, dtype=np.int32)
+    n = v.shape[0]
+    T32 = np.ascontiguousarray(T, dtype=np.float32)
+    Z, Y, X = T32.shape
+    edges = np.zeros((2 * n, 2), np.int32)
+    labels = np.zeros(n, np.int32)
+    sizes = np.zeros(n, np.int32)
+    ne = lib().orc_link_centerpoints(_ptr(v), n, _ptr(T32), X, Y, Z, float(min_mean_tdf), float(max_distance),
+                                     _ptr(edges), _ptr(labels), _ptr(sizes))
+    return edges[:ne].copy(), labels, sizes
+
+
+def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape):
+    """removeSmallTrees (kernels.cl:510-534) into a zeroed int8 volume."""
+    v = np.ascontiguousarray(vertices, dtype=np.int32)
+    e = np.ascontiguousarray(edges, dtype=np.int32)
+    out = np.zeros(shape, np.int8)
+    Z, Y, X = shape
+    lib().orc_rasterize_trees(_ptr(v), _ptr(e), e.shape[0], _ptr(np.ascontiguousarray(labels, dtype=np.int32)),
+                              _ptr(np.ascontiguousarray(sizes, dtype=np.int32)), int(min_tree_length), _ptr(out),
+                              X, Y, Z)
+    return out
+
 
 def centerpoints(T, R, field4, tdf_high: float, cube_size: int, f64: bool = False):
     """parallelCenterlineExtraction.cpp:667-899 up to the vertex list.

@@ -268,6 +268,174 @@ void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Centerline linking (runNewCenterlineAlg back half,                       */
+/* parallelCenterlineExtraction.cpp:911-1332; kernels.cl:327-559)           */
+/* ------------------------------------------------------------------------ */
+
+#define CLAMPI(v, n) ((v) < 0 ? 0 : ((v) >= (n) ? (n) - 1 : (v)))
+
+static float orc_vdist(const int32_t *v, int a, int b) {
+    const float dx = (float)v[3 * a] - (float)v[3 * b];
+    const float dy = (float)v[3 * a + 1] - (float)v[3 * b + 1];
+    const float dz = (float)v[3 * a + 2] - (float)v[3 * b + 2];
+    return sqrtf((dx * dx + dy * dy) + dz * dz);
+}
+
+/* the TDF through OpenCL's linear sampler (unnormalised, clamp to edge) */
+static float orc_sample_tdf(const float *T, int X, int Y, int Z, float u, float v, float w) {
+    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
+    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
+    const float a = uu - fu, b = vv - fv, c = ww - fw;
+    int i0 = (int)fu, j0 = (int)fv, k0 = (int)fw;
+    const int i1 = CLAMPI(i0 + 1, X), j1 = CLAMPI(j0 + 1, Y), k1 = CLAMPI(k0 + 1, Z);
+    i0 = CLAMPI(i0, X); j0 = CLAMPI(j0, Y); k0 = CLAMPI(k0, Z);
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+#define TT(i, j, k) T[(int64_t)(i) + (int64_t)X * ((int64_t)(j) + (int64_t)Y * (int64_t)(k))]
+    float o = ((ia * ib) * ic) * TT(i0, j0, k0);
+    o = o + ((a * ib) * ic) * TT(i1, j0, k0);
+    o = o + ((ia * b) * ic) * TT(i0, j1, k0);
+    o = o + ((a * b) * ic) * TT(i1, j1, k0);
+    o = o + ((ia * ib) * c) * TT(i0, j0, k1);
+    o = o + ((a * ib) * c) * TT(i1, j0, k1);
+    o = o + ((ia * b) * c) * TT(i0, j1, k1);
+    o = o + ((a * b) * c) * TT(i1, j1, k1);
+#undef TT
+    return o;
+}
+
+static float orc_mean_tdf(const float *T, int X, int Y, int Z, const float xa[3], const float s[3], int d) {
+    float sum = 0.0f;
+    for (int k = 0; k <= d; k++) {
+        const float alpha = (float)k / (float)d;
+        sum = sum + orc_sample_tdf(T, X, Y, Z, xa[0] + s[0] * alpha, xa[1] + s[1] * alpha, xa[2] + s[2] * alpha);
+    }
+    return sum / (float)(d + 1);
+}
+
+static uint32_t orc_hp2d_key(uint32_t x, uint32_t y) {
+    uint32_t k = 0;
+    for (int bit = 0; bit < 16; bit++) k |= (((y >> bit) & 1u) | (((x >> bit) & 1u) << 1)) << (2 * bit);
+    return k;
+}
+
+static int orc_cmp_u32(const void *a, const void *b) {
+    const uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static int orc_find(int *parent, int i) {
+    while (parent[i] != i) i = parent[i];
+    return i;
+}
+
+int orc_link_centerpoints(const int32_t *v, int n, const float *T, int X, int Y, int Z, float min_avg, float maxd,
+                          int32_t *edges, int32_t *labels, int32_t *sizes) {
+    /* candidate lists, ascending partner (linkLengths + compact) */
+    int *cnt = (int *)calloc((size_t)n, sizeof(int));
+    int *lst = (int *)malloc(sizeof(int) * (size_t)n * (size_t)n);
+    float *len = (float *)malloc(sizeof(float) * (size_t)n * (size_t)n);
+    int *partner = (int *)malloc(sizeof(int) * 2 * (size_t)n);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int a = 0; a < n; a++) {
+        int c = 0;
+        for (int b = 0; b < n; b++) {
+            const float d = orc_vdist(v, a, b);
+            if (d < maxd && d > 0.0f) {
+                lst[(size_t)a * n + c] = b;
+                len[(size_t)a * n + c] = d;
+                c++;
+            }
+        }
+        cnt[a] = c;
+    }
+    /* linkCenterpoints */
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int a = 0; a < n; a++) {
+        const float xa[3] = {(float)v[3 * a], (float)v[3 * a + 1], (float)v[3 * a + 2]};
+        float shortest = maxd * 2.0f;
+        int best_b = -1, best_c = -1;
+        for (int i = 0; i < cnt[a]; i++) {
+            const int b = lst[(size_t)a * n + i];
+            const int db = (int)roundf(len[(size_t)a * n + i]);
+            if ((float)db >= shortest) continue;
+            const float ab[3] = {(float)v[3 * b] - xa[0], (float)v[3 * b + 1] - xa[1], (float)v[3 * b + 2] - xa[2]};
+            for (int j = 0; j < i; j++) {
+                const int c = lst[(size_t)a * n + j];
+                if (c == b) continue;
+                const int dc = (int)roundf(len[(size_t)a * n + j]);
+                if (!((float)(db + dc) < shortest)) continue;
+                const float ac[3] = {(float)v[3 * c] - xa[0], (float)v[3 * c + 1] - xa[1],
+                                     (float)v[3 * c + 2] - xa[2]};
+                const float lb = sqrtf((ab[0] * ab[0] + ab[1] * ab[1]) + ab[2] * ab[2]);
+                const float lc = sqrtf((ac[0] * ac[0] + ac[1] * ac[1]) + ac[2] * ac[2]);
+                const float dot =
+                    ((ab[0] / lb) * (ac[0] / lc) + (ab[1] / lb) * (ac[1] / lc)) + (ab[2] / lb) * (ac[2] / lc);
+                if (dot > -0.41614684f) continue; /* acos(dot) < 2 */
+                if (orc_mean_tdf(T, X, Y, Z, xa, ab, db) < min_avg) continue;
+                if (orc_mean_tdf(T, X, Y, Z, xa, ac, dc) < min_avg) continue;
+                best_b = b;
+                best_c = c;
+                shortest = (float)(db + dc);
+            }
+        }
+        partner[2 * a] = best_b;
+        partner[2 * a + 1] = best_c;
+    }
+    /* removeDuplicateEdges, then the 2-D pyramid order */
+    uint32_t *keys = (uint32_t *)malloc(sizeof(uint32_t) * 2 * (size_t)n);
+    int ne = 0;
+    for (int t = 0; t < 2 * n; t++) {
+        const int a = t >> 1, b = partner[t];
+        if (b < 0) continue;
+        const int back = partner[2 * b] == a || partner[2 * b + 1] == a;
+        if (a <= b || !back) keys[ne++] = orc_hp2d_key((uint32_t)a, (uint32_t)b);
+    }
+    qsort(keys, (size_t)ne, sizeof(uint32_t), orc_cmp_u32);
+    for (int e = 0; e < ne; e++) {
+        uint32_t x = 0, y = 0;
+        for (int bit = 0; bit < 16; bit++) {
+            y |= ((keys[e] >> (2 * bit)) & 1u) << bit;
+            x |= ((keys[e] >> (2 * bit + 1)) & 1u) << bit;
+        }
+        edges[2 * e] = (int32_t)x;
+        edges[2 * e + 1] = (int32_t)y;
+    }
+    /* components labelled by their smallest vertex; sizes */
+    int *parent = (int *)malloc(sizeof(int) * (size_t)n);
+    for (int i = 0; i < n; i++) parent[i] = i;
+    for (int e = 0; e < ne; e++) {
+        const int ra = orc_find(parent, edges[2 * e]), rb = orc_find(parent, edges[2 * e + 1]);
+        if (ra < rb) parent[rb] = ra;
+        else if (rb < ra) parent[ra] = rb;
+    }
+    for (int i = 0; i < n; i++) {
+        labels[i] = orc_find(parent, i);
+        sizes[i] = 0;
+    }
+    for (int i = 0; i < n; i++) sizes[labels[i]]++;
+    free(cnt); free(lst); free(len); free(partner); free(keys); free(parent);
+    return ne;
+}
+
+void orc_rasterize_trees(const int32_t *v, const int32_t *edges, int ne, const int32_t *labels,
+                         const int32_t *sizes, int min_tree, int8_t *out, int X, int Y, int Z) {
+    for (int e = 0; e < ne; e++) {
+        const int a = edges[2 * e], b = edges[2 * e + 1];
+        if (sizes[labels[a]] < min_tree) continue;
+        const float xa[3] = {(float)v[3 * a], (float)v[3 * a + 1], (float)v[3 * a + 2]};
+        const float d[3] = {(float)v[3 * b] - xa[0], (float)v[3 * b + 1] - xa[1], (float)v[3 * b + 2] - xa[2]};
+        const int l = (int)roundf(sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]));
+        for (int i = 0; i < l; i++) {
+            const float alpha = (float)i / (float)l;
+            const int x = (int)roundf(xa[0] + d[0] * alpha), y = (int)roundf(xa[1] + d[1] * alpha),
+                      z = (int)roundf(xa[2] + d[2] * alpha);
+            if (x >= 0 && y >= 0 && z >= 0 && x < X && y < Y && z < Z)
+                out[(int64_t)x + (int64_t)X * ((int64_t)y + (int64_t)Y * z)] = 1;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Precision-templated kernels                                               */
 /* ------------------------------------------------------------------------ */
 

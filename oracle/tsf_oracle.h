@@ -95,6 +95,17 @@ void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask);
 
 /* Threads used by the OpenMP loops (0 = library default). */
 void orc_set_threads(int n);
+
+/* centerline linking (parallelCenterlineExtraction.cpp:911-1332,
+ * kernels.cl:327-559): returns the edge count; edges (capacity 2n pairs) in
+ * the 2-D pyramid order, labels = smallest vertex index of the component,
+ * sizes indexed by label. */
+int orc_link_centerpoints(const int32_t *v, int n, const float *T, int X, int Y, int Z, float min_avg, float maxd,
+                          int32_t *edges, int32_t *labels, int32_t *sizes);
+/* removeSmallTrees (kernels.cl:510-534): rasterise edges of trees of at least
+ * min_tree vertices into out (X*Y*Z int8, not cleared) */
+void orc_rasterize_trees(const int32_t *v, const int32_t *edges, int ne, const int32_t *labels,
+                         const int32_t *sizes, int min_tree, int8_t *out, int X, int Y, int Z);
 int orc_get_threads(void);
 
 #ifdef __cplusplus

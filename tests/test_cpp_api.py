@@ -55,9 +55,24 @@ def _oracle_run(oracle, vol_u8, iters):
     return oracle.from_unorm16(T16), R, field
 
 
+def _read_vtk(path):
+    lines = open(path).read().split("\n")
+    npts = int(lines[4].split()[1])
+    pts = np.array([list(map(int, l.split())) for l in lines[5:5 + npts]], np.int32).reshape(-1, 3)
+    k = lines.index("", 5 + npts)
+    nl = int(lines[k + 1].split()[1])
+    edges = np.array([list(map(int, l.split()))[1:] for l in lines[k + 2:k + 2 + nl]], np.int32).reshape(-1, 2)
+    return pts, edges
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "vertices"])
+@pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "no-loop-removal", "default"])
 def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
+    """run() of the Synthetic-Vascusynth preset on an .mhd volume: the TDF,
+    the centerpoints and vertices bit for bit against the oracle; without loop
+    removal the linked and rasterised trees bit for bit; by default (loop
+    removal, here with a VTK file) a loop-free graph whose rasterisation is
+    the centerline volume."""
     pytest.importorskip("torch")
     vol = synth.vascular_tree((44, 52, 60), seed=11)
     vol_u8 = np.round(vol * 90.0).astype(np.uint8)          # some voxels above the preset maximum 75
@@ -66,8 +81,13 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     iters = 21                                              # odd: the reference runs 20
     args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
             "--centerline-method", "gpu", "--gvf-iterations", str(iters)]
-    if mode != "vertices":
+    vtk = str(tmp_path / "centerline.vtk")
+    if mode in ("tdf-only", "centerpoints-only"):
         args += ["--" + mode]
+    elif mode == "no-loop-removal":
+        args += ["--loop-removal", "false"]
+    else:
+        args += ["--centerline-vtk-file", vtk]
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     X, Y, Z = map(int, open(tmp_path / "size.txt").read().split())
@@ -81,7 +101,33 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     cl = np.fromfile(tmp_path / "centerline.raw", np.int8).reshape(Z, Y, X)
     if mode == "centerpoints-only":
         assert np.array_equal(cl, ref["mask2"])
-    else:
-        got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
-        assert np.array_equal(got, ref["vertices"])
-        assert cl.sum() == len(ref["vertices"])
+        return
+    got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
+    assert np.array_equal(got, ref["vertices"])
+    # linking, Synthetic-Vascusynth: min-mean-tdf 0.3, max-distance 10, min-tree-length 3
+    edges, labels, sizes = oracle.link_centerpoints(ref["vertices"], T, 0.3, 10.0)
+    if mode == "no-loop-removal":
+        assert np.array_equal(cl, oracle.rasterize_trees(ref["vertices"], edges, labels, sizes, 3, T.shape))
+        return
+    pts, ve = _read_vtk(vtk)
+    assert len(ve) > 0
+    n_comp = len({tuple(r) for r in _roots(len(pts), ve)})
+    assert len(ve) == len(pts) - n_comp                    # a forest
+    import test_centerline_graph as G
+    ref_cl, _ = G._raster(pts, ve, np.zeros(T.shape, np.float32))
+    assert np.array_equal(cl, ref_cl)
+
+
+def _roots(n, e):
+    parent = list(range(n))
+
+    def find(i):
+        while parent[i] != i:
+            i = parent[i]
+        return i
+
+    for a, b in e:
+        ra, rb = find(a), find(b)
+        if ra != rb:
+            parent[ra] = rb
+    return [(find(i),) for i in range(n)]

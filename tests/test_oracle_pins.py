@@ -170,3 +170,73 @@ def test_fmg_reduces_residual(oracle, synth):
         return np.abs(r[:, 2:-2, 2:-2, 2:-2]).mean()
 
     assert res(b) < res(a)
+
+
+def _hp2d_traverse(img):
+    """The reference's 2-D histogram pyramid (constructHPLevel2D,
+    scanHPLevel2D, traverseHP2D: kernels.cl:100-142, 229-275) simulated
+    directly: returns the (x, y) of every set pixel of img[y, x], in the
+    order the traversal enumerates them."""
+    S = 2
+    while S < max(img.shape):
+        S *= 2
+    base = np.zeros((S, S), np.int64)
+    base[:img.shape[0], :img.shape[1]] = img
+    levels = [base]
+    while levels[-1].shape[0] > 2:
+        l = levels[-1]
+        levels.append(l[0::2, 0::2] + l[0::2, 1::2] + l[1::2, 0::2] + l[1::2, 1::2])
+
+    def rd(l, x, y):
+        return int(l[y, x]) if 0 <= x < l.shape[1] and 0 <= y < l.shape[0] else 0
+
+    offsets = [(0, 0), (0, 1), (1, 0), (1, 1)]
+    out = []
+    for t in range(int(base.sum())):
+        x = y = acc0 = 0
+        for l in reversed(levels):
+            n0, n1, n2 = rd(l, x, y), rd(l, x, y + 1), rd(l, x + 1, y)
+            acc = acc0 + n0
+            c0 = acc <= t
+            acc += n1
+            c1 = acc <= t
+            acc += n2
+            c2 = acc <= t
+            dx, dy = offsets[c0 + c1 + c2]
+            x, y = 2 * (x + dx), 2 * (y + dy)
+            acc0 += c0 * n0 + c1 * n1 + c2 * n2
+        out.append((x // 2, y // 2))
+    return out
+
+
+@pytest.mark.parametrize("shape", [(8, 8), (13, 21), (40, 33)])
+def test_pyramid_2d_order_is_key_sort(shape):
+    """The edge list order of the linking stage: a sort by the key that
+    interleaves the bits of (x, y) with y as the low bit."""
+    rng = np.random.default_rng(5)
+    img = (rng.random(shape) < 0.15).astype(np.int64)
+    ys, xs = np.nonzero(img)
+    key = np.zeros(xs.shape, np.int64)
+    for b in range(8):
+        key |= (((ys >> b) & 1) | (((xs >> b) & 1) << 1)).astype(np.int64) << (2 * b)
+    o = np.argsort(key, kind="stable")
+    assert _hp2d_traverse(img) == list(zip(xs[o].tolist(), ys[o].tolist()))
+
+
+def test_link_chain_known_answer(oracle):
+    """Vertices on a line 3 voxels apart inside a bright tube: every inner
+    vertex links to both neighbours (angle pi >= 2 rad), one tree.  The end
+    vertices have one candidate within the distance and link nothing
+    themselves; the tuple (1, 0) is kept as is (no (0, 1)).  Rasterisation
+    runs from an edge's first vertex and stops before the second, so x = 2
+    (vertex 0, only ever a second vertex) stays unset."""
+    T = np.zeros((12, 12, 40), np.float32)
+    T[4:8, 4:8, :] = 1.0
+    v = np.array([[2 + 3 * i, 6, 6] for i in range(12)], np.int32)
+    edges, labels, sizes = oracle.link_centerpoints(v, T, 0.5, 5.0)
+    pairs = {tuple(sorted(e)) for e in edges.tolist()}
+    assert pairs == {(i, i + 1) for i in range(11)}
+    assert edges.tolist()[0] == [1, 0]
+    assert (labels == 0).all() and sizes[0] == 12
+    cl = oracle.rasterize_trees(v, edges, labels, sizes, 5, T.shape)
+    assert cl[6, 6, 3:35].all() and cl.sum() == 32

@@ -9,7 +9,10 @@
 //  runCircleFittingMethod  (:212-939): small-radius TDF on the un-diffused
 //      field when radius-min < 2.5, GVF (Jacobi or FMG) of the large-blur
 //      field, large-radius TDF, combine;
-//  runNewCenterlineAlg front half (parallelCenterlineExtraction.cpp:667-899).
+//  runNewCenterlineAlg (parallelCenterlineExtraction.cpp:667-1332): candidate
+//      centerpoints and vertices, linking into trees (GPU), then either the
+//      host loop removal and rasterisation (loop-removal or a VTK file) or
+//      the GPU rasterisation of the large trees.
 // The reference's GVF loop returns the result of iterations - 1 when the
 // iteration count is odd (gradientVectorFlow.cpp:1137-1172); run() does the
 // same.  Options outside this library's scope (other centerline methods, the
@@ -347,16 +350,71 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
                                    stream.s), "vertices");
         check_cuda(cudaStreamSynchronize(stream.s), "vertices");
         std::vector<SIPL::int3> vlist((size_t)nv);
-        char *mask = new char[n]();
-        for (int64_t i = 0; i < nv; i++) {
-            vlist[(size_t)i] = SIPL::int3(hv3[3 * i], hv3[3 * i + 1], hv3[3 * i + 2]);
-            mask[(size_t)hv3[3 * i] + (size_t)X * ((size_t)hv3[3 * i + 1] + (size_t)Y * hv3[3 * i + 2])] = 1;
-        }
+        for (int64_t i = 0; i < nv; i++) vlist[(size_t)i] = SIPL::int3(hv3[3 * i], hv3[3 * i + 1], hv3[3 * i + 2]);
         output->setCenterpoints(vlist);
-        output->setCenterlineVoxels(mask);
-        std::cout << "NOTE: centerline linking and segmentation are not part of this library; the centerline "
-                     "voxels mark the detected centerpoints"
-                  << std::endl;
+
+        // runNewCenterlineAlg, back half (parallelCenterlineExtraction.cpp:911-1332)
+        const int nvi = (int)nv;
+        const size_t lwb = tsf_link_workspace_size(nvi);
+        DevBuf lws(lwb), dedges(sizeof(int32_t) * 4 * (size_t)nvi), dlabels(sizeof(int32_t) * (size_t)nvi),
+            dsizes(sizeof(int32_t) * (size_t)nvi);
+        int ne = 0;
+        const int lcode = tsf_link_centerpoints(verts.as<int32_t>(), nvi, d_T, tdf16, X, Y, Z,
+                                                getParam(parameters, "min-mean-tdf"),
+                                                getParam(parameters, "max-distance"), dedges.as<int32_t>(), &ne,
+                                                dlabels.as<int32_t>(), dsizes.as<int32_t>(), lws.p, lwb, S);
+        std::cout << "number of edges detected " << ne << std::endl;
+        if (lcode == TSF_ERR_COUNT_RANGE) throw SIPL::SIPLException("No edges were found", __LINE__, __FILE__);
+        check(lcode, "linking");
+        const int min_tree = (int)getParam(parameters, "min-tree-length");
+        const std::string vtk = getParamStr(parameters, "centerline-vtk-file");
+        if (vtk != "off" || getParamBool(parameters, "loop-removal")) {
+            // host loop removal and rasterisation (parallelCenterlineExtraction.cpp:1168-1247)
+            std::vector<int32_t> he(2 * (size_t)ne), hl((size_t)nvi), hs((size_t)nvi);
+            std::vector<float> radius(n);
+            check_cuda(cudaMemcpyAsync(he.data(), dedges.p, he.size() * 4, cudaMemcpyDeviceToHost, stream.s), "edges");
+            check_cuda(cudaMemcpyAsync(hl.data(), dlabels.p, hl.size() * 4, cudaMemcpyDeviceToHost, stream.s), "labels");
+            check_cuda(cudaMemcpyAsync(hs.data(), dsizes.p, hs.size() * 4, cudaMemcpyDeviceToHost, stream.s), "sizes");
+            check_cuda(cudaMemcpyAsync(radius.data(), fr.R.p, n * 4, cudaMemcpyDeviceToHost, stream.s), "radius");
+            check_cuda(cudaStreamSynchronize(stream.s), "graph download");
+            const int split = vtk != "off" ? (int)getParam(parameters, "max-edge-distance") : 0;
+            char *centerlines = new char[n]();
+            int cap = 4 * (nvi + ne) + 1024, nov = 0, noe = 0, gcode;
+            std::vector<int32_t> ov, oe;
+            for (;;) {
+                ov.assign(3 * (size_t)cap, 0);
+                oe.assign(2 * (size_t)cap, 0);
+                std::memset(centerlines, 0, n);
+                std::vector<float> rad = radius;
+                gcode = tsf_centerline_graph(hv3.data(), nvi, he.data(), ne, hl.data(), hs.data(), min_tree, split,
+                                             X, Y, Z, rad.data(), reinterpret_cast<int8_t *>(centerlines), ov.data(),
+                                             oe.data(), cap, &nov, &noe);
+                if (gcode != TSF_ERR_CAPACITY) break;
+                cap = 2 * std::max(nov, noe);
+            }
+            if (gcode == TSF_ERR_COUNT_RANGE) {
+                delete[] centerlines;
+                throw SIPL::SIPLException("Centerline graph size is 0! Can't continue. Maybe lower min-tree-length?",
+                                          __LINE__, __FILE__);
+            }
+            if (gcode != TSF_OK) {
+                delete[] centerlines;
+                check(gcode, "centerline graph");
+            }
+            output->setCenterlineVoxels(centerlines);
+            if (vtk != "off" && tsf_write_centerline_vtk(vtk.c_str(), ov.data(), nov, oe.data(), noe) != TSF_OK)
+                throw SIPL::IOException(vtk.c_str(), __LINE__, __FILE__);
+        } else {
+            // removeSmallTrees on the GPU (kernels.cl:510-534)
+            DevBuf cl(n);
+            check_cuda(cudaMemsetAsync(cl.p, 0, n, stream.s), "centerlines");
+            check(tsf_rasterize_trees(verts.as<int32_t>(), dedges.as<int32_t>(), ne, dlabels.as<int32_t>(),
+                                      dsizes.as<int32_t>(), min_tree, cl.as<int8_t>(), X, Y, Z, S),
+                  "rasterise trees");
+            check_cuda(cudaStreamSynchronize(stream.s), "centerlines");
+            output->setDeviceCenterlineVoxels(static_cast<int8_t *>(cl.release()));
+        }
+        std::cout << "NOTE: segmentation is not part of this library" << std::endl;
         if (getParamStr(parameters, "storage-dir") != "off")
             writeDataToDisk(output, getParamStr(parameters, "storage-dir"), getParamStr(parameters, "storage-name"));
         return output;

@@ -70,6 +70,12 @@ def _declare(L):
         "tsf_gvf": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
         "tsf_gvf_mode": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _i, _p]),
         "tsf_gvf_device_error": (_i, [_i]),
+        "tsf_link_workspace_size": (_sz, [_i]),
+        "tsf_link_centerpoints": (_i, [_p, _i, _p, _i, _i, _i, _i, _f, _f, _p, _p, _p, _p, _p, _sz, _p]),
+        "tsf_rasterize_trees": (_i, [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i, _p]),
+        "tsf_remove_loops": (_i, [_p, _i, _p, _i, _i, _i, _i, _p, _p, _i, _p, _p]),
+        "tsf_centerline_graph": (_i, [_p, _i, _p, _i, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p, _p]),
+        "tsf_write_centerline_vtk": (_i, [C.c_char_p, _p, _i, _p, _i]),
         "tsf_gvf_adjoint_checkpoint_interval": (_i, [_i, _i, _i, _i, _i, _sz]),
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
@@ -299,6 +305,83 @@ def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = 
     _check(load().tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
                                       float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
     return T, R
+
+
+def link_centerpoints(vertices, T, min_mean_tdf: float, max_distance: float, unorm16: bool = False, stream=None):
+    """vertices: (n, 3) int32 CUDA tensor (x, y, z); T: the TDF (float32, or
+    int16-typed unorm16 bits).  Returns (edges (m, 2) int32 in the 2-D pyramid
+    order, labels (n,), tree sizes (n,))."""
+    torch = _torch()
+    L = load()
+    n = vertices.shape[0]
+    Z, Y, X = T.shape
+    edges = torch.zeros((2 * n, 2), dtype=torch.int32, device=T.device)
+    labels = torch.empty(n, dtype=torch.int32, device=T.device)
+    sizes = torch.empty(n, dtype=torch.int32, device=T.device)
+    ws = workspace(L.tsf_link_workspace_size(n))
+    ne = C.c_int(0)
+    _check(L.tsf_link_centerpoints(_ptr(vertices), n, _ptr(T), int(unorm16), X, Y, Z, float(min_mean_tdf),
+                                   float(max_distance), _ptr(edges), C.byref(ne), _ptr(labels), _ptr(sizes),
+                                   _ptr(ws), ws.numel(), _stream(stream)))
+    return edges[:ne.value], labels, sizes
+
+
+def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape, stream=None):
+    torch = _torch()
+    Z, Y, X = shape
+    out = torch.zeros(shape, dtype=torch.int8, device=vertices.device)
+    e = edges.contiguous()
+    _check(load().tsf_rasterize_trees(_ptr(vertices), _ptr(e) if e.numel() else None, e.shape[0], _ptr(labels),
+                                      _ptr(sizes), int(min_tree_length), _ptr(out), X, Y, Z, _stream(stream)))
+    return out
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def remove_loops(vertices, edges, shape):
+    """Host removeLoops (parallelCenterlineExtraction.cpp:129-285) on numpy
+    arrays: vertices (n, 3) int (x, y, z), edges (m, 2).  Returns (vertices,
+    edges) of the loop-free graph."""
+    import numpy as np
+    v = np.ascontiguousarray(vertices, dtype=np.int32)
+    e = np.ascontiguousarray(edges, dtype=np.int32)
+    Z, Y, X = shape
+    cap = max(16, 2 * (len(v) + len(e)))
+    ov, oe = np.zeros((cap, 3), np.int32), np.zeros((cap, 2), np.int32)
+    nv, ne = C.c_int(0), C.c_int(0)
+    _check(load().tsf_remove_loops(_np_ptr(v), len(v), _np_ptr(e), len(e), X, Y, Z, _np_ptr(ov), _np_ptr(oe), cap,
+                                   C.byref(nv), C.byref(ne)))
+    return ov[:nv.value].copy(), oe[:ne.value].copy()
+
+
+def centerline_graph(vertices, edges, labels, sizes, min_tree_length, radius, max_edge_distance=0):
+    """Host centerline graph stage (parallelCenterlineExtraction.cpp:1168-1247)
+    on numpy arrays; returns (centerlines int8 volume, radius (updated copy),
+    vertices, edges)."""
+    import numpy as np
+    v = np.ascontiguousarray(vertices, dtype=np.int32)
+    e = np.ascontiguousarray(edges, dtype=np.int32)
+    rad = np.ascontiguousarray(radius, dtype=np.float32).copy()
+    Z, Y, X = rad.shape
+    cl = np.zeros(rad.shape, np.int8)
+    cap = 4 * (len(v) + len(e)) + 1024
+    while True:
+        ov, oe = np.zeros((cap, 3), np.int32), np.zeros((cap, 2), np.int32)
+        nv, ne = C.c_int(0), C.c_int(0)
+        r2 = rad.copy()
+        cl[...] = 0
+        code = load().tsf_centerline_graph(_np_ptr(v), len(v), _np_ptr(e), len(e),
+                                           _np_ptr(np.ascontiguousarray(labels, dtype=np.int32)),
+                                           _np_ptr(np.ascontiguousarray(sizes, dtype=np.int32)), int(min_tree_length),
+                                           int(max_edge_distance), X, Y, Z, _np_ptr(r2), _np_ptr(cl), _np_ptr(ov),
+                                           _np_ptr(oe), cap, C.byref(nv), C.byref(ne))
+        if code != 6:
+            break
+        cap = 2 * max(nv.value, ne.value)
+    _check(code)
+    return cl, r2, ov[:nv.value].copy(), oe[:ne.value].copy()
 
 
 def tdf_combine(Ts, Rs, Tl, Rl, unorm16: bool = False, stream=None):
