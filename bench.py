@@ -403,6 +403,7 @@ def run_tsf(args, rank, world):
         "clocks": clk,
     }
     res["fwd_adjoint"] = fwd_adjoint_timing(torch, pipe, args)
+    res["linking"] = linking_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
@@ -463,6 +464,38 @@ def fwd_adjoint_timing(torch, pipe, args):
             "adjoint_workspace_gb": round(state["gvf_ws"].numel() / 1e9, 2),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
+
+
+def linking_timing(torch, T, pipe, with_cpu):
+    """Centerline linking of the step's vertices (tsf_link_centerpoints +
+    tsf_rasterize_trees; the Synthetic-Vascusynth linking parameters), CUDA
+    events over 5 repetitions after one warm-up, and the oracle on the host."""
+    nv = min(pipe.last["n_vertices"], pipe.max_vertices)
+    if nv < 2:
+        return None
+    v = pipe.verts[:nv].contiguous()
+    shape = pipe.Tl.shape
+    T.link_centerpoints(v, pipe.Tl, 0.3, 10.0)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    a.record()
+    for _ in range(reps):
+        edges, labels, sizes = T.link_centerpoints(v, pipe.Tl, 0.3, 10.0)
+        T.rasterize_trees(v, edges, labels, sizes, 3, shape)
+    b.record()
+    torch.cuda.synchronize()
+    out = {"vertices": nv, "edges": int(edges.shape[0]), "ms": round(a.elapsed_time(b) / reps, 3),
+           "note": "includes the host synchronisation that returns the edge count"}
+    if with_cpu:
+        import oracle as O
+        vh, Th = v.cpu().numpy(), pipe.Tl.cpu().numpy()
+        t0 = time.perf_counter()
+        e, l, s_ = O.link_centerpoints(vh, Th, 0.3, 10.0)
+        O.rasterize_trees(vh, e, l, s_, 3, Th.shape)
+        out["cpu_oracle_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
+        out["cpu_cores"] = O.get_threads()
+    return out
 
 
 def run_adjoint(args):
