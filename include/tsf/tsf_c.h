@@ -292,6 +292,37 @@ int tsf_remove_loops(const int *vertices, int n_vertices, const int *edges, int 
 int tsf_write_centerline_vtk(const char *path, const int *vertices, int n_vertices,
                              const int *edges, int n_edges);
 
+/* ---------------------------------------------------------------------------
+ * Segmentation
+ * ------------------------------------------------------------------------- */
+
+/* Workspace bytes for tsf_segment_inverse_gradient. */
+size_t tsf_segment_workspace_size(int X, int Y, int Z);
+
+/* runInverseGradientSegmentation (segmentation.cpp:5-205; kernels
+ * initGrowing, grow, dilate, erode, kernels_no_3d_write.cl:1100-1207 and
+ * 1370-1412).  d_centerlines: X*Y*Z int8 (1 on the centerline); d_field4: the
+ * vector field the TDF was computed on (vx, vy, vz, |v|) in `storage`;
+ * d_radius: X*Y*Z float.  Grows from the centerline against the field
+ * magnitude until an iteration accepts nothing, then closes the result
+ * (3x3x3 dilation, then erosion) into d_segmentation (X*Y*Z int8, 0 / 1,
+ * every voxel written).  Within one grow iteration the reference's writes race
+ * (a voxel's own verdict against its neighbours' "check it" marks); here the
+ * iteration decides first and applies second, with the precedence accepted >
+ * to check > dropped.  *iterations (may be null) receives the number of grow
+ * iterations, the last of which accepted nothing.  Synchronises `stream`. */
+int tsf_segment_inverse_gradient(const int8_t *d_centerlines, const void *d_field4, int storage,
+                                 const float *d_radius, int X, int Y, int Z, int8_t *d_segmentation,
+                                 int *iterations, void *d_workspace, size_t workspace_bytes,
+                                 void *stream);
+
+/* runSphereSegmentation (segmentation.cpp:207-307; kernel
+ * sphereSegmentation, kernels_no_3d_write.cl:1209-1234): d_segmentation
+ * (X*Y*Z int8, written) is 1 within distance < radius of every voxel with
+ * d_centerlines != 0. */
+int tsf_segment_spheres(const int8_t *d_centerlines, const float *d_radius, int X, int Y, int Z,
+                        int8_t *d_segmentation, void *stream);
+
 /* Reverse-mode derivative of tsf_tdf_circle (no counterpart in the
  * reference): given d_gT = dL/dT (float per voxel), ADDS dL/d(field x,y,z) to
  * d_gfield (planar FP32, 3N) -- through the trilinear samples at the arg-max

@@ -15,10 +15,13 @@
 //
 // Results: the TDF always; with `tdf-only` nothing else.  With
 // `centerpoints-only` the centerline voxels are the filtered candidate mask,
-// exactly the reference's output for that option.  Otherwise the centerline
-// voxels mark the centerpoint vertices and getCenterpoints() lists them; the
-// linking of vertices into centerlines and the segmentation are not part of
-// this library (hasSegmentation() stays false).
+// exactly the reference's output for that option.  Otherwise getCenterpoints()
+// lists the centerpoint vertices, the vertices are linked into trees and the
+// centerline voxels are the rasterised large trees (after loop removal with
+// `loop-removal` or a `centerline-vtk-file`, which is also written).  Unless
+// `no-segmentation` is set, the segmentation follows: inverse-gradient region
+// growing from the centerlines, or spheres of the TDF radius with
+// `sphere-segmentation`.
 //
 // Exceptions follow the reference: SIPL::IOException for a missing file,
 // SIPL::SIPLException for a bad header, an unsupported type or option, or a

@@ -68,6 +68,10 @@ def _declare(L):
     L.orc_link_centerpoints.argtypes = [_p, _i, _p, _i, _i, _i, _f, _f, _p, _p, _p]
     L.orc_rasterize_trees.restype = None
     L.orc_rasterize_trees.argtypes = [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i]
+    L.orc_segment_inverse_gradient.restype = _i
+    L.orc_segment_inverse_gradient.argtypes = [_p, _p, _p, _i, _i, _i, _p]
+    L.orc_segment_spheres.restype = None
+    L.orc_segment_spheres.argtypes = [_p, _p, _i, _i, _i, _p]
     L.orc_threshold_f32.argtypes = [_p, _i64, _f, _p]
     L.orc_set_threads.argtypes = [_i]
     L.orc_get_threads.restype = _i
@@ -324,6 +328,34 @@ def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape)
     lib().orc_rasterize_trees(_ptr(v), _ptr(e), e.shape[0], _ptr(np.ascontiguousarray(labels, dtype=np.int32)),
                               _ptr(np.ascontiguousarray(sizes, dtype=np.int32)), int(min_tree_length), _ptr(out),
                               X, Y, Z)
+    return out
+
+
+def segment_inverse_gradient(centerlines, field4, radius):
+    """runInverseGradientSegmentation (segmentation.cpp:5-205; initGrowing,
+    grow, dilate, erode, kernels_no_3d_write.cl:1100-1207, 1370-1412).
+    centerlines (Z, Y, X) int8; field4 (Z, Y, X, 4) as read (float32, storage
+    already converted); radius (Z, Y, X) float32.  Returns (segmentation int8,
+    grow iterations).  Grow iterations decide first and apply second with the
+    precedence accepted > to check > dropped."""
+    cl = np.ascontiguousarray(centerlines, dtype=np.int8)
+    F = np.ascontiguousarray(field4, dtype=np.float32)
+    R = np.ascontiguousarray(radius, dtype=np.float32)
+    Z, Y, X = cl.shape
+    assert F.shape == (Z, Y, X, 4) and R.shape == cl.shape
+    out = np.zeros(cl.shape, np.int8)
+    it = lib().orc_segment_inverse_gradient(_ptr(cl), _ptr(F), _ptr(R), X, Y, Z, _ptr(out))
+    return out, it
+
+
+def segment_spheres(centerlines, radius):
+    """runSphereSegmentation (segmentation.cpp:207-307; sphereSegmentation,
+    kernels_no_3d_write.cl:1209-1234)."""
+    cl = np.ascontiguousarray(centerlines, dtype=np.int8)
+    R = np.ascontiguousarray(radius, dtype=np.float32)
+    Z, Y, X = cl.shape
+    out = np.zeros(cl.shape, np.int8)
+    lib().orc_segment_spheres(_ptr(cl), _ptr(R), X, Y, Z, _ptr(out))
     return out
 
 

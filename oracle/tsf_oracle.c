@@ -436,6 +436,154 @@ void orc_rasterize_trees(const int32_t *v, const int32_t *edges, int ne, const i
 }
 
 /* ------------------------------------------------------------------------ */
+/* Segmentation (segmentation.cpp:5-307; kernels_no_3d_write.cl:1100-1235,   */
+/* 1370-1412).  Reads clamp to the edge (the reference's sampler), writes    */
+/* outside the volume are dropped (the buffer kernels' bounds checks).       */
+/* ------------------------------------------------------------------------ */
+
+#define SEG_IDX(x, y, z) ((int64_t)(x) + (int64_t)X * ((int64_t)(y) + (int64_t)Y * (int64_t)(z)))
+#define SEG_IN(x, y, z) ((x) >= 0 && (y) >= 0 && (z) >= 0 && (x) < X && (y) < Y && (z) < Z)
+
+/* initGrowing (kernels_no_3d_write.cl:1100-1124) on state = copy of cl */
+static void seg_init_growing(const int8_t *cl, const float *radius, int8_t *state, int X, int Y, int Z) {
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                if (cl[SEG_IDX(x, y, z)] != 1) continue;
+                int N = (int)roundf(radius[SEG_IDX(x, y, z)] / 2.0f);
+                if (N < 1) N = 1;
+                if (N > 4) N = 4;
+                for (int a = -N; a <= N; a++)
+                    for (int b = -N; b <= N; b++)
+                        for (int c = -N; c <= N; c++) {
+                            const int nx = x + a, ny = y + b, nz = z + c;
+                            if (!SEG_IN(nx, ny, nz)) continue;
+                            if (cl[SEG_IDX(nx, ny, nz)] == 0) state[SEG_IDX(nx, ny, nz)] = 2;
+                        }
+            }
+}
+
+/* One grow iteration (kernels_no_3d_write.cl:1128-1207): decide from `cur`,
+ * then apply with the precedence accepted > to check > dropped (the reference
+ * races these writes).  Returns 1 if anything was accepted. */
+static int seg_grow_once(int8_t *cur, int8_t *acc, int8_t *mark, const float *F, int X, int Y, int Z) {
+    int any = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : any)
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                const int64_t i = SEG_IDX(x, y, z);
+                if (cur[i] != 2) continue;
+                const float wX = F[4 * i + 3];
+                int grew = 0;
+                for (int a = -1; a < 2; a++)
+                    for (int b = -1; b < 2; b++)
+                        for (int c = -1; c < 2; c++) {
+                            if (a == 0 && b == 0 && c == 0) continue;
+                            const int yx = x + a, yy = y + b, yz = z + c;
+                            const int64_t j = SEG_IDX(CLAMPI(yx, X), CLAMPI(yy, Y), CLAMPI(yz, Z));
+                            if (cur[j] == 1) continue;
+                            const float w = F[4 * j + 3];
+                            const float fx = F[4 * j] / w, fy = F[4 * j + 1] / w, fz = F[4 * j + 2] / w;
+                            if (!(w > wX)) continue;
+                            /* the neighbour of Y whose direction best matches F(Y) */
+                            float best = -2.0f;
+                            int zx = 0, zy = 0, zz = 0;
+                            for (int a2 = -1; a2 < 2; a2++)
+                                for (int b2 = -1; b2 < 2; b2++)
+                                    for (int c2 = -1; c2 < 2; c2++) {
+                                        if (a2 == 0 && b2 == 0 && c2 == 0) continue;
+                                        const float l = sqrtf((float)(a2 * a2 + b2 * b2 + c2 * c2));
+                                        const float dx = (float)a2 / l, dy = (float)b2 / l, dz = (float)c2 / l;
+                                        const float v = (fx * dx + fy * dy) + fz * dz;
+                                        if (v > best) {
+                                            best = v;
+                                            zx = yx + a2;
+                                            zy = yy + b2;
+                                            zz = yz + c2;
+                                        }
+                                    }
+                            if (zx != x || zy != y || zz != z) continue;
+                            if (!SEG_IN(yx, yy, yz)) continue;  /* accepted only through Y inside */
+#pragma omp atomic write
+                            mark[SEG_IDX(yx, yy, yz)] = 1;
+                            grew = 1;
+                        }
+                if (grew) {
+                    acc[i] = 1;
+                    any = 1;
+                }
+            }
+    const int64_t n = (int64_t)X * Y * Z;
+    for (int64_t i = 0; i < n; i++) {
+        cur[i] = (cur[i] == 1 || acc[i]) ? 1 : (mark[i] ? 2 : 0);
+        acc[i] = 0;
+        mark[i] = 0;
+    }
+    return any;
+}
+
+int orc_segment_inverse_gradient(const int8_t *cl, const float *field4, const float *radius, int X, int Y, int Z,
+                                 int8_t *out) {
+    const int64_t n = (int64_t)X * Y * Z;
+    int8_t *cur = (int8_t *)malloc((size_t)n), *acc = (int8_t *)calloc((size_t)n, 1),
+           *mark = (int8_t *)calloc((size_t)n, 1), *dil = (int8_t *)calloc((size_t)n, 1);
+    memcpy(cur, cl, (size_t)n);
+    seg_init_growing(cl, radius, cur, X, Y, Z);
+    int it = 0;
+    for (;;) {
+        it++;
+        if (!seg_grow_once(cur, acc, mark, field4, X, Y, Z)) break;
+    }
+    /* dilate (kernels_no_3d_write.cl:1370-1389) into a zeroed volume */
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                if (cur[SEG_IDX(x, y, z)] != 1) continue;
+                for (int a = -1; a < 2; a++)
+                    for (int b = -1; b < 2; b++)
+                        for (int c = -1; c < 2; c++)
+                            if (SEG_IN(x + a, y + b, z + c)) dil[SEG_IDX(x + a, y + b, z + c)] = 1;
+            }
+    /* erode (kernels_no_3d_write.cl:1391-1412), clamp-to-edge reads */
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                int keep = dil[SEG_IDX(x, y, z)] == 1;
+                for (int a = -1; a < 2; a++)
+                    for (int b = -1; b < 2; b++)
+                        for (int c = -1; c < 2; c++)
+                            keep = keep && dil[SEG_IDX(CLAMPI(x + a, X), CLAMPI(y + b, Y), CLAMPI(z + c, Z))] == 1;
+                out[SEG_IDX(x, y, z)] = keep ? 1 : 0;
+            }
+    free(cur);
+    free(acc);
+    free(mark);
+    free(dil);
+    return it;
+}
+
+/* sphereSegmentation (kernels_no_3d_write.cl:1209-1234) into a zeroed out */
+void orc_segment_spheres(const int8_t *cl, const float *radius, int X, int Y, int Z, int8_t *out) {
+    memset(out, 0, (size_t)X * Y * Z);
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                if (cl[SEG_IDX(x, y, z)] == 0) continue;
+                const float r = radius[SEG_IDX(x, y, z)];
+                if (!(r > 0.0f)) continue;
+                const int M = X > Y ? (X > Z ? X : Z) : (Y > Z ? Y : Z);
+                const int N = (int)ceilf(r < (float)M ? r : (float)M);
+                for (int a = -N; a <= N; a++)
+                    for (int b = -N; b <= N; b++)
+                        for (int c = -N; c <= N; c++) {
+                            if (!(sqrtf((float)(a * a + b * b + c * c)) < r)) continue;
+                            if (SEG_IN(x + a, y + b, z + c)) out[SEG_IDX(x + a, y + b, z + c)] = 1;
+                        }
+            }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Precision-templated kernels                                               */
 /* ------------------------------------------------------------------------ */
 

@@ -108,6 +108,16 @@ void orc_rasterize_trees(const int32_t *v, const int32_t *edges, int ne, const i
                          const int32_t *sizes, int min_tree, int8_t *out, int X, int Y, int Z);
 int orc_get_threads(void);
 
+/* runInverseGradientSegmentation (segmentation.cpp:5-205): grows from the
+ * centerline (initGrowing, grow; each iteration decides, then applies with the
+ * precedence accepted > to check > dropped), closes (dilate, erode) into out
+ * (X*Y*Z int8, written).  field4 as read (float).  Returns the number of grow
+ * iterations, the last of which accepted nothing. */
+int orc_segment_inverse_gradient(const int8_t *cl, const float *field4, const float *radius, int X, int Y, int Z,
+                                 int8_t *out);
+/* runSphereSegmentation (segmentation.cpp:207-307) into out (written) */
+void orc_segment_spheres(const int8_t *cl, const float *radius, int X, int Y, int Z, int8_t *out);
+
 #ifdef __cplusplus
 }
 #endif

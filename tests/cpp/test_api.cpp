@@ -6,7 +6,8 @@
 //   test_api cpu                 parameter, TSFOutput and I/O tests (no GPU)
 //   test_api run <file.mhd> <out_dir> [--name value ...]
 //                                run() on a volume; writes tdf.raw (float),
-//                                centerline.raw (int8), vertices.txt
+//                                centerline.raw (int8), segmentation.raw
+//                                (int8, when there is one), vertices.txt
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -192,6 +193,11 @@ static int run_mode(int argc, char **argv) {
     if (o->hasCenterlineVoxels()) {
         FILE *f = std::fopen((out + "/centerline.raw").c_str(), "wb");
         std::fwrite(o->getCenterlineVoxels(), 1, n, f);
+        std::fclose(f);
+    }
+    if (o->hasSegmentation()) {
+        FILE *f = std::fopen((out + "/segmentation.raw").c_str(), "wb");
+        std::fwrite(o->getSegmentation(), 1, n, f);
         std::fclose(f);
     }
     std::ofstream vt(out + "/vertices.txt");

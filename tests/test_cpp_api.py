@@ -66,7 +66,8 @@ def _read_vtk(path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "no-loop-removal", "default", "vtk"])
+@pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "no-loop-removal", "default", "vtk",
+                                  "sphere", "no-segmentation"])
 def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     """run() of the Synthetic-Vascusynth preset on an .mhd volume: the TDF,
     the centerpoints and vertices bit for bit against the oracle; without loop
@@ -74,7 +75,9 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     removal) the centerlines of the host graph stage applied to the oracle's
     linked graph; with a VTK file, the file's graph rasterises to the
     centerline volume (split vertices may land on existing positions, which
-    the reference's position-keyed loop removal merges)."""
+    the reference's position-keyed loop removal merges).  The segmentation
+    (inverse gradient, or spheres) of those centerlines bit for bit against
+    the oracle, with the radius averaged along the edges after loop removal."""
     pytest.importorskip("torch")
     vol = synth.vascular_tree((44, 52, 60), seed=11)
     vol_u8 = np.round(vol * 90.0).astype(np.uint8)          # some voxels above the preset maximum 75
@@ -88,6 +91,10 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
         args += ["--" + mode]
     elif mode == "no-loop-removal":
         args += ["--loop-removal", "false"]
+    elif mode == "sphere":
+        args += ["--loop-removal", "false", "--sphere-segmentation", "true"]
+    elif mode == "no-segmentation":
+        args += ["--no-segmentation", "true"]
     elif mode == "vtk":
         args += ["--centerline-vtk-file", vtk]
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
@@ -98,23 +105,36 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     T, R, field = _oracle_run(oracle, vol_u8, iters)
     assert np.array_equal(tdf, T)
     if mode == "tdf-only":
+        assert not (tmp_path / "segmentation.raw").exists()
         return
     ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
     cl = np.fromfile(tmp_path / "centerline.raw", np.int8).reshape(Z, Y, X)
     if mode == "centerpoints-only":
         assert np.array_equal(cl, ref["mask2"])
+        assert not (tmp_path / "segmentation.raw").exists()
         return
+    seg_file = tmp_path / "segmentation.raw"
+    assert seg_file.exists() == (mode != "no-segmentation")
+    seg = np.fromfile(seg_file, np.int8).reshape(Z, Y, X) if seg_file.exists() else None
     got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
     assert np.array_equal(got, ref["vertices"])
     # linking, Synthetic-Vascusynth: min-mean-tdf 0.3, max-distance 10, min-tree-length 3
     edges, labels, sizes = oracle.link_centerpoints(ref["vertices"], T, 0.3, 10.0)
-    if mode == "no-loop-removal":
+    if mode in ("no-loop-removal", "sphere"):
         assert np.array_equal(cl, oracle.rasterize_trees(ref["vertices"], edges, labels, sizes, 3, T.shape))
+        if mode == "sphere":
+            assert np.array_equal(seg, oracle.segment_spheres(cl, R))
+        else:
+            ref_seg, _ = oracle.segment_inverse_gradient(cl, field, R)
+            assert ref_seg.sum() > cl.sum()
+            assert np.array_equal(seg, ref_seg)
         return
     import tsf_gb300 as tsf
-    if mode == "default":
-        ref_cl, _, _, _ = tsf.centerline_graph(ref["vertices"], edges, labels, sizes, 3, R)
+    if mode in ("default", "no-segmentation"):
+        ref_cl, rad, _, _ = tsf.centerline_graph(ref["vertices"], edges, labels, sizes, 3, R)
         assert np.array_equal(cl, ref_cl)
+        if mode == "default":
+            assert np.array_equal(seg, oracle.segment_inverse_gradient(ref_cl, field, rad)[0])
         return
     pts, ve = _read_vtk(vtk)
     assert len(ve) > 0

@@ -12,7 +12,10 @@
 //  runNewCenterlineAlg (parallelCenterlineExtraction.cpp:667-1332): candidate
 //      centerpoints and vertices, linking into trees (GPU), then either the
 //      host loop removal and rasterisation (loop-removal or a VTK file) or
-//      the GPU rasterisation of the large trees.
+//      the GPU rasterisation of the large trees;
+//  runInverseGradientSegmentation / runSphereSegmentation (segmentation.cpp):
+//      unless no-segmentation, on the centerlines, the GVF field and the
+//      radius (averaged along the edges after host loop removal).
 // The reference's GVF loop returns the result of iterations - 1 when the
 // iteration count is odd (gradientVectorFlow.cpp:1137-1172); run() does the
 // same.  Options outside this library's scope (other centerline methods, the
@@ -368,6 +371,9 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         check(lcode, "linking");
         const int min_tree = (int)getParam(parameters, "min-tree-length");
         const std::string vtk = getParamStr(parameters, "centerline-vtk-file");
+        const bool segment = !getParamBool(parameters, "no-segmentation");
+        const int8_t *d_cl = nullptr;   // the centerlines on the device, for the segmentation
+        DevBuf dcl;
         if (vtk != "off" || getParamBool(parameters, "loop-removal")) {
             // host loop removal and rasterisation (parallelCenterlineExtraction.cpp:1168-1247)
             std::vector<int32_t> he(2 * (size_t)ne), hl((size_t)nvi), hs((size_t)nvi);
@@ -381,11 +387,12 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
             char *centerlines = new char[n]();
             int cap = 4 * (nvi + ne) + 1024, nov = 0, noe = 0, gcode;
             std::vector<int32_t> ov, oe;
+            std::vector<float> rad;
             for (;;) {
                 ov.assign(3 * (size_t)cap, 0);
                 oe.assign(2 * (size_t)cap, 0);
                 std::memset(centerlines, 0, n);
-                std::vector<float> rad = radius;
+                rad = radius;
                 gcode = tsf_centerline_graph(hv3.data(), nvi, he.data(), ne, hl.data(), hs.data(), min_tree, split,
                                              X, Y, Z, rad.data(), reinterpret_cast<int8_t *>(centerlines), ov.data(),
                                              oe.data(), cap, &nov, &noe);
@@ -402,6 +409,14 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
                 check(gcode, "centerline graph");
             }
             output->setCenterlineVoxels(centerlines);
+            if (segment) {
+                // the reference writes the centerlines and the averaged radius back to its images
+                // (parallelCenterlineExtraction.cpp:1235-1249)
+                dcl.alloc(n);
+                check_cuda(cudaMemcpyAsync(dcl.p, centerlines, n, cudaMemcpyHostToDevice, stream.s), "centerlines");
+                check_cuda(cudaMemcpyAsync(fr.R.p, rad.data(), n * 4, cudaMemcpyHostToDevice, stream.s), "radius");
+                d_cl = dcl.as<int8_t>();
+            }
             if (vtk != "off" && tsf_write_centerline_vtk(vtk.c_str(), ov.data(), nov, oe.data(), noe) != TSF_OK)
                 throw SIPL::IOException(vtk.c_str(), __LINE__, __FILE__);
         } else {
@@ -412,9 +427,26 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
                                       dsizes.as<int32_t>(), min_tree, cl.as<int8_t>(), X, Y, Z, S),
                   "rasterise trees");
             check_cuda(cudaStreamSynchronize(stream.s), "centerlines");
+            d_cl = cl.as<int8_t>();        // owned by the output from here on
             output->setDeviceCenterlineVoxels(static_cast<int8_t *>(cl.release()));
         }
-        std::cout << "NOTE: segmentation is not part of this library" << std::endl;
+        // runInverseGradientSegmentation / runSphereSegmentation (tube-segmentation.cpp:967-976)
+        if (segment) {
+            DevBuf seg(n);
+            if (!getParamBool(parameters, "sphere-segmentation")) {
+                const size_t swb = tsf_segment_workspace_size(X, Y, Z);
+                DevBuf sws(swb);
+                int iters = 0;
+                check(tsf_segment_inverse_gradient(d_cl, fr.field.p, st, fr.R.as<float>(), X, Y, Z,
+                                                   seg.as<int8_t>(), &iters, sws.p, swb, S),
+                      "segmentation");
+                std::cout << "segmentation result grown in " << iters << " iterations" << std::endl;
+            } else {
+                check(tsf_segment_spheres(d_cl, fr.R.as<float>(), X, Y, Z, seg.as<int8_t>(), S), "segmentation");
+            }
+            check_cuda(cudaStreamSynchronize(stream.s), "segmentation");
+            output->setDeviceSegmentation(static_cast<int8_t *>(seg.release()));
+        }
         if (getParamStr(parameters, "storage-dir") != "off")
             writeDataToDisk(output, getParamStr(parameters, "storage-dir"), getParamStr(parameters, "storage-name"));
         return output;

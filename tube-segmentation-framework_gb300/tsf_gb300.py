@@ -73,6 +73,9 @@ def _declare(L):
         "tsf_link_workspace_size": (_sz, [_i]),
         "tsf_link_centerpoints": (_i, [_p, _i, _p, _i, _i, _i, _i, _f, _f, _p, _p, _p, _p, _p, _sz, _p]),
         "tsf_rasterize_trees": (_i, [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i, _p]),
+        "tsf_segment_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_segment_inverse_gradient": (_i, [_p, _p, _i, _p, _i, _i, _i, _p, _p, _p, _sz, _p]),
+        "tsf_segment_spheres": (_i, [_p, _p, _i, _i, _i, _p, _p]),
         "tsf_remove_loops": (_i, [_p, _i, _p, _i, _i, _i, _i, _p, _p, _i, _p, _p]),
         "tsf_centerline_graph": (_i, [_p, _i, _p, _i, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p, _p]),
         "tsf_write_centerline_vtk": (_i, [C.c_char_p, _p, _i, _p, _i]),
@@ -333,6 +336,30 @@ def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape,
     e = edges.contiguous()
     _check(load().tsf_rasterize_trees(_ptr(vertices), _ptr(e) if e.numel() else None, e.shape[0], _ptr(labels),
                                       _ptr(sizes), int(min_tree_length), _ptr(out), X, Y, Z, _stream(stream)))
+    return out
+
+
+def segment_inverse_gradient(centerlines, field4, radius, storage: str = "f32", stream=None):
+    """runInverseGradientSegmentation: centerlines (Z, Y, X) int8, field4
+    (Z, Y, X, 4) in `storage`'s dtype, radius (Z, Y, X) float32, all CUDA.
+    Returns (segmentation int8, grow iterations)."""
+    torch = _torch()
+    L = load()
+    Z, Y, X = centerlines.shape
+    out = torch.empty((Z, Y, X), dtype=torch.int8, device=centerlines.device)
+    ws = workspace(L.tsf_segment_workspace_size(X, Y, Z))
+    it = C.c_int(0)
+    _check(L.tsf_segment_inverse_gradient(_ptr(centerlines), _ptr(field4), STORAGE[storage], _ptr(radius), X, Y, Z,
+                                          _ptr(out), C.byref(it), _ptr(ws), ws.numel(), _stream(stream)))
+    return out, it.value
+
+
+def segment_spheres(centerlines, radius, stream=None):
+    """runSphereSegmentation: 1 within distance < radius of every centerline voxel."""
+    torch = _torch()
+    Z, Y, X = centerlines.shape
+    out = torch.empty((Z, Y, X), dtype=torch.int8, device=centerlines.device)
+    _check(load().tsf_segment_spheres(_ptr(centerlines), _ptr(radius), X, Y, Z, _ptr(out), _stream(stream)))
     return out
 
 
