@@ -404,6 +404,8 @@ def run_tsf(args, rank, world):
     }
     res["fwd_adjoint"] = fwd_adjoint_timing(torch, pipe, args)
     res["linking"] = linking_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
+    res["segmentation"] = segmentation_timing(torch, T, pipe,
+                                              rank == 0 and world == 1 and not args.no_cpu_baseline)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
@@ -495,6 +497,56 @@ def linking_timing(torch, T, pipe, with_cpu):
         O.rasterize_trees(vh, e, l, s_, 3, Th.shape)
         out["cpu_oracle_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
         out["cpu_cores"] = O.get_threads()
+    return out
+
+
+def segmentation_timing(torch, T, pipe, with_cpu):
+    """Segmentation of the step's linked centerlines (trees of at least 3
+    vertices, the Synthetic-Vascusynth parameters) on the step's GVF field and
+    radius: inverse-gradient growing (tsf_segment_inverse_gradient, which
+    synchronises once per batch of grow iterations) and spheres
+    (tsf_segment_spheres), CUDA events over 5 repetitions after one warm-up,
+    and the oracle's inverse-gradient growing on the host."""
+    nv = min(pipe.last["n_vertices"], pipe.max_vertices)
+    if nv < 2:
+        return None
+    v = pipe.verts[:nv].contiguous()
+    shape = pipe.Tl.shape
+    edges, labels, sizes = T.link_centerpoints(v, pipe.Tl, 0.3, 10.0)
+    cl = T.rasterize_trees(v, edges, labels, sizes, 3, shape)
+    R = pipe.Rl
+    seg, iters = T.segment_inverse_gradient(cl, pipe.field, R, storage=pipe.storage)
+    T.segment_spheres(cl, R)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    a.record()
+    for _ in range(reps):
+        T.segment_inverse_gradient(cl, pipe.field, R, storage=pipe.storage)
+    b.record()
+    torch.cuda.synchronize()
+    ig_ms = a.elapsed_time(b) / reps
+    a.record()
+    for _ in range(reps):
+        sph = T.segment_spheres(cl, R)
+    b.record()
+    torch.cuda.synchronize()
+    out = {"centerline_voxels": int(cl.sum()), "grow_iterations": iters,
+           "segmented_voxels": int(seg.to(torch.int32).sum()), "inverse_gradient_ms": round(ig_ms, 3),
+           "sphere_voxels": int(sph.to(torch.int32).sum()),
+           "sphere_ms": round(a.elapsed_time(b) / reps, 3)}
+    if with_cpu:
+        import oracle as O
+        F = pipe.field
+        if pipe.storage == "snorm16":       # max(-1, s / 32767), divided on the host
+            Fh = np.maximum(np.float32(-1.0), F.cpu().numpy().astype(np.float32) / np.float32(32767.0))
+        else:
+            Fh = F.float().cpu().numpy()
+        t0 = time.perf_counter()
+        ref, rit = O.segment_inverse_gradient(cl.cpu().numpy(), Fh, R.cpu().numpy())
+        out["cpu_oracle_inverse_gradient_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
+        out["cpu_cores"] = O.get_threads()
+        out["matches_oracle"] = bool(rit == iters and (ref == seg.cpu().numpy()).all())
     return out
 
 
