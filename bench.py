@@ -773,7 +773,36 @@ def run_fmg_workload(args):
     total = evs[0].elapsed_time(evs[-1])
     return {"workload": "lung-airway CT 512x512x400, FMG GVF %d cycles x 3 components, FP16 storage" % args.fmg_cycles,
             "ms_per_volume": round(total, 3), "volumes_per_s": round(1000.0 / total, 3), "stages_ms": stages,
-            "kernel_launches": int(launches), "n_candidates": nc, "n_vertices": nv}
+            "kernel_launches": int(launches), "n_candidates": nc, "n_vertices": nv,
+            "lung_cropping": crop_timing(torch, T, hu, not args.no_cpu_baseline)}
+
+
+def crop_timing(torch, T, hu, with_cpu):
+    """The lung cropping scan lines (cropDatasetLung over the three slice
+    directions) on the raw int16 HU volume: CUDA events over 5 repetitions
+    after one warm-up; the kernels read the volume twice (the z-columns serve
+    the x and the y slices, the x-rows the z slices)."""
+    d = torch.from_numpy(hu).cuda()
+    T.crop_scan_lines(d, 1)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    a.record()
+    for _ in range(reps):
+        cx, cy, cz = T.crop_scan_lines(d, 1)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    out = {"ms": round(ms, 3), "bytes_read": 2 * hu.nbytes, "GBs": round(2 * hu.nbytes / ms / 1e6, 1),
+           "max_counts": [int(c.max()) for c in (cx, cy, cz)]}
+    if with_cpu:
+        import oracle as O
+        t0 = time.perf_counter()
+        ref = O.crop_scan_lines(hu, 1)
+        out["cpu_oracle_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
+        out["cpu_cores"] = 1
+        out["matches_oracle"] = all(np.array_equal(g.cpu().numpy(), r) for g, r in zip((cx, cy, cz), ref))
+    return out
 
 
 def main():

@@ -293,6 +293,42 @@ int tsf_write_centerline_vtk(const char *path, const int *vertices, int n_vertic
                              const int *edges, int n_edges);
 
 /* ---------------------------------------------------------------------------
+ * Cropping (the input stage)
+ * ------------------------------------------------------------------------- */
+
+/* Workspace bytes for tsf_crop_scan_lines. */
+size_t tsf_crop_workspace_size(int X, int Y, int Z);
+
+/* cropDatasetThreshold (method 0) / cropDatasetLung (method 1),
+ * kernels.cl:813-946, enqueued for the three slice directions at
+ * tube-segmentation.cpp:1577-1604: d_volume is the raw volume of TSF_TYPE_*
+ * `type` (before toFloat); d_counts (X + Y + Z int16: slices along x, then y,
+ * then z) receives, per slice, the number of scan lines that are inside --
+ * with a voxel above `threshold` (method 0), or whose HU run-length state
+ * machine (limit -150, +1024 for unsigned data; runs of 30) finds two white
+ * areas and one black or more than one of each (method 1; integer data only). */
+int tsf_crop_scan_lines(const void *d_volume, int type, int X, int Y, int Z, int method, float threshold,
+                        int16_t *d_counts, void *d_workspace, size_t workspace_bytes, void *stream);
+
+/* Host (no device memory): the crop box from the counts
+ * (tube-segmentation.cpp:1611-1719).  box receives x1, y1, z1 and the cropped
+ * extents SX, SY, SZ (multiples of 4 where the volume allows, as the reference
+ * rounds them).  start_z_middle: the z search of "cropping-start-z middle"
+ * (used by the lung cropping) instead of "end".  TSF_ERR_INVALID_ARG ("Invalid
+ * cropping to new size ...") for an empty box. */
+int tsf_crop_bounds(const int16_t *counts, int X, int Y, int Z, int min_scan_lines, int start_z_middle, int *box);
+
+/* Host: the fixed in-plane crop of the AAA-Vessels-CT preset without cropping
+ * (tube-segmentation.cpp:1747-1772): round(extent * fraction) removed from both
+ * sides of x and y, every extent then shrunk to a multiple of 4.  box as above. */
+int tsf_crop_box_fixed(int X, int Y, int Z, float fraction, int *box);
+
+/* Copies box (x1, y1, z1, SX, SY, SZ) of the raw volume to d_out (SX*SY*SZ
+ * elements of `type`, x fastest) -- the reference's enqueueCopyImage of the
+ * cropped region (tube-segmentation.cpp:1727-1744). */
+int tsf_crop_copy(const void *d_volume, int type, int X, int Y, int Z, const int *box, void *d_out, void *stream);
+
+/* ---------------------------------------------------------------------------
  * Segmentation
  * ------------------------------------------------------------------------- */
 

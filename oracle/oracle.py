@@ -70,6 +70,8 @@ def _declare(L):
     L.orc_rasterize_trees.argtypes = [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i]
     L.orc_segment_inverse_gradient.restype = _i
     L.orc_segment_inverse_gradient.argtypes = [_p, _p, _p, _i, _i, _i, _p]
+    L.orc_crop_scan_lines.restype = None
+    L.orc_crop_scan_lines.argtypes = [_p, _i, _i, _i, _i, _i, _f, _p]
     L.orc_segment_spheres.restype = None
     L.orc_segment_spheres.argtypes = [_p, _p, _i, _i, _i, _p]
     L.orc_threshold_f32.argtypes = [_p, _i64, _f, _p]
@@ -329,6 +331,21 @@ def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape)
                               _ptr(np.ascontiguousarray(sizes, dtype=np.int32)), int(min_tree_length), _ptr(out),
                               X, Y, Z)
     return out
+
+
+RAW_TYPES = {np.dtype(np.uint8): 0, np.dtype(np.int8): 1, np.dtype(np.uint16): 2, np.dtype(np.int16): 3,
+             np.dtype(np.float32): 4}
+
+
+def crop_scan_lines(vol, method: int, threshold: float = 0.0):
+    """cropDatasetThreshold (method 0) / cropDatasetLung (method 1),
+    kernels.cl:813-946, over the three slice directions: (counts_x, counts_y,
+    counts_z) int16 of the raw volume (Z, Y, X) of a MET_* dtype."""
+    v = np.ascontiguousarray(vol)
+    Z, Y, X = v.shape
+    counts = np.zeros(X + Y + Z, np.int16)
+    lib().orc_crop_scan_lines(_ptr(v), RAW_TYPES[v.dtype], X, Y, Z, int(method), float(threshold), _ptr(counts))
+    return counts[:X], counts[X:X + Y], counts[X + Y:]
 
 
 def segment_inverse_gradient(centerlines, field4, radius):

@@ -584,6 +584,66 @@ void orc_segment_spheres(const int8_t *cl, const float *radius, int X, int Y, in
 }
 
 /* ------------------------------------------------------------------------ */
+/* Cropping (cropDatasetThreshold / cropDatasetLung, kernels.cl:813-946),    */
+/* one pass per slice direction as the reference enqueues them               */
+/* (tube-segmentation.cpp:1577-1604).  type: ORC_RAW_*.                       */
+/* ------------------------------------------------------------------------ */
+
+static double crop_value(const void *vol, int type, int64_t i) {
+    switch (type) {
+    case ORC_RAW_U8: return (double)((const uint8_t *)vol)[i];
+    case ORC_RAW_I8: return (double)((const int8_t *)vol)[i];
+    case ORC_RAW_U16: return (double)((const uint16_t *)vol)[i];
+    case ORC_RAW_I16: return (double)((const int16_t *)vol)[i];
+    default: return (double)((const float *)vol)[i];
+    }
+}
+
+void orc_crop_scan_lines(const void *vol, int type, int X, int Y, int Z, int method, float threshold,
+                         int16_t *counts) {
+    const int unsigned_type = type == ORC_RAW_U8 || type == ORC_RAW_U16;
+    const int hu_limit = unsigned_type ? -150 + 1024 : -150;
+    const int ext[3] = {X, Y, Z};
+    int16_t *out[3] = {counts, counts + X, counts + X + Y};
+    for (int dir = 0; dir < 3; dir++) {
+        const int line_n = dir == 1 ? X : Y;      /* scanLineSize */
+        const int elem_n = dir == 2 ? X : Z;      /* scanLineElementSize */
+        for (int slice = 0; slice < ext[dir]; slice++) {
+            int16_t lines = 0;
+            for (int line = 0; line < line_n; line++) {
+                int found = 0, w = 0, b = 0, dw = 0, db = 0;
+                for (int e = 0; e < elem_n; e++) {
+                    int x, y, z;
+                    if (dir == 0) { x = slice; y = line; z = e; }
+                    else if (dir == 1) { x = line; y = slice; z = e; }
+                    else { x = e; y = line; z = slice; }
+                    const int64_t i = (int64_t)x + (int64_t)X * ((int64_t)y + (int64_t)Y * z);
+                    if (method == 0) {
+                        /* integer values convert to float for the comparison */
+                        const float v = type == ORC_RAW_F32 ? ((const float *)vol)[i] : (float)crop_value(vol, type, i);
+                        if (v > threshold) found = 1;
+                    } else {
+                        /* the read value stored into a short */
+                        int hu;
+                        if (type == ORC_RAW_U16) hu = (int16_t)((const uint16_t *)vol)[i];
+                        else hu = (int16_t)(int)crop_value(vol, type, i);
+                        if (hu > hu_limit) {
+                            if (w == 30) { dw++; b = 0; }
+                            w++;
+                        } else {
+                            if (b == 30) { db++; w = 0; }
+                            b++;
+                        }
+                    }
+                }
+                if (method == 0 ? found : ((dw == 2 && db == 1) || (db > 1 && dw > 1))) lines++;
+            }
+            out[dir][slice] = lines;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Precision-templated kernels                                               */
 /* ------------------------------------------------------------------------ */
 

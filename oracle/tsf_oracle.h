@@ -108,6 +108,13 @@ void orc_rasterize_trees(const int32_t *v, const int32_t *edges, int ne, const i
                          const int32_t *sizes, int min_tree, int8_t *out, int X, int Y, int Z);
 int orc_get_threads(void);
 
+/* Raw voxel types (the reference's MET_* element types). */
+enum { ORC_RAW_U8 = 0, ORC_RAW_I8 = 1, ORC_RAW_U16 = 2, ORC_RAW_I16 = 3, ORC_RAW_F32 = 4 };
+/* cropDatasetThreshold (method 0) / cropDatasetLung (method 1), kernels.cl:813-946:
+ * per-slice counts of inside scan lines, X + Y + Z int16 (x slices, y, z). */
+void orc_crop_scan_lines(const void *vol, int type, int X, int Y, int Z, int method, float threshold,
+                         int16_t *counts);
+
 /* runInverseGradientSegmentation (segmentation.cpp:5-205): grows from the
  * centerline (initGrowing, grow; each iteration decides, then applies with the
  * precedence accepted > to check > dropped), closes (dilate, erode) into out

@@ -7,7 +7,8 @@
 //   test_api run <file.mhd> <out_dir> [--name value ...]
 //                                run() on a volume; writes tdf.raw (float),
 //                                centerline.raw (int8), segmentation.raw
-//                                (int8, when there is one), vertices.txt
+//                                (int8, when there is one), vertices.txt,
+//                                size.txt and shift.txt
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -185,6 +186,8 @@ static int run_mode(int argc, char **argv) {
     const SIPL::int3 s = *o->getSize();
     const size_t n = (size_t)s.x * s.y * s.z;
     std::ofstream(out + "/size.txt") << s.x << " " << s.y << " " << s.z << "\n";
+    const SIPL::int3 sh = o->getShiftVector();
+    std::ofstream(out + "/shift.txt") << sh.x << " " << sh.y << " " << sh.z << "\n";
     {
         FILE *f = std::fopen((out + "/tdf.raw").c_str(), "wb");
         std::fwrite(o->getTDF(), sizeof(float), n, f);

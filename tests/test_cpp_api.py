@@ -66,6 +66,36 @@ def _read_vtk(path):
 
 
 @pytest.mark.gpu
+def test_run_threshold_cropping(api_tests, oracle, synth, tmp_path):
+    """run() with threshold cropping (cropping-start-z end): the vessel tree
+    embedded in a dim, larger volume is cropped to the box the oracle's
+    scan-line counts and the reference's host rule give, the shift vector is
+    the box corner, and the TDF of the cropped volume matches the oracle's."""
+    import test_crop
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(1)
+    vol_u8 = (rng.random((60, 70, 84)) * 30).astype(np.uint8)
+    vol_u8[7:51, 11:63, 13:73] = np.round(synth.vascular_tree((44, 52, 60), seed=11) * 90.0).astype(np.uint8)
+    base = str(tmp_path / "vol")
+    _write_mhd(base, vol_u8)
+    iters = 21
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
+            "--centerline-method", "gpu", "--gvf-iterations", str(iters), "--tdf-only",
+            "--cropping", "threshold", "--cropping-threshold", "60", "--min-scan-lines-threshold", "3"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    cx, cy, cz = oracle.crop_scan_lines(vol_u8, 0, 60.0)
+    x1, y1, z1, SX, SY, SZ = test_crop.py_crop_bounds(cx, cy, cz, 3, False)
+    assert (SX, SY, SZ) != (84, 70, 60)
+    assert tuple(map(int, open(tmp_path / "size.txt").read().split())) == (SX, SY, SZ)
+    assert tuple(map(int, open(tmp_path / "shift.txt").read().split())) == (x1, y1, z1)
+    cropped = np.ascontiguousarray(vol_u8[z1:z1 + SZ, y1:y1 + SY, x1:x1 + SX])
+    T, _, _ = _oracle_run(oracle, cropped, iters)
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(SZ, SY, SX)
+    assert np.array_equal(tdf, T)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "no-loop-removal", "default", "vtk",
                                   "sphere", "no-segmentation"])
 def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):

@@ -4,8 +4,9 @@
 //
 // Stage order and parameter semantics follow the reference:
 //  readDatasetAndTransfer  (tube-segmentation.cpp:1399-1905): .mhd header,
-//      raw data, limits (getLimits :1380-1396), shrink to a multiple of 4,
-//      toFloat;
+//      raw data, limits (getLimits :1380-1396), upload, then lung or
+//      threshold cropping, the AAA-Vessels-CT in-plane crop or the shrink to
+//      a multiple of 4 on the device, toFloat;
 //  runCircleFittingMethod  (:212-939): small-radius TDF on the un-diffused
 //      field when radius-min < 2.5, GVF (Jacobi or FMG) of the large-blur
 //      field, large-radius TDF, combine;
@@ -19,7 +20,7 @@
 // The reference's GVF loop returns the result of iterations - 1 when the
 // iteration count is odd (gradientVectorFlow.cpp:1137-1172); run() does the
 // same.  Options outside this library's scope (other centerline methods, the
-// spline TDF, cropping, a CPU device) raise SIPL::SIPLException.
+// spline TDF, a CPU device) raise SIPL::SIPLException.
 #include <cuda_runtime_api.h>
 
 #include <algorithm>
@@ -68,6 +69,7 @@ struct DevBuf {
         return q;
     }
     template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+    void swap(DevBuf &o) { std::swap(p, o.p); }
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
 };
@@ -184,21 +186,45 @@ HostVolume read_volume(const std::string &filename, paramList &parameters, float
     return v;
 }
 
-// Shrink every extent down to a multiple of 4 (tube-segmentation.cpp:1800-1828).
-void shrink_to_multiple_of_4(HostVolume &v) {
-    SIPL::int3 s = v.size;
-    s.x -= s.x % 4;
-    s.y -= s.y % 4;
-    s.z -= s.z % 4;
-    if (s.x == v.size.x && s.y == v.size.y && s.z == v.size.z) return;
-    std::vector<char> out((size_t)s.x * s.y * s.z * v.elem);
-    for (int z = 0; z < s.z; z++)
-        for (int y = 0; y < s.y; y++)
-            std::memcpy(&out[((size_t)z * s.y + y) * s.x * v.elem],
-                        &v.data[((size_t)z * v.size.y + y) * v.size.x * v.elem], (size_t)s.x * v.elem);
-    std::cout << "NOTE: reduced size to " << s.x << ", " << s.y << ", " << s.z << std::endl;
-    v.data.swap(out);
-    v.size = s;
+// readDatasetAndTransfer after the upload (tube-segmentation.cpp:1556-1828):
+// lung or threshold cropping (scan-line counts on the GPU, the box on the
+// host), else the fixed in-plane crop of the AAA-Vessels-CT preset, else the
+// shrink of every extent to a multiple of 4.  box = x1, y1, z1, SX, SY, SZ;
+// returns the shift vector (left at zero by the AAA crop, as in the reference).
+SIPL::int3 input_box(paramList &P, const HostVolume &hv, const void *d_raw, cudaStream_t s, int *box) {
+    const int X = hv.size.x, Y = hv.size.y, Z = hv.size.z;
+    const std::string cropping = getParamStr(P, "cropping");
+    if (cropping == "lung" || cropping == "threshold") {
+        std::cout << "performing cropping" << std::endl;
+        const bool lung = cropping == "lung";
+        const int min_lines = (int)getParam(P, lung ? "min-scan-lines-lung" : "min-scan-lines-threshold");
+        const bool middle = lung || getParamStr(P, "cropping-start-z") == "middle";
+        const size_t wsb = tsf_crop_workspace_size(X, Y, Z);
+        DevBuf ws(wsb), counts(sizeof(int16_t) * ((size_t)X + Y + Z));
+        check(tsf_crop_scan_lines(d_raw, hv.type, X, Y, Z, lung ? 1 : 0, lung ? 0.0f : getParam(P, "cropping-threshold"),
+                                  counts.as<int16_t>(), ws.p, wsb, (void *)s),
+              "cropping");
+        std::vector<int16_t> hc((size_t)X + Y + Z);
+        check_cuda(cudaMemcpyAsync(hc.data(), counts.p, hc.size() * sizeof(int16_t), cudaMemcpyDeviceToHost, s),
+                   "cropping");
+        check_cuda(cudaStreamSynchronize(s), "cropping");
+        if (tsf_crop_bounds(hc.data(), X, Y, Z, min_lines, middle ? 1 : 0, box) != TSF_OK)
+            raise(tsf_last_error_string());
+        std::cout << "Dataset cropped to " << box[3] << ", " << box[4] << ", " << box[5] << std::endl;
+        return SIPL::int3(box[0], box[1], box[2]);
+    }
+    if (getParamStr(P, "parameters") == "AAA-Vessels-CT") {
+        check(tsf_crop_box_fixed(X, Y, Z, 0.15f, box), "cropping");
+        std::cout << "NOTE: reduced size to " << box[3] << ", " << box[4] << ", " << box[5] << std::endl;
+        return SIPL::int3(0, 0, 0);
+    }
+    box[0] = box[1] = box[2] = 0;
+    box[3] = X - X % 4;
+    box[4] = Y - Y % 4;
+    box[5] = Z - Z % 4;
+    if (box[3] != X || box[4] != Y || box[5] != Z)
+        std::cout << "NOTE: reduced size to " << box[3] << ", " << box[4] << ", " << box[5] << std::endl;
+    return SIPL::int3(0, 0, 0);
 }
 
 int storage_from_parameters(paramList &p) {
@@ -292,27 +318,32 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         raise("device " + getParamStr(parameters, "device") + " is not supported: this library runs on the GPU");
     const std::string method = getParamStr(parameters, "centerline-method");
     if (method != "gpu") raise("centerline-method " + method + " is not part of this library (use gpu)");
-    if (getParamStr(parameters, "cropping") != "no")
-        raise("cropping " + getParamStr(parameters, "cropping") +
-              " is not part of this library; crop the volume beforehand and use --cropping no");
 
     float minimum = 0.0f, maximum = 1.0f;
     HostVolume hv = read_volume(filename, parameters, minimum, maximum);
     std::cout << "Dataset of size " << hv.size.x << " " << hv.size.y << " " << hv.size.z << " loaded" << std::endl;
-    shrink_to_multiple_of_4(hv);
-    const int X = hv.size.x, Y = hv.size.y, Z = hv.size.z;
+    Stream stream;
+    void *S = (void *)stream.s;
+    DevBuf raw(hv.data.size());
+    check_cuda(cudaMemcpyAsync(raw.p, hv.data.data(), hv.data.size(), cudaMemcpyHostToDevice, stream.s), "upload");
+    int box[6];
+    const SIPL::int3 shift = input_box(parameters, hv, raw.p, stream.s, box);
+    const int X = box[3], Y = box[4], Z = box[5];
     const size_t n = (size_t)X * Y * Z;
+    if (X != hv.size.x || Y != hv.size.y || Z != hv.size.z) {
+        DevBuf cropped(n * hv.elem);
+        check(tsf_crop_copy(raw.p, hv.type, hv.size.x, hv.size.y, hv.size.z, box, cropped.p, S), "cropping");
+        raw.swap(cropped);
+    }
+    std::vector<char>().swap(hv.data);   // the upload has been staged; the host copy is not needed again
     const bool tdf16 = getParamBool(parameters, "16bit-vectors");
     const int st = storage_from_parameters(parameters);
 
     TSFOutput *output = new TSFOutput(new SIPL::int3(X, Y, Z), tdf16);
     output->setSpacing(hv.spacing);
-    output->setShiftVector(SIPL::int3(0, 0, 0));
+    output->setShiftVector(shift);
     try {
-        Stream stream;
-        void *S = (void *)stream.s;
-        DevBuf raw(hv.data.size()), vol(n * 4);
-        check_cuda(cudaMemcpyAsync(raw.p, hv.data.data(), hv.data.size(), cudaMemcpyHostToDevice, stream.s), "upload");
+        DevBuf vol(n * 4);
         check(tsf_to_float(raw.p, hv.type, (int64_t)n, minimum, maximum, vol.as<float>(), S), "toFloat");
         raw.alloc(0);
 

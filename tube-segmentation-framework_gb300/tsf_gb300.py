@@ -73,6 +73,11 @@ def _declare(L):
         "tsf_link_workspace_size": (_sz, [_i]),
         "tsf_link_centerpoints": (_i, [_p, _i, _p, _i, _i, _i, _i, _f, _f, _p, _p, _p, _p, _p, _sz, _p]),
         "tsf_rasterize_trees": (_i, [_p, _p, _i, _p, _p, _i, _p, _i, _i, _i, _p]),
+        "tsf_crop_workspace_size": (_sz, [_i, _i, _i]),
+        "tsf_crop_scan_lines": (_i, [_p, _i, _i, _i, _i, _i, _f, _p, _p, _sz, _p]),
+        "tsf_crop_bounds": (_i, [_p, _i, _i, _i, _i, _i, _p]),
+        "tsf_crop_box_fixed": (_i, [_i, _i, _i, _f, _p]),
+        "tsf_crop_copy": (_i, [_p, _i, _i, _i, _i, _p, _p, _p]),
         "tsf_segment_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_segment_inverse_gradient": (_i, [_p, _p, _i, _p, _i, _i, _i, _p, _p, _p, _sz, _p]),
         "tsf_segment_spheres": (_i, [_p, _p, _i, _i, _i, _p, _p]),
@@ -336,6 +341,55 @@ def rasterize_trees(vertices, edges, labels, sizes, min_tree_length: int, shape,
     e = edges.contiguous()
     _check(load().tsf_rasterize_trees(_ptr(vertices), _ptr(e) if e.numel() else None, e.shape[0], _ptr(labels),
                                       _ptr(sizes), int(min_tree_length), _ptr(out), X, Y, Z, _stream(stream)))
+    return out
+
+
+def _raw_type(t):
+    torch = _torch()
+    return {torch.uint8: 0, torch.int8: 1, torch.int16: 3, torch.float32: 4}[t.dtype]
+
+
+def crop_scan_lines(vol, method: int, threshold: float = 0.0, raw_type: int = None, stream=None):
+    """cropDatasetThreshold (method 0) / cropDatasetLung (method 1) on a raw
+    CUDA volume (Z, Y, X): (counts_x, counts_y, counts_z) int16.  raw_type
+    overrides the type taken from the dtype (2 = uint16 data held in an int16
+    tensor)."""
+    torch = _torch()
+    L = load()
+    Z, Y, X = vol.shape
+    rt = _raw_type(vol) if raw_type is None else raw_type
+    counts = torch.empty(X + Y + Z, dtype=torch.int16, device=vol.device)
+    ws = workspace(L.tsf_crop_workspace_size(X, Y, Z))
+    _check(L.tsf_crop_scan_lines(_ptr(vol), rt, X, Y, Z, int(method), float(threshold), _ptr(counts), _ptr(ws),
+                                 ws.numel(), _stream(stream)))
+    return counts[:X], counts[X:X + Y], counts[X + Y:]
+
+
+def crop_bounds(cx, cy, cz, min_scan_lines: int, start_z_middle: bool):
+    """Host crop box (x1, y1, z1, SX, SY, SZ) from numpy int16 counts."""
+    import numpy as np
+    c = np.ascontiguousarray(np.concatenate([cx, cy, cz]), dtype=np.int16)
+    box = (C.c_int * 6)()
+    _check(load().tsf_crop_bounds(_np_ptr(c), len(cx), len(cy), len(cz), int(min_scan_lines), int(start_z_middle),
+                                  box))
+    return tuple(box)
+
+
+def crop_box_fixed(shape, fraction: float):
+    Z, Y, X = shape
+    box = (C.c_int * 6)()
+    _check(load().tsf_crop_box_fixed(X, Y, Z, float(fraction), box))
+    return tuple(box)
+
+
+def crop_copy(vol, box, raw_type: int = None, stream=None):
+    torch = _torch()
+    Z, Y, X = vol.shape
+    x1, y1, z1, SX, SY, SZ = box
+    out = torch.empty((SZ, SY, SX), dtype=vol.dtype, device=vol.device)
+    b = (C.c_int * 6)(*box)
+    _check(load().tsf_crop_copy(_ptr(vol), _raw_type(vol) if raw_type is None else raw_type, X, Y, Z, b, _ptr(out),
+                                _stream(stream)))
     return out
 
 
