@@ -5,7 +5,10 @@
 //   TSFOutput *runSegmentation(...)   -- the same call under the name the
 //                                        benchmark description uses
 //
-// run() reads an .mhd/.raw volume, converts it to [0,1] floats, and runs the
+// run() reads an .mhd/.raw volume, crops it (`cropping lung|threshold`; the
+// AAA-Vessels-CT preset's in-plane crop; else a shrink of every extent to a
+// multiple of 4; getShiftVector() gives the box corner), converts it to [0,1]
+// floats, and runs the
 // GPU hot path of the `gpu` centerline method on the current CUDA device:
 // Gaussian blur, the vector field, the small-radius TDF on the un-diffused
 // field, GVF (Jacobi, or full multigrid with use-fmg-gvf), the large-radius
