@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--fmg-cycles", type=int, default=10)
     ap.add_argument("--adjoint", action="store_true",
                     help="time the forward + adjoint (gradient) pass alone and print its JSON line")
+    ap.add_argument("--stage", choices=["spline", "circle", "segment", "crop"],
+                    help="time one stage alone and print its JSON line (a small, self-contained command for "
+                         "kernel profiles): a TDF on the vessel-tree field after --iters GVF iterations, the "
+                         "segmentation of that step's centerlines, or the lung cropping of the 512x512x400 CT")
     ap.add_argument("--summarize-ncu-csv", metavar="CSV",
                     help="print a per-kernel table (launches, total time, share) of an ncu "
                          "--metrics gpu__time_duration.sum --csv launch list and exit")
@@ -406,6 +410,7 @@ def run_tsf(args, rank, world):
     res["linking"] = linking_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
     res["segmentation"] = segmentation_timing(torch, T, pipe,
                                               rank == 0 and world == 1 and not args.no_cpu_baseline)
+    res["spline_tdf"] = spline_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
@@ -548,6 +553,93 @@ def segmentation_timing(torch, T, pipe, with_cpu):
         out["cpu_cores"] = O.get_threads()
         out["matches_oracle"] = bool(rit == iters and (ref == seg.cpu().numpy()).all())
     return out
+
+
+def spline_timing(torch, T, pipe, with_cpu):
+    """The spline TDF (tsf_tdf_spline, the large-radius TDF of the
+    use-spline-tdf presets) on the step's GVF field, from max(1.5, rmin) to
+    rmax in the workload's steps, beside the circle-fitting TDF on the same
+    field and radii; CUDA events over 3 repetitions after one warm-up, and the
+    oracle on a 64-slice slab of the field on the host."""
+    P = PARAMS
+    rmin = max(1.5, P["rmin"])
+    Tsp, Rsp = T.tdf_spline(pipe.field, rmin, P["rmax"], P["rstep"], storage=pipe.storage)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    a.record()
+    for _ in range(reps):
+        Tsp, Rsp = T.tdf_spline(pipe.field, rmin, P["rmax"], P["rstep"], storage=pipe.storage)
+    b.record()
+    torch.cuda.synchronize()
+    sp_ms = a.elapsed_time(b) / reps
+    a.record()
+    for _ in range(reps):
+        T.tdf_circle(pipe.field, rmin, P["rmax"], P["rstep"], storage=pipe.storage)
+    b.record()
+    torch.cuda.synchronize()
+    out = {"radii": [rmin, P["rmax"], P["rstep"]], "ms": round(sp_ms, 3),
+           "circle_fit_same_radii_ms": round(a.elapsed_time(b) / reps, 3),
+           "valid_voxels": int((Tsp > 0).sum())}
+    if with_cpu:
+        import oracle as O
+        F = pipe.field
+        if pipe.storage == "snorm16":       # max(-1, s / 32767), divided on the host
+            Fh = np.maximum(np.float32(-1.0), F.cpu().numpy().astype(np.float32) / np.float32(32767.0))
+        else:
+            Fh = F.float().cpu().numpy()
+        z0 = Fh.shape[0] // 2 - 32
+        slab = np.ascontiguousarray(Fh[z0:z0 + 64])
+        t0 = time.perf_counter()
+        O.tdf_spline(slab, rmin, P["rmax"], P["rstep"])
+        cpu_s = time.perf_counter() - t0
+        out["cpu_oracle_ms_per_volume"] = round(cpu_s * 1e3 * Fh.shape[0] / 64, 1)
+        out["cpu_cores"] = O.get_threads()
+        out["cpu_sample"] = "64-slice slab of the field, scaled to the volume"
+    return out
+
+
+def run_stage(args):
+    """One stage alone.  spline / circle: the vessel tree (--size^3), blur,
+    vector field and --iters GVF iterations in --storage, then the TDF 3 times
+    after one warm-up (CUDA events; spline from max(1.5, rmin), circle from
+    max(2.5, rmin), both to the workload's rmax).  segment: one pipeline step
+    with --iters GVF iterations, then segmentation_timing.  crop:
+    crop_timing on the 512x512x400 lung CT."""
+    import torch
+    import synthetic
+    import tsf_gb300 as T
+    n, st, P = args.size, args.storage, PARAMS
+    if args.stage == "crop":
+        hu = synthetic.lung_ct((400, 512, 512), seed=args.seed)
+        return {"stage": "crop", "workload": "lung-airway CT 512x512x400 int16",
+                "lung_cropping": crop_timing(torch, T, hu, False)}
+    if args.stage == "segment":
+        pipe = Pipeline(T, torch, (n, n, n), st, args.iters, args.mu)
+        pipe.vol.copy_(torch.from_numpy(synthetic.vascular_tree((n, n, n), seed=args.seed)))
+        pipe.step()
+        torch.cuda.synchronize()
+        return {"stage": "segment", "workload": "vessel tree %d^3, GVF %d iterations, %s storage" % (n, args.iters, st),
+                "segmentation": segmentation_timing(torch, T, pipe, False)}
+    vol = torch.from_numpy(synthetic.vascular_tree((n, n, n), seed=args.seed)).cuda()
+    b = T.blur(vol, P["large_blur"])
+    f0, _ = T.vector_field(b, P["fmax"], P["vsign"], storage=st)
+    v = T.gvf(f0, args.mu, args.iters, storage=st)
+    field = T.gvf_finish(v, storage=st)
+    if args.stage == "spline":
+        run = lambda: T.tdf_spline(field, max(1.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
+    else:
+        run = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
+    run()
+    torch.cuda.synchronize()
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(3):
+        Tt, _ = run()
+    e.record()
+    torch.cuda.synchronize()
+    return {"stage": args.stage, "workload": "vessel tree %d^3, GVF %d iterations, %s storage" % (n, args.iters, st),
+            "ms": round(a.elapsed_time(e) / 3, 3), "nonzero": int((Tt != 0).sum())}
 
 
 def run_adjoint(args):
@@ -812,6 +904,9 @@ def main():
         return
     if args.adjoint:
         print(json.dumps(run_adjoint(args)))
+        return
+    if args.stage:
+        print(json.dumps(run_stage(args)))
         return
     if args.fmg:
         print(json.dumps(run_fmg_workload(args)))

@@ -226,6 +226,20 @@ int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, 
                         float rmax, float rstep, void *d_T, int tdf_unorm16, float *d_R, int mode,
                         void *stream);
 
+/* splineTDF (kernels.cl:1159-1254, kernels_no_3d_write.cl:1574-1671; driver
+ * runSplineTDF, tubeDetectionFilters.cpp:4-55, called with
+ * max(1.5, radius-min) at tube-segmentation.cpp:785-786): the normalised
+ * Hessian's eigenvectors, then 12 arms in the plane of e2 and e3, each a line
+ * search from max(1, rmin) in steps of rstep up to rmax for the first border
+ * point of the field magnitude (minimum mean rise 0.1).  T = 0 where an arm
+ * finds none or the border field points along the arm, else
+ * min(1, mean(1 - |n . e1|) * symmetry + 0.2); R = the sum of the radii found
+ * / 12.  T as float, or unorm16 when tdf_unorm16 != 0.  At most 4096 radii per
+ * arm (the reference does not end the search for a step that does not
+ * advance the radius). */
+int tsf_tdf_spline(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
+                   float rstep, void *d_T, int tdf_unorm16, float *d_R, void *stream);
+
 /* combine (kernels.cl:561-572, tube-segmentation.cpp:802-824): where the small
  * TDF exceeds the large one, take it and its radius.  d_T_large / d_R_large
  * are updated in place; T arrays are float or unorm16 per tdf_unorm16. */

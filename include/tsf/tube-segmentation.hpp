@@ -12,7 +12,8 @@
 // GPU hot path of the `gpu` centerline method on the current CUDA device:
 // Gaussian blur, the vector field, the small-radius TDF on the un-diffused
 // field, GVF (Jacobi, or full multigrid with use-fmg-gvf), the large-radius
-// TDF and the combination of both, then the candidate stage (threshold,
+// TDF (circle fitting, or the spline TDF with use-spline-tdf) and the
+// combination of both, then the candidate stage (threshold,
 // compaction, cross-section filter, per-cube arg-max).  kernel_dir is
 // accepted and ignored (the kernels are compiled into the library).
 //

@@ -85,6 +85,7 @@ def _declare(L):
         getattr(L, "orc_gvf_finish" + s).argtypes = [_p, _i64, _i, _p]
         getattr(L, "orc_eig3" + s).argtypes = [_p, _p, _p]
         getattr(L, "orc_tdf_circle" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
+        getattr(L, "orc_tdf_spline" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
         getattr(L, "orc_combine" + s).argtypes = [_p, _p, _p, _p, _i64]
         getattr(L, "orc_candidates2" + s).argtypes = [_p, _p, _i, _i, _i, _p, _i64, _p]
         getattr(L, "orc_dd" + s).argtypes = [_p, _p, _i, _i, _i, _i, _p]
@@ -234,6 +235,19 @@ def tdf_circle(field4: np.ndarray, rmin: float, rmax: float, rstep: float,
     R = np.empty((Z, Y, X), dt)
     getattr(lib(), "orc_tdf_circle" + s)(_ptr(field4), X, Y, Z, float(rmin), float(rmax),
                                          float(rstep), _ptr(T), _ptr(R))
+    return T, R
+
+
+def tdf_spline(field4: np.ndarray, rmin: float, rmax: float, rstep: float, f64: bool = False):
+    """splineTDF, kernels.cl:1159-1254, with runSplineTDF's constants
+    (rMin = max(1, rmin), 12 arms, minAverageMag 0.1) -> (T, R) float volumes."""
+    dt, s = _real(f64)
+    field4 = np.ascontiguousarray(field4, dtype=dt)
+    Z, Y, X = field4.shape[:3]
+    T = np.empty((Z, Y, X), dt)
+    R = np.empty((Z, Y, X), dt)
+    getattr(lib(), "orc_tdf_spline" + s)(_ptr(field4), X, Y, Z, float(rmin), float(rmax), float(rstep), _ptr(T),
+                                         _ptr(R))
     return T, R
 
 

@@ -158,6 +158,15 @@ void orc_circle_table(float cosv[32], float sinv[32]) {
     }
 }
 
+void orc_arm_table(float cosv[12], float sinv[12]) {
+    const float two_pi = 2.0f * 3.14159265358979323846f;   /* 2 * M_PI_F */
+    for (int j = 0; j < 12; j++) {
+        const float alpha = two_pi * (float)j / 12.0f;
+        cosv[j] = (float)cos((double)alpha);
+        sinv[j] = (float)sin((double)alpha);
+    }
+}
+
 /* createBlurMask, tube-segmentation.cpp:188-211: half width m = ceil(sigma/0.5)
  * clamped to [1,5]; weights exp(-(a^2+b^2+c^2)/(2 sigma^2)) normalised to sum 1.
  * The exponential is evaluated in double (C exp) and rounded to float; the

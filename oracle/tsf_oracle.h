@@ -56,6 +56,10 @@ void orc_from_unorm16_array(const uint16_t *in, float *out, int64_t n);
  * sample directions of circleFittingTDF (kernels.cl:1068-1069). */
 void orc_circle_table(float cosv[32], float sinv[32]);
 
+/* The 12 arm directions of splineTDF (kernels.cl:1211-1212): alpha_j =
+ * 2 * M_PI_F * j / 12 in float, cos and sin in double rounded to float. */
+void orc_arm_table(float cosv[12], float sinv[12]);
+
 /* createBlurMask (tube-segmentation.cpp:188-211).  mask must hold 11^3 floats.
  * Returns maskSize (the half width m). */
 int orc_blur_mask(float sigma, float *mask);
@@ -78,6 +82,8 @@ int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, in
     void orc_gvf_finish##S(const R *v_planar, int64_t n, int storage, R *field4);       \
     void orc_eig3##S(const R A[9], R V[9], R d[3]);                                     \
     void orc_tdf_circle##S(const R *field4, int X, int Y, int Z, float rMin, float rMax,  \
+                           float rStep, R *T, R *radius);                               \
+    void orc_tdf_spline##S(const R *field4, int X, int Y, int Z, float rMin, float rMax,  \
                            float rStep, R *T, R *radius);                               \
     void orc_combine##S(const R *Ts, const R *Rs, R *Tl, R *Rl, int64_t n);             \
     void orc_candidates2##S(const R *radius, const R *field4, int X, int Y, int Z,       \

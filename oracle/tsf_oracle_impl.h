@@ -450,6 +450,90 @@ void FN(orc_tdf_circle)(const REAL *F, int X, int Y, int Z, float rMin, float rM
             }
 }
 
+/* splineTDF, kernels.cl:1159-1254 (kernels_no_3d_write.cl:1574-1671), with
+ * the driver's constants (tubeDetectionFilters.cpp:37-48): rMin = max(1, rMin),
+ * 12 arms, minAverageMag 0.1.  Normalised Hessian, eigenvectors e1, e2, e3;
+ * per arm a line search from rMin for the first border point (magnitude
+ * falling after having risen, mean of the last two magnitudes above the
+ * voxel's own by more than 0.1); an arm without one, or whose border field
+ * points along the arm, makes the voxel invalid (T = 0).  At most 4096 radii
+ * per arm (the reference loops forever for a step that does not advance). */
+void FN(orc_tdf_spline)(const REAL *F, int X, int Y, int Z, float rMin, float rMax,
+                        float rStep, REAL *T, REAL *Rout) {
+    float cf[12], sf[12];
+    orc_arm_table(cf, sf);
+    if (rMin < 1.0f) rMin = 1.0f;
+    const REAL minAvg = (REAL)0.1f;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                REAL H[3][3], A[9], V[9], d[3];
+                FN(orc_hessian)(F, X, Y, Z, x, y, z, 1, H);
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) A[3 * i + j] = H[i][j];
+                FN(orc_eig3)(A, V, d);
+                const REAL e1[3] = {V[0 * 3 + 0], V[1 * 3 + 0], V[2 * 3 + 0]};
+                const REAL e2[3] = {V[0 * 3 + 1], V[1 * 3 + 1], V[2 * 3 + 1]};
+                const REAL e3[3] = {V[0 * 3 + 2], V[1 * 3 + 2], V[2 * 3 + 2]};
+                const REAL *c4 = F + 4 * IDX(x, y, z);
+                const REAL cur = RSQRT_((c4[0] * c4[0] + c4[1] * c4[1]) + c4[2] * c4[2]);
+                REAL maxRadius[12], sum = 0, avgRadius = 0;
+                int invalid = 0;
+                for (int j = 0; j < 12; j++) {
+                    maxRadius[j] = 999;
+                    const REAL c = (REAL)cf[j], s = (REAL)sf[j];
+                    const REAL va[3] = {c * e3[0] + s * e2[0], c * e3[1] + s * e2[1], c * e3[2] + s * e2[2]};
+                    REAL smp[3];
+                    FN(orc_sample_linear)(F, X, Y, Z, (REAL)x + (REAL)rMin * va[0], (REAL)y + (REAL)rMin * va[1],
+                                          (REAL)z + (REAL)rMin * va[2], smp);
+                    REAL prevMagnitude = RSQRT_((smp[0] * smp[0] + smp[1] * smp[1]) + smp[2] * smp[2]);
+                    int up = cur > prevMagnitude ? 0 : 1;
+                    int nr = 0;
+                    for (REAL radius = (REAL)rMin + (REAL)rStep; radius <= (REAL)rMax && nr < 4096;
+                         radius = radius + (REAL)rStep, nr++) {
+                        REAL vec[3];
+                        FN(orc_sample_linear)(F, X, Y, Z, (REAL)x + radius * va[0], (REAL)y + radius * va[1],
+                                              (REAL)z + radius * va[2], vec);
+                        const REAL magnitude = RSQRT_((vec[0] * vec[0] + vec[1] * vec[1]) + vec[2] * vec[2]);
+                        if (up == 1 && magnitude < prevMagnitude &&
+                            (prevMagnitude + magnitude) / (REAL)2 - cur > minAvg) {
+                            maxRadius[j] = radius;
+                            avgRadius = avgRadius + radius;
+                            const REAL n[3] = {vec[0] / magnitude, vec[1] / magnitude, vec[2] / magnitude};
+                            const REAL la = RSQRT_((va[0] * va[0] + va[1] * va[1]) + va[2] * va[2]);
+                            const REAL na[3] = {-(va[0] / la), -(va[1] / la), -(va[2] / la)};
+                            if ((n[0] * na[0] + n[1] * na[1]) + n[2] * na[2] < 0) {
+                                invalid = 1;
+                                sum = 0;
+                            }
+                            sum = sum + ((REAL)1 - RFABS_((n[0] * e1[0] + n[1] * e1[1]) + n[2] * e1[2]));
+                            break;
+                        }
+                        if (magnitude > prevMagnitude) up = 1;
+                        prevMagnitude = magnitude;
+                    }
+                    if (maxRadius[j] == 999 || invalid == 1) {
+                        invalid = 1;
+                        break;
+                    }
+                }
+                Rout[IDX(x, y, z)] = avgRadius / (REAL)12;
+                if (invalid) {
+                    T[IDX(x, y, z)] = 0;
+                } else {
+                    REAL avgSymmetry = 0;
+                    for (int j = 0; j < 6; j++) {
+                        const REAL a = maxRadius[j], b = maxRadius[6 + j];
+                        avgSymmetry = avgSymmetry + (a < b ? a : b) / (a > b ? a : b);
+                    }
+                    avgSymmetry = avgSymmetry / (REAL)6;
+                    const REAL t = (sum / (REAL)12) * avgSymmetry + (REAL)0.2f;
+                    T[IDX(x, y, z)] = t < (REAL)1 ? t : (REAL)1;
+                }
+            }
+}
+
 /* combine, kernels.cl:561-572 */
 void FN(orc_combine)(const REAL *Ts, const REAL *Rs, REAL *Tl, REAL *Rl, int64_t n) {
 #pragma omp parallel for schedule(static)

@@ -38,8 +38,9 @@ def _write_mhd(path, vol_u8):
     vol_u8.tofile(path + ".raw")
 
 
-def _oracle_run(oracle, vol_u8, iters):
-    """run() with the Synthetic-Vascusynth preset, restated with the oracle."""
+def _oracle_run(oracle, vol_u8, iters, spline=False):
+    """run() with the Synthetic-Vascusynth preset, restated with the oracle
+    (spline: the large-radius TDF is the spline TDF from max(1.5, radius-min))."""
     v = np.clip(vol_u8.astype(np.float32), np.float32(0), np.float32(75)) / np.float32(75)   # toFloat
     st = "snorm16"
     f_small = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                          # small-blur 1.0
@@ -47,7 +48,7 @@ def _oracle_run(oracle, vol_u8, iters):
     f4 = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                               # large-blur 1.0
     vv = oracle.gvf(f4, 0.05, iters - iters % 2, st)
     field = oracle.gvf_finish(vv, st)
-    Tl, Rl = oracle.tdf_circle(field, 2.5, 4.0, 1.0)
+    Tl, Rl = oracle.tdf_spline(field, 1.5, 4.0, 1.0) if spline else oracle.tdf_circle(field, 2.5, 4.0, 1.0)
     us, ul = oracle.to_unorm16(Ts), oracle.to_unorm16(Tl)
     m = ul < us
     T16 = np.where(m, us, ul)
@@ -63,6 +64,29 @@ def _read_vtk(path):
     nl = int(lines[k + 1].split()[1])
     edges = np.array([list(map(int, l.split()))[1:] for l in lines[k + 2:k + 2 + nl]], np.int32).reshape(-1, 2)
     return pts, edges
+
+
+@pytest.mark.gpu
+def test_run_spline_tdf(api_tests, oracle, synth, tmp_path):
+    """run() with use-spline-tdf: the combined TDF (small-radius circle fit,
+    large-radius spline TDF) matches the oracle's, and the pipeline links and
+    segments on it."""
+    pytest.importorskip("torch")
+    vol_u8 = np.round(synth.vascular_tree((44, 52, 60), seed=11) * 90.0).astype(np.uint8)
+    base = str(tmp_path / "vol")
+    _write_mhd(base, vol_u8)
+    iters = 21
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
+            "--centerline-method", "gpu", "--gvf-iterations", str(iters), "--use-spline-tdf", "true"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    T, R, field = _oracle_run(oracle, vol_u8, iters, spline=True)
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(T.shape)
+    assert np.array_equal(tdf, T)
+    ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
+    got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
+    assert len(got) > 20 and np.array_equal(got, ref["vertices"])
+    assert (tmp_path / "segmentation.raw").exists()
 
 
 @pytest.mark.gpu

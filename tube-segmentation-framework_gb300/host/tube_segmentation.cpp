@@ -19,8 +19,9 @@
 //      radius (averaged along the edges after host loop removal).
 // The reference's GVF loop returns the result of iterations - 1 when the
 // iteration count is odd (gradientVectorFlow.cpp:1137-1172); run() does the
-// same.  Options outside this library's scope (other centerline methods, the
-// spline TDF, a CPU device) raise SIPL::SIPLException.
+// same.  Options outside this library's scope (other centerline methods, a
+// CPU device) raise SIPL::SIPLException.  With use-spline-tdf the large-radius
+// TDF is the spline TDF (from max(1.5, radius-min), tube-segmentation.cpp:785-789).
 #include <cuda_runtime_api.h>
 
 #include <algorithm>
@@ -273,7 +274,6 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         }
         f4small.alloc(0);   // free early, as the reference does
     }
-    if (getParamBool(P, "use-spline-tdf")) raise("the spline TDF (use-spline-tdf) is not part of this library");
 
     DevBuf blurred;
     const float *src = d_vol;
@@ -305,8 +305,12 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
     }
     out.T.alloc(n * ts);
     out.R.alloc(n * 4);
-    check(tsf_tdf_circle(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
-                         out.R.as<float>(), S), "TDF");
+    if (getParamBool(P, "use-spline-tdf"))
+        check(tsf_tdf_spline(out.field.p, X, Y, Z, st, std::max(1.5f, rMin), rMax, rStep, out.T.p, tdf16,
+                             out.R.as<float>(), S), "spline TDF");
+    else
+        check(tsf_tdf_circle(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
+                             out.R.as<float>(), S), "TDF");
     if (rMin < 2.5f)
         check(tsf_tdf_combine(Ts.p, Rs.as<float>(), out.T.p, out.R.as<float>(), (int64_t)n, tdf16, S), "combine");
 }

@@ -96,6 +96,7 @@ def _declare(L):
         "tsf_blur_backward_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_blur_backward": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
+        "tsf_tdf_spline": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
         "tsf_tdf_circle_mode": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _i, _p]),
         "tsf_candidates_workspace_size": (_sz, [_i, _i, _i]),
@@ -312,6 +313,17 @@ def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = 
     R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
     _check(load().tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
                                       float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
+    return T, R
+
+
+def tdf_spline(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, stream=None):
+    """splineTDF with runSplineTDF's constants: (T, R) on the device."""
+    torch = _torch()
+    Z, Y, X = field4.shape[:3]
+    T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
+    R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
+    _check(load().tsf_tdf_spline(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax), float(rstep),
+                                 _ptr(T), int(unorm16), _ptr(R), _stream(stream)))
     return T, R
 
 
