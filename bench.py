@@ -177,6 +177,7 @@ class Pipeline:
         self.Rl = torch.empty_like(self.Ts)
         self.gvf_ws = T.workspace(L.tsf_gvf_workspace_size(X, Y, Z, st))
         self.cand_ws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
+        self.tdf_ws = T.workspace(L.tsf_tdf_workspace_size(X, Y, Z, st))   # x-paired texels (16-bit storage)
         self.max_vertices = 1 << 16
         self.verts = torch.zeros((self.max_vertices, 3), dtype=torch.int32, device=dev)
         self.last = None
@@ -194,16 +195,18 @@ class Pipeline:
         T.blur(self.vol, P["large_blur"], out=self.blurred)
         # small-radius pass on the un-diffused field of the unblurred volume (small-blur 0)
         self._vf(self.vol, None, self.f4_small)
-        T._check(T.load().tsf_tdf_circle(T._ptr(self.f4_small), *self._xyz(), T.STORAGE[s], P["rmin"], 3.0, 0.5,
-                                         T._ptr(self.Ts), 0, T._ptr(self.Rs), T._stream()))
+        T._check(T.load().tsf_tdf_circle_ws(T._ptr(self.f4_small), *self._xyz(), T.STORAGE[s], P["rmin"], 3.0, 0.5,
+                                            T._ptr(self.Ts), 0, T._ptr(self.Rs), T._ptr(self.tdf_ws),
+                                            self.tdf_ws.numel(), T._stream()))
         rec("tdf_small")
         self._vf(self.blurred, self.f0, None)
         rec("vector_field")
         self.gvf_only()
         rec("gvf")
         T.gvf_finish(self.v, s, out=self.field)
-        T._check(T.load().tsf_tdf_circle(T._ptr(self.field), *self._xyz(), T.STORAGE[s], max(2.5, P["rmin"]),
-                                         P["rmax"], P["rstep"], T._ptr(self.Tl), 0, T._ptr(self.Rl), T._stream()))
+        T._check(T.load().tsf_tdf_circle_ws(T._ptr(self.field), *self._xyz(), T.STORAGE[s], max(2.5, P["rmin"]),
+                                            P["rmax"], P["rstep"], T._ptr(self.Tl), 0, T._ptr(self.Rl),
+                                            T._ptr(self.tdf_ws), self.tdf_ws.numel(), T._stream()))
         T.tdf_combine(self.Ts, self.Rs, self.Tl, self.Rl)
         rec("tdf_large")
         self.last = self._candidates()
@@ -603,7 +606,8 @@ def run_stage(args):
     """One stage alone.  spline / circle: the vessel tree (--size^3), blur,
     vector field and --iters GVF iterations in --storage, then the TDF 3 times
     after one warm-up (CUDA events; spline from max(1.5, rmin), circle from
-    max(2.5, rmin), both to the workload's rmax).  segment: one pipeline step
+    max(2.5, rmin), both to the workload's rmax; circle is timed without and
+    with the paired-texel workspace).  segment: one pipeline step
     with --iters GVF iterations, then segmentation_timing.  crop:
     crop_timing on the 512x512x400 lung CT."""
     import torch
@@ -626,20 +630,28 @@ def run_stage(args):
     f0, _ = T.vector_field(b, P["fmax"], P["vsign"], storage=st)
     v = T.gvf(f0, args.mu, args.iters, storage=st)
     field = T.gvf_finish(v, storage=st)
+    runs = {}
     if args.stage == "spline":
-        run = lambda: T.tdf_spline(field, max(1.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
+        runs["spline"] = lambda: T.tdf_spline(field, max(1.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
     else:
-        run = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
-    run()
+        ws = T.workspace(T.load().tsf_tdf_workspace_size(n, n, n, T.STORAGE[st]))
+        runs["circle"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
+        runs["circle_paired"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st,
+                                                     ws=ws)
+    for run in runs.values():
+        run()
     torch.cuda.synchronize()
-    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(3):
-        Tt, _ = run()
-    e.record()
-    torch.cuda.synchronize()
-    return {"stage": args.stage, "workload": "vessel tree %d^3, GVF %d iterations, %s storage" % (n, args.iters, st),
-            "ms": round(a.elapsed_time(e) / 3, 3), "nonzero": int((Tt != 0).sum())}
+    out = {"stage": args.stage, "workload": "vessel tree %d^3, GVF %d iterations, %s storage" % (n, args.iters, st)}
+    for name, run in runs.items():
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            Tt, _ = run()
+        e.record()
+        torch.cuda.synchronize()
+        out[name + "_ms"] = round(a.elapsed_time(e) / 3, 3)
+        out[name + "_nonzero"] = int((Tt != 0).sum())
+    return out
 
 
 def run_adjoint(args):
@@ -828,6 +840,7 @@ def run_fmg_workload(args):
     ws = T.workspace(L.tsf_gvf_fmg_workspace_size(X, Y, Z, T.STORAGE[st]))
     Ts = torch.empty_like(vol); Rs = torch.empty_like(vol); Tl = torch.empty_like(vol); Rl = torch.empty_like(vol)
     cws = T.workspace(L.tsf_candidates_workspace_size(X, Y, Z))
+    tws = T.workspace(L.tsf_tdf_workspace_size(X, Y, Z, T.STORAGE[st]))
     verts = torch.zeros((1 << 16, 3), dtype=torch.int32, device="cuda")
     import ctypes as C
 
@@ -836,13 +849,15 @@ def run_fmg_workload(args):
             else (lambda: None)
         rec()
         T._check(L.tsf_vector_field(T._ptr(vol), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4s), T._stream()))
-        T._check(L.tsf_tdf_circle(T._ptr(f4s), X, Y, Z, T.STORAGE[st], P["rmin"], 3.0, 0.5, T._ptr(Ts), 0, T._ptr(Rs), T._stream()))
+        T._check(L.tsf_tdf_circle_ws(T._ptr(f4s), X, Y, Z, T.STORAGE[st], P["rmin"], 3.0, 0.5, T._ptr(Ts), 0, T._ptr(Rs),
+                                     T._ptr(tws), tws.numel(), T._stream()))
         T.blur(vol, P["blur"], out=b)
         T._check(L.tsf_vector_field(T._ptr(b), X, Y, Z, P["fmax"], P["vsign"], T.STORAGE[st], None, T._ptr(f4), T._stream()))
         rec()
         T._check(L.tsf_gvf_fmg(T._ptr(f4), T._ptr(out), X, Y, Z, 0.2, args.fmg_cycles, T.STORAGE[st], T._ptr(ws), ws.numel(), T._stream()))
         rec()
-        T._check(L.tsf_tdf_circle(T._ptr(out), X, Y, Z, T.STORAGE[st], 2.5, P["rmax"], P["rstep"], T._ptr(Tl), 0, T._ptr(Rl), T._stream()))
+        T._check(L.tsf_tdf_circle_ws(T._ptr(out), X, Y, Z, T.STORAGE[st], 2.5, P["rmax"], P["rstep"], T._ptr(Tl), 0,
+                                     T._ptr(Rl), T._ptr(tws), tws.numel(), T._stream()))
         T.tdf_combine(Ts, Rs, Tl, Rl)
         rec()
         nc, nv = C.c_int64(0), C.c_int64(0)

@@ -226,6 +226,20 @@ int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, 
                         float rmax, float rstep, void *d_T, int tdf_unorm16, float *d_R, int mode,
                         void *stream);
 
+/* Workspace bytes for tsf_tdf_circle_ws: 16 per voxel for the 16-bit storage
+ * formats (an x-paired copy of the field), 0 for F32. */
+size_t tsf_tdf_workspace_size(int X, int Y, int Z, int storage);
+
+/* tsf_tdf_circle with a workspace (same reference interface, same results bit
+ * for bit): for 16-bit storage the call first writes an x-paired copy of the
+ * field into the workspace (entry i = texel i and texel i + 1), so that a
+ * trilinear sample inside the volume takes four 16-byte loads instead of eight
+ * 8-byte ones.  With a smaller or misaligned workspace (16-byte alignment) it
+ * behaves as tsf_tdf_circle. */
+int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
+                      float rstep, void *d_T, int tdf_unorm16, float *d_R, void *d_workspace,
+                      size_t workspace_bytes, void *stream);
+
 /* splineTDF (kernels.cl:1159-1254, kernels_no_3d_write.cl:1574-1671; driver
  * runSplineTDF, tubeDetectionFilters.cpp:4-55, called with
  * max(1.5, radius-min) at tube-segmentation.cpp:785-786): the normalised

@@ -151,6 +151,31 @@ def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm, mode)
     assert np.array_equal(R.cpu().numpy(), oR)
 
 
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)])
+def test_tdf_paired_texels(torch_dev, tsf, oracle, synth, storage, rng_):
+    """tsf_tdf_circle_ws: for 16-bit storage the interior samples read the
+    x-paired copy of the field (four 16-byte loads per sample); T and R are the
+    oracle's bit for bit, and a workspace that is too small or misaligned
+    falls back to the plain path with the same result."""
+    torch = torch_dev
+    shape = (40, 44, 49)
+    field4, _ = _field(oracle, synth, shape, 8, storage)
+    d4 = _to_device_field4(torch, field4, storage)
+    L = tsf.load()
+    need = L.tsf_tdf_workspace_size(shape[2], shape[1], shape[0], tsf.STORAGE[storage])
+    assert need == (0 if storage == "f32" else 16 * field4[..., 0].size)
+    oT, oR = oracle.tdf_circle(field4, *rng_)
+    for unorm in (False, True):
+        for ws in (tsf.workspace(need), tsf.workspace(need + 64)[8:], tsf.workspace(need // 2)):
+            T, R = tsf.tdf_circle(d4, *rng_, storage=storage, unorm16=unorm, ws=ws)
+            if unorm:
+                assert np.array_equal(_u16(T), oracle.to_unorm16(oT))
+            else:
+                assert np.array_equal(T.cpu().numpy(), oT)
+            assert np.array_equal(R.cpu().numpy(), oR)
+
+
 @pytest.mark.parametrize("unorm", [False, True])
 def test_combine(torch_dev, tsf, oracle, unorm):
     torch = torch_dev

@@ -35,7 +35,9 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
             size_t ws_bytes, int mode, cudaStream_t s);
 int launch_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int st, cudaStream_t s);
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode);
+                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, void *ws = nullptr,
+                      size_t ws_bytes = 0);
+size_t tdf_workspace_size(int X, int Y, int Z, int st);
 int launch_tdf_combine(const void *Ts, const float *Rs, void *Tl, float *Rl, int64_t n, int unorm, cudaStream_t s);
 size_t candidates_workspace_size(int X, int Y, int Z);
 size_t compact_workspace_size(int X, int Y, int Z);
@@ -103,6 +105,15 @@ int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int sto
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
                    void *d_T, int tdf_unorm16, float *d_R, void *stream) {
     return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), 0);
+}
+
+size_t tsf_tdf_workspace_size(int X, int Y, int Z, int storage) { return tdf_workspace_size(X, Y, Z, storage); }
+
+int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
+                      void *d_T, int tdf_unorm16, float *d_R, void *d_workspace, size_t workspace_bytes,
+                      void *stream) {
+    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), 0,
+                             d_workspace, workspace_bytes);
 }
 
 // tsf_tdf_circle with the kernel forced (0 = default, 1 = one voxel per lane).

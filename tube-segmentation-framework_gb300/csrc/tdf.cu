@@ -85,11 +85,14 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 constexpr int kSeg = 128;
 constexpr int kTdfWarps = 4;
 
-template <int ST, bool NORM, bool UNORM>
+// PAIR: interior samples read the x-paired copy P of a 16-bit field (one
+// 16-byte load per corner row, sample_linear_pair_in) instead of F.
+template <int ST, bool NORM, bool UNORM, bool PAIR>
 __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                                     float rmin, float rmax, float rstep,
                                                                     const CircleTable tab, void *T,
-                                                                    float *__restrict__ Rout, int fast_ok) {
+                                                                    float *__restrict__ Rout, int fast_ok,
+                                                                    const uint4 *__restrict__ P) {
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
     __shared__ unsigned char sin_[kTdfWarps][kSeg];      // samples stay inside: unclamped sampler
@@ -138,8 +141,13 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                         const float va0 = c * e3x + s * e2x;
                         const float va1 = c * e3y + s * e2y;
                         const float va2 = c * e3z + s * e2z;
-                        const float3 smp =
-                            sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1, fz + radius * va2);
+                        float3 smp;
+                        if constexpr (PAIR)
+                            smp = sample_linear_pair_in<ST>(P, X, XY, fx + radius * va0, fy + radius * va1,
+                                                            fz + radius * va2);
+                        else
+                            smp = sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1,
+                                                       fz + radius * va2);
                         const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
                         rs = rs + dt;
                     }
@@ -186,6 +194,21 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
     }
 }
 
+// The x-paired copy of a 16-bit field4 image: P[i] = (texel i, texel of the
+// next x, clamped at the last column), 16 bytes per voxel.
+__global__ void tdf_pair_kernel(const uint2 *__restrict__ F, uint4 *__restrict__ P, int X, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = (int)(i % X);
+    const uint2 a = __ldg(F + i), b = __ldg(F + i + (x + 1 < X ? 1 : 0));
+    P[i] = make_uint4(a.x, a.y, b.x, b.y);
+}
+
+size_t tdf_workspace_size(int X, int Y, int Z, int st) {
+    if (X <= 0 || Y <= 0 || Z <= 0 || !valid_storage(st) || st == TSF_STORE_F32) return 0;
+    return (size_t)X * Y * Z * sizeof(uint4);
+}
+
 template <bool UNORM>
 __global__ void combine_kernel(const void *__restrict__ Ts, const float *__restrict__ Rs, void *Tl, float *Rl, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,8 +225,10 @@ __global__ void combine_kernel(const void *__restrict__ Ts, const float *__restr
 }
 
 // tdf_mode: 0 = default (load-balanced sweeps), 1 = one voxel per lane.
+// ws / ws_bytes: room for the x-paired copy of a 16-bit field (tdf_workspace_size);
+// without it, or for FP32 storage, the samples read the field itself.
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode) {
+                      void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, void *ws, size_t ws_bytes) {
     int r = check_dims(X, Y, Z);
     if (r) return r;
     if (!d_field4 || !d_T || !d_R) return fail(TSF_ERR_INVALID_ARG, "null buffer");
@@ -214,11 +239,23 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
     const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
     const bool queue = tdf_mode != 1;
     const int fast_ok = (int64_t)X * Y * Z < ((int64_t)1 << 31) - 1;   // 32-bit texel offsets
+    const int64_t n = (int64_t)X * Y * Z;
+    const size_t need = tdf_workspace_size(X, Y, Z, st);
+    const bool pair = queue && fast_ok && need > 0 && ws && ws_bytes >= need &&
+                      (reinterpret_cast<uintptr_t>(ws) & 15) == 0 && (reinterpret_cast<uintptr_t>(d_field4) & 7) == 0;
+    uint4 *P = pair ? static_cast<uint4 *>(ws) : nullptr;
+    if (pair) {
+        tdf_pair_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const uint2 *>(d_field4), P, X, n);
+        TSF_CHECK_LAUNCH("tdf_pair_kernel");
+    }
 #define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
     do {                                                                                                             \
-        if (queue)                                                                                                   \
-            tdf_queue_kernel<ST, NORM, UN><<<qblocks, 32 * kTdfWarps, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, \
-                                                                              tab, d_T, d_R, fast_ok);               \
+        if (queue && pair)                                                                                           \
+            tdf_queue_kernel<ST, NORM, UN, ST != TSF_STORE_F32><<<qblocks, 32 * kTdfWarps, 0, s>>>(                 \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, P);                                    \
+        else if (queue)                                                                                              \
+            tdf_queue_kernel<ST, NORM, UN, false><<<qblocks, 32 * kTdfWarps, 0, s>>>(                               \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, nullptr);                              \
         else                                                                                                         \
             tdf_circle_kernel<ST, NORM, UN><<<g, b, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R);    \
     } while (0)

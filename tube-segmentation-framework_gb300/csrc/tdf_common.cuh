@@ -121,6 +121,44 @@ __device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY,
     return o;
 }
 
+// One stored 16-bit field4 texel (8 bytes) to floats, as Vec4Load does.
+template <int ST> __device__ __forceinline__ float4 unpack_texel(uint32_t lo, uint32_t hi) {
+    using T = typename Store<ST>::T;
+    const uint2 raw = make_uint2(lo, hi);
+    T c[4];
+    memcpy(c, &raw, 8);
+    return make_float4(Store<ST>::load(c[0]), Store<ST>::load(c[1]), Store<ST>::load(c[2]), Store<ST>::load(c[3]));
+}
+
+// sample_linear_in on the x-paired copy of a 16-bit field: entry i holds
+// texel i and texel i + 1 (16 bytes), so each of the four (y, z) corner rows
+// is one 16-byte load instead of two 8-byte loads.  Same texels, weights and
+// sums in the same order, so the same bits as sample_linear_in.
+template <int ST>
+__device__ __forceinline__ float3 sample_linear_pair_in(const uint4 *P, int X, int XY, float u, float v, float w) {
+    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
+    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
+    const float a = uu - fu, b = vv - fv, c = ww - fw;
+    const int base = (int)fu + X * (int)fv + XY * (int)fw;
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
+    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    const uint4 p00 = __ldg(P + base), p10 = __ldg(P + base + X);
+    const uint4 p01 = __ldg(P + base + XY), p11 = __ldg(P + base + XY + X);
+    const float4 t000 = unpack_texel<ST>(p00.x, p00.y), t100 = unpack_texel<ST>(p00.z, p00.w);
+    const float4 t010 = unpack_texel<ST>(p10.x, p10.y), t110 = unpack_texel<ST>(p10.z, p10.w);
+    const float4 t001 = unpack_texel<ST>(p01.x, p01.y), t101 = unpack_texel<ST>(p01.z, p01.w);
+    const float4 t011 = unpack_texel<ST>(p11.x, p11.y), t111 = unpack_texel<ST>(p11.z, p11.w);
+    float3 o;
+    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
+    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
+    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
+    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
+    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
+    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
+    return o;
+}
+
 // Margin m such that every trilinear corner of a sample at distance <= r
 // from a voxel lies within m - 1 voxels of it, for sample directions
 // a = cos e3 + sin e2 with |e2|, |e3| <= 1.00005 and |e2 . e3| <= 1e-3

@@ -265,7 +265,10 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4small.p, S), "vector field");
         Ts.alloc(n * ts);
         Rs.alloc(n * 4);
-        check(tsf_tdf_circle(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), S), "TDF");
+        const size_t twb = tsf_tdf_workspace_size(X, Y, Z, st);
+        DevBuf tws(twb);
+        check(tsf_tdf_circle_ws(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), tws.p, twb, S),
+              "TDF");
         if (rMax < 2.5f) {
             out.T.p = Ts.release();
             out.R.p = Rs.release();
@@ -308,9 +311,13 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
     if (getParamBool(P, "use-spline-tdf"))
         check(tsf_tdf_spline(out.field.p, X, Y, Z, st, std::max(1.5f, rMin), rMax, rStep, out.T.p, tdf16,
                              out.R.as<float>(), S), "spline TDF");
-    else
-        check(tsf_tdf_circle(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
-                             out.R.as<float>(), S), "TDF");
+    else {
+        const size_t twb = tsf_tdf_workspace_size(X, Y, Z, st);
+        DevBuf tws(twb);
+        check(tsf_tdf_circle_ws(out.field.p, X, Y, Z, st, std::max(2.5f, rMin), rMax, rStep, out.T.p, tdf16,
+                                out.R.as<float>(), tws.p, twb, S),
+              "TDF");
+    }
     if (rMin < 2.5f)
         check(tsf_tdf_combine(Ts.p, Rs.as<float>(), out.T.p, out.R.as<float>(), (int64_t)n, tdf16, S), "combine");
 }

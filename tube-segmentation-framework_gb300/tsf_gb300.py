@@ -96,6 +96,8 @@ def _declare(L):
         "tsf_blur_backward_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_blur_backward": (_i, [_p, _p, _i, _i, _i, _f, _p, _p, _p, _sz, _p]),
         "tsf_tdf_circle": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
+        "tsf_tdf_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_tdf_circle_ws": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p, _sz, _p]),
         "tsf_tdf_spline": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _p]),
         "tsf_tdf_combine": (_i, [_p, _p, _p, _p, _i64, _i, _p]),
         "tsf_tdf_circle_mode": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _i, _p, _i, _p]),
@@ -306,11 +308,19 @@ def gvf_finish(v, storage: str = "f32", out=None, stream=None):
 
 
 def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, mode: int = 0,
-               stream=None):
+               stream=None, ws=None):
+    """Circle-fitting TDF.  ws: a workspace of tsf_tdf_workspace_size bytes
+    (tsf_tdf_circle_ws: paired texels for 16-bit storage); mode forces the
+    kernel (tsf_tdf_circle_mode) when ws is None."""
     torch = _torch()
     Z, Y, X = field4.shape[:3]
     T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
     R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
+    if ws is not None:
+        _check(load().tsf_tdf_circle_ws(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
+                                        float(rstep), _ptr(T), int(unorm16), _ptr(R), _ptr(ws), ws.numel(),
+                                        _stream(stream)))
+        return T, R
     _check(load().tsf_tdf_circle_mode(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
                                       float(rstep), _ptr(T), int(unorm16), _ptr(R), int(mode), _stream(stream)))
     return T, R
