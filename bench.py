@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--fmg-cycles", type=int, default=10)
     ap.add_argument("--adjoint", action="store_true",
                     help="time the forward + adjoint (gradient) pass alone and print its JSON line")
-    ap.add_argument("--stage", choices=["spline", "circle", "segment", "crop"],
+    ap.add_argument("--stage", choices=["spline", "circle", "segment", "crop", "gvf"],
                     help="time one stage alone and print its JSON line (a small, self-contained command for "
                          "kernel profiles): a TDF on the vessel-tree field after --iters GVF iterations, the "
                          "segmentation of that step's centerlines, or the lung cropping of the 512x512x400 CT")
@@ -609,7 +609,9 @@ def run_stage(args):
     max(2.5, rmin), both to the workload's rmax; circle is timed without and
     with the paired-texel workspace).  segment: one pipeline step
     with --iters GVF iterations, then segmentation_timing.  crop:
-    crop_timing on the 512x512x400 lung CT."""
+    crop_timing on the 512x512x400 lung CT.  gvf: the streaming and the
+    register-vector GVF kernels (tsf_gvf_mode 0, 1) timed over --iters
+    iterations."""
     import torch
     import synthetic
     import tsf_gb300 as T
@@ -628,6 +630,21 @@ def run_stage(args):
     vol = torch.from_numpy(synthetic.vascular_tree((n, n, n), seed=args.seed)).cuda()
     b = T.blur(vol, P["large_blur"])
     f0, _ = T.vector_field(b, P["fmax"], P["vsign"], storage=st)
+    if args.stage == "gvf":
+        # each GVF kernel choice: one warm-up call of --iters iterations, then one timed call
+        out = {"stage": "gvf", "workload": "vessel tree %d^3, %s storage, %d iterations per call" % (n, st, args.iters)}
+        ws = T.workspace(T.load().tsf_gvf_workspace_size(n, n, n, T.STORAGE[st]))
+        for mode, name in ((0, "streaming"), (1, "register_vector")):
+            v = f0.clone()
+            T.gvf(f0, args.mu, args.iters, st, v=v, ws=ws, mode=mode)
+            torch.cuda.synchronize()
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            T.gvf(f0, args.mu, args.iters, st, v=v, ws=ws, mode=mode)
+            e.record()
+            torch.cuda.synchronize()
+            out[name + "_us_per_iteration"] = round(a.elapsed_time(e) * 1e3 / args.iters, 2)
+        return out
     v = T.gvf(f0, args.mu, args.iters, storage=st)
     field = T.gvf_finish(v, storage=st)
     runs = {}

@@ -64,16 +64,18 @@ def test_vector_field_bitexact(torch_dev, tsf, oracle, synth, storage, vsign):
 
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("mu,iters", [(0.05, 17), (0.1, 8)])
-@pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130), (9, 10, 256)])
+@pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130), (9, 10, 256),
+                                   (19, 37, 136), (5, 32, 128), (21, 50, 264)])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape, mode):
     """mode 0: the z-streaming TMA kernel wherever rows are a multiple of 16
     bytes -- tiles shifted back inside at the +x / +y edges (X = 136, 264;
     Y = 9, 22), rows shorter than a tile (X = 8, 40), z ranges split into
     several chunks (Z = 19, 35), the thinnest volumes (Z = 5); X = 33 and, for
-    the 16-bit formats, X = 130 take the other kernels.  mode 1: the
-    register-vector kernel (16- or 8-byte vectors, ragged last warps) or, for
-    odd rows, the one-thread-per-voxel kernel."""
+    the 16-bit formats, X = 130 take the other kernels; taller volumes
+    (Y = 32, 37, 50) cover several row tiles, the last shifted back inside.
+    mode 1: the register-vector kernel (16- or 8-byte vectors, ragged last
+    warps) or, for odd rows, the one-thread-per-voxel kernel."""
     torch = torch_dev
     vol = oracle.blur(_vol(synth, shape, 4), 0.5)
     ref4 = oracle.vector_field(vol, 0.2, 1, storage)
@@ -87,16 +89,19 @@ def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape, 
     assert np.array_equal(_np_stored(f4, storage), oracle.gvf_finish(ov, storage))
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_gvf_modes_identical(torch_dev, tsf, synth, oracle, storage):
-    """The register-vector kernel (mode 1) and the streaming kernel (mode 2)
-    give the same bits."""
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("shape", [(40, 36, 44), (30, 48, 160)])
+def test_gvf_modes_identical(torch_dev, tsf, synth, oracle, storage, shape):
+    """The register-vector kernel (mode 1) and the streaming kernel (modes 0
+    and 2) give the same bits."""
     torch = torch_dev
-    vol = oracle.blur(_vol(synth, (40, 36, 44), 5), 0.5)
+    vol = oracle.blur(_vol(synth, shape, 5), 0.5)
     p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
     a = tsf.gvf(p, 0.05, 23, storage, mode=1)
     b = tsf.gvf(p, 0.05, 23, storage, mode=2)
-    assert torch.equal(a, b)
+    c = tsf.gvf(p, 0.05, 23, storage, mode=0)
+    assert torch.equal(a, b) and torch.equal(a, c)
+    assert tsf.gvf_device_error() == 0
 
 
 def test_gvf_minimum_extent(torch_dev, tsf, oracle):
