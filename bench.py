@@ -783,9 +783,10 @@ def run_reference(args):
 
 
 def run_accuracy(args):
-    """GVF field, TDF and centerpoint agreement of the GPU path for each storage
-    format against the FP64 oracle run of the same method (same volume, same
-    parameters).  TDF errors are absolute (T is in [0, 1])."""
+    """GVF field, TDF, centerpoint, centerline and segmentation agreement of the
+    GPU path for each storage format against the FP64 oracle run of the same
+    method (same volume, same parameters).  TDF errors are absolute (T is in
+    [0, 1])."""
     import torch
     import oracle as O
     import synthetic
@@ -806,9 +807,18 @@ def run_accuracy(args):
     Tl64, Rl64 = O.tdf_circle(field64, max(2.5, P["rmin"]), P["rmax"], P["rstep"], f64=True)
     T64, R64 = O.combine(Ts64, Rs64, Tl64, Rl64, f64=True)
     ref = O.centerpoints(T64, R64, field64, P["tdf_high"], P["cube_size"], f64=True)
+    # linking (Synthetic-Vascusynth: min-mean-tdf 0.3, max-distance 10, min-tree-length 3)
+    # and inverse-gradient segmentation of the FP64 method's results
+    e64, l64, s64 = O.link_centerpoints(ref["vertices"], T64.astype(np.float32), 0.3, 10.0)
+    cl64 = O.rasterize_trees(ref["vertices"], e64, l64, s64, 3, shape)
+    seg64, _ = O.segment_inverse_gradient(cl64, field64.astype(np.float32), R64.astype(np.float32))
     t_oracle = time.perf_counter() - t0
     out = {"size": n, "iterations": args.iters, "mu": args.mu, "oracle_s": round(t_oracle, 1),
-           "fp64_vertices": int(len(ref["vertices"]))}
+           "fp64_vertices": int(len(ref["vertices"])), "fp64_centerline_voxels": int(cl64.sum()),
+           "fp64_segmented_voxels": int(seg64.sum()),
+           "note": "linking, rasterisation and segmentation of the FP64 method's TDF, radius and field run in the "
+                   "oracle's float restatement; Dice = 2|A and B| / (|A| + |B|)"}
+    dice = lambda a, b: round(2.0 * float(np.logical_and(a, b).sum()) / max(1.0, float(a.sum() + b.sum())), 6)
     vset = set(map(tuple, ref["vertices"].tolist()))
     for st in ("f32", "f16", "bf16", "snorm16"):
         pipe = Pipeline(T, torch, shape, st, args.iters, args.mu)
@@ -829,6 +839,13 @@ def run_accuracy(args):
                    "vertices": int(len(gset)), "vertices_equal_fp64": inter,
                    "vertex_jaccard": round(inter / max(1, len(vset | gset)), 5),
                    "same_vertex_list": bool(np.array_equal(got, ref["vertices"]))}
+        dv = pipe.verts[: min(pipe.last["n_vertices"], pipe.max_vertices)].contiguous()
+        edges, labels, sizes = T.link_centerpoints(dv, pipe.Tl, 0.3, 10.0)
+        cl = T.rasterize_trees(dv, edges, labels, sizes, 3, shape)
+        seg, _ = T.segment_inverse_gradient(cl, pipe.field, pipe.Rl, storage=st)
+        cl, seg = cl.cpu().numpy() != 0, seg.cpu().numpy() != 0
+        out[st]["centerline_dice"] = dice(cl, cl64 != 0)
+        out[st]["segmentation_dice"] = dice(seg, seg64 != 0)
         del pipe
         torch.cuda.empty_cache()
     return out
