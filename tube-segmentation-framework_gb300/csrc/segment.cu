@@ -76,60 +76,121 @@ __global__ void seg_init_kernel(const int8_t *__restrict__ cl, const float *__re
             }
 }
 
-// grow, deciding half: acc[X] = 1 if X (at 2) accepts, mark[Y] = 1 for the
-// neighbours it marks; *any = 1 if anything was accepted
-template <int ST>
-__global__ void seg_decide_kernel(const int8_t *__restrict__ state, const void *__restrict__ F, const Dirs26 dirs,
-                                  int8_t *__restrict__ acc, int8_t *__restrict__ mark, int *__restrict__ any, int X,
-                                  int Y, int Z) {
-    SEG_XYZ(X, Y, Z);
-    const int64_t i = lin(x, y, z, X, Y);
-    if (state[i] != 2) return;
-    const float wx = Vec4Load<ST>::load(F, i).w;
-    bool grew = false;
-    for (int k = 0; k < 26; k++) {
-        const int yx = x + dirs.o[k][0], yy = y + dirs.o[k][1], yz = z + dirs.o[k][2];
-        const int64_t j = lin(clampi(yx, X), clampi(yy, Y), clampi(yz, Z), X, Y);
-        if (state[j] == 1) continue;
-        float4 fy = Vec4Load<ST>::load(F, j);
-        fy.x /= fy.w;
-        fy.y /= fy.w;
-        fy.z /= fy.w;
-        if (!(fy.w > wx)) continue;
-        float best = -2.0f;
-        int bk = 0;
-        for (int m = 0; m < 26; m++) {
-            const float v = (fy.x * dirs.d[m][0] + fy.y * dirs.d[m][1]) + fy.z * dirs.d[m][2];
-            if (v > best) {
-                best = v;
-                bk = m;
-            }
-        }
-        // Z = Y + o[bk] is X  <=>  o[bk] = -o[k]
-        if (bk != 25 - k) continue;
-        if (yx < 0 || yy < 0 || yz < 0 || yx >= X || yy >= Y || yz >= Z) continue;
-        mark[lin(yx, yy, yz, X, Y)] = 1;
-        grew = true;
-    }
-    if (grew) {
-        acc[i] = 1;
-        *any = 1;
+// The voxels at 2 form the front, kept as a list of linear indices so that an
+// iteration costs the front, not the volume.  Front entries are unique: the
+// initial list is a compaction of the state, and a voxel enters the next list
+// only with the first mark it receives (an atomic OR on the mark byte's word).
+
+// Warp-aggregated append of index i (when `take`) to list / *cnt.
+__device__ __forceinline__ void seg_append(bool take, int64_t i, int64_t *list, unsigned long long *cnt) {
+    const unsigned full = 0xffffffffu;
+    const unsigned m = __ballot_sync(full, take);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (unsigned long long)__popc(m));
+    base = __shfl_sync(full, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// the initial front: every voxel at 2, in any order
+__global__ void seg_front_init_kernel(const int8_t *__restrict__ state, int64_t n, int64_t *__restrict__ front,
+                                      unsigned long long *__restrict__ cnt) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // whole warps stay in the loop so that the ballots see every lane
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x; b < n; b += stride) {
+        const int64_t i = b + threadIdx.x;
+        seg_append(i < n && state[i] == 2, i, front, cnt);
     }
 }
 
-// grow, applying half (and clearing acc / mark for the next iteration)
-__global__ void seg_apply_kernel(int8_t *__restrict__ state, int8_t *__restrict__ acc, int8_t *__restrict__ mark,
-                                 int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int8_t s = state[i];
-    int8_t t;
-    if (s == 1 || acc[i]) t = 1;
-    else if (mark[i]) t = 2;
-    else t = 0;
-    state[i] = t;
-    acc[i] = 0;
-    mark[i] = 0;
+// grow, deciding half, one warp per front voxel X, lane k < 26 its neighbour
+// k: acc[X] = 1 if X accepts; each marked neighbour Y gets mark[Y] = 1 and,
+// on its first mark, a place in the next front; *any = 1 if anything was
+// accepted.  Decisions read only the iteration's starting state, so the order
+// of the list changes nothing.
+template <int ST>
+__global__ void seg_front_decide_kernel(const int8_t *__restrict__ state, const void *__restrict__ F,
+                                        const Dirs26 dirs, int8_t *__restrict__ acc, int8_t *mark,
+                                        const int64_t *__restrict__ front, const unsigned long long *__restrict__ nfront,
+                                        int64_t *__restrict__ next, unsigned long long *__restrict__ nnext,
+                                        int *__restrict__ any, int X, int Y, int Z) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t nf = (int64_t)*nfront;
+    const int64_t plane = (int64_t)X * Y;
+    for (int64_t f = (((int64_t)blockIdx.x * blockDim.x) + threadIdx.x) >> 5; f < nf; f += warps) {
+        const int64_t i = front[f];
+        if (state[i] != 2) continue;                       // warp-uniform
+        const int z = (int)(i / plane), y = (int)((i - (int64_t)z * plane) / X), x = (int)(i - (int64_t)z * plane - (int64_t)y * X);
+        const float wx = Vec4Load<ST>::load(F, i).w;
+        bool grew = false, marked_first = false;
+        int64_t yj = 0;
+        if (lane < 26) {
+            const int k = lane;
+            const int yx = x + dirs.o[k][0], yy = y + dirs.o[k][1], yz = z + dirs.o[k][2];
+            const int64_t j = lin(clampi(yx, X), clampi(yy, Y), clampi(yz, Z), X, Y);
+            if (state[j] != 1) {
+                float4 fy = Vec4Load<ST>::load(F, j);
+                fy.x /= fy.w;
+                fy.y /= fy.w;
+                fy.z /= fy.w;
+                if (fy.w > wx) {
+                    float best = -2.0f;
+                    int bk = 0;
+                    for (int m = 0; m < 26; m++) {
+                        const float v = (fy.x * dirs.d[m][0] + fy.y * dirs.d[m][1]) + fy.z * dirs.d[m][2];
+                        if (v > best) {
+                            best = v;
+                            bk = m;
+                        }
+                    }
+                    // Z = Y + o[bk] is X  <=>  o[bk] = -o[k]; accepted only through Y inside
+                    if (bk == 25 - k && yx >= 0 && yy >= 0 && yz >= 0 && yx < X && yy < Y && yz < Z) {
+                        grew = true;
+                        yj = lin(yx, yy, yz, X, Y);
+                        unsigned *word = reinterpret_cast<unsigned *>(mark + (yj & ~(int64_t)3));
+                        const unsigned bit = 1u << (8 * (int)(yj & 3));
+                        marked_first = (atomicOr(word, bit) & bit) == 0;
+                    }
+                }
+            }
+        }
+        seg_append(marked_first, yj, next, nnext);
+        if (__ballot_sync(full, grew) && lane == 0) {
+            acc[i] = 1;
+            *any = 1;
+        }
+    }
+}
+
+// grow, applying half 1: the front's own verdicts (accepted -> 1, else 0)
+__global__ void seg_front_apply_kernel(int8_t *__restrict__ state, int8_t *__restrict__ acc,
+                                       const int64_t *__restrict__ front, const unsigned long long *__restrict__ nfront) {
+    const int64_t nf = (int64_t)*nfront;
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nf; f += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = front[f];
+        if (state[i] != 2) continue;
+        state[i] = acc[i] ? 1 : 0;
+        acc[i] = 0;
+    }
+}
+
+// grow, applying half 2: the marked voxels go to 2 unless accepted (the
+// precedence accepted > to check > dropped); their list is the next front.
+// Clears the marks, and the count of the front just applied (that list holds
+// the next iteration's marks).
+__global__ void seg_mark_apply_kernel(int8_t *__restrict__ state, int8_t *mark, const int64_t *__restrict__ next,
+                                      const unsigned long long *__restrict__ nnext,
+                                      unsigned long long *__restrict__ nfront) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *nfront = 0;
+    const int64_t nn = (int64_t)*nnext;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < nn; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = next[g];
+        mark[j] = 0;
+        if (state[j] != 1) state[j] = 2;
+    }
 }
 
 // dilate: out (zeroed) = 1 on the 3x3x3 neighbourhood of every voxel at 1
@@ -188,7 +249,8 @@ constexpr int kGrowBatch = 8;
 
 size_t segment_workspace_size(int X, int Y, int Z) {
     const size_t n = (size_t)X * Y * Z;
-    return 3 * al256(n) + al256(kGrowBatch * sizeof(int));
+    // state, acc, mark (int8); two front lists (int64); two counts; the batch's accept flags
+    return 3 * al256(n) + 2 * al256(n * sizeof(int64_t)) + 256 + al256(kGrowBatch * sizeof(int));
 }
 
 static dim3 seg_block() { return dim3(32, 4, 2); }
@@ -202,26 +264,35 @@ int run_segment_inverse_gradient(const int8_t *cl, const void *F, int st, const 
     if (!cl || !F || !radius || !out) return fail(TSF_ERR_INVALID_ARG, "null buffer");
     if (!ws || ws_bytes < segment_workspace_size(X, Y, Z))
         return fail(TSF_ERR_WORKSPACE, "segmentation workspace too small");
+    if ((reinterpret_cast<uintptr_t>(ws) & 7) != 0) return fail(TSF_ERR_INVALID_ARG, "workspace must be 8-byte aligned");
     const int64_t n = (int64_t)X * Y * Z;
     char *w = (char *)ws;
     int8_t *state = (int8_t *)w, *acc = (int8_t *)(w + al256(n)), *mark = (int8_t *)(w + 2 * al256(n));
-    int *flags = (int *)(w + 3 * al256(n));
+    int64_t *lists[2] = {(int64_t *)(w + 3 * al256(n)),
+                         (int64_t *)(w + 3 * al256(n) + al256(n * sizeof(int64_t)))};
+    unsigned long long *cnt = (unsigned long long *)(w + 3 * al256(n) + 2 * al256(n * sizeof(int64_t)));
+    int *flags = (int *)((char *)cnt + 256);
     const Dirs26 dirs = host_dirs26();
     TSF_TRY_CUDA(cudaMemcpyAsync(state, cl, (size_t)n, cudaMemcpyDeviceToDevice, s));
     TSF_TRY_CUDA(cudaMemsetAsync(acc, 0, 2 * al256(n), s));
+    TSF_TRY_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), s));
     seg_init_kernel<<<seg_grid(X, Y, Z), seg_block(), 0, s>>>(cl, radius, state, X, Y, Z);
-    TSF_CHECK_LAUNCH("seg_init_kernel");
-    const unsigned nb = (unsigned)((n + 255) / 256);
+    const unsigned gblocks = 8 * 152;
+    seg_front_init_kernel<<<gblocks, 256, 0, s>>>(state, n, lists[0], cnt);
+    TSF_CHECK_LAUNCHES("seg_init/front_init", 2);
+    int p = 0;                                            // lists[p] holds the front
     int64_t it = 0;
     for (;;) {
         TSF_TRY_CUDA(cudaMemsetAsync(flags, 0, kGrowBatch * sizeof(int), s));
         for (int b = 0; b < kGrowBatch; b++) {
             TSF_DISPATCH_STORAGE(st, ST, {
-                seg_decide_kernel<ST>
-                    <<<seg_grid(X, Y, Z), seg_block(), 0, s>>>(state, F, dirs, acc, mark, flags + b, X, Y, Z);
+                seg_front_decide_kernel<ST><<<gblocks, 256, 0, s>>>(state, F, dirs, acc, mark, lists[p], cnt + p,
+                                                                    lists[1 - p], cnt + (1 - p), flags + b, X, Y, Z);
             });
-            seg_apply_kernel<<<nb, 256, 0, s>>>(state, acc, mark, n);
-            TSF_CHECK_LAUNCHES("seg_decide/apply", 2);
+            seg_front_apply_kernel<<<gblocks, 256, 0, s>>>(state, acc, lists[p], cnt + p);
+            seg_mark_apply_kernel<<<gblocks, 256, 0, s>>>(state, mark, lists[1 - p], cnt + (1 - p), cnt + p);
+            TSF_CHECK_LAUNCHES("seg_decide/apply", 3);
+            p = 1 - p;
         }
         int h[kGrowBatch];
         TSF_TRY_CUDA(cudaMemcpyAsync(h, flags, sizeof(h), cudaMemcpyDeviceToHost, s));
