@@ -15,7 +15,8 @@
  * specification.  What is pinned: the eigen-solver against numpy's eigh, the
  * HP traversal order against a key sort, the storage conversions against
  * numpy, and the end-to-end centerpoint quality on the reference's own
- * synthetic test volume (tests/data/synthetic/dataset_1) when it is present.
+ * synthetic test volume (tests/data/synthetic/dataset_1) when it is present,
+ * and the whole run() chain passes the reference's system-test gates there.
  *
  * Every routine exists in two precisions: suffix _f32 (float arithmetic, the
  * same operation order as the CUDA kernels, compiled with -ffp-contract=off)
