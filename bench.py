@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
+    ap.add_argument("--mra", action="store_true",
+                    help="instead of the default workload: the 512^3 MRA-like volume, 1000 GVF iterations in FP16 "
+                         "storage -- the full pipeline step, and forward + adjoint with memory-budgeted checkpointing")
     ap.add_argument("--adjoint", action="store_true",
                     help="time the forward + adjoint (gradient) pass alone and print its JSON line")
     ap.add_argument("--stage", choices=["spline", "circle", "segment", "crop", "gvf"],
@@ -671,6 +674,66 @@ def run_stage(args):
     return out
 
 
+def run_mra(args):
+    """The MRA-like workload (bright tubes of radii 5 -> 0.8 on 0.1, Rician
+    noise sigma 0.08; 512^3, FP16 field storage, 1000 GVF iterations): the
+    full hot-path step (CUDA events over one step after one warm-up), then the
+    forward + hand-written adjoint of mean((TDF - G)^2) in the same storage
+    (straight-through rounding) with the checkpoint interval chosen against
+    60 % of the free device memory -- the full tape (1000 states) would not
+    fit, the checkpointed one must."""
+    import torch
+    import synthetic
+    import tsf_gb300 as T
+    import calibration as CAL
+    n = 512 if args.size == 256 else args.size
+    K = 1000 if args.iters == 500 else args.iters
+    st = "f16" if args.storage == "f16" else args.storage
+    shape = (n, n, n)
+    vol = synthetic.mra_tree(shape, seed=args.seed)
+    out = {"workload": "MRA-like %d^3, Rician noise, %s storage, GVF %d iterations" % (n, st, K)}
+    pipe = Pipeline(T, torch, shape, st, K, args.mu)
+    pipe.vol.copy_(torch.from_numpy(vol))
+    pipe.step()
+    torch.cuda.synchronize()
+    evs = []
+    pipe.step(evs)
+    torch.cuda.synchronize()
+    stages = {name: round(evs[i - 1][1].elapsed_time(evs[i][1]), 3) for i, (name, _) in enumerate(evs) if i > 0}
+    total = evs[0][1].elapsed_time(evs[-1][1])
+    out["step"] = {"ms": round(total, 3), "volumes_per_s": round(1000.0 / total, 4), "stages_ms": stages,
+                   "gvox_iter_s": round(n ** 3 * K / (stages.get("gvf", total) * 1e-3) / 1e9, 1),
+                   "n_vertices": int(pipe.last["n_vertices"])}
+    vol_d = pipe.vol.clone()
+    del pipe
+    torch.cuda.empty_cache()
+    state_bytes = 3 * n ** 3 * T.load().tsf_storage_bytes(T.STORAGE[st])
+    p = CAL.Params(mu=args.mu, sigma=PARAMS["large_blur"], iterations=K, fmax=PARAMS["fmax"], rmin=PARAMS["rmin"],
+                   rmax=PARAMS["rmax"], rstep=PARAMS["rstep"], storage=st)
+    G = torch.zeros_like(vol_d)
+    Tc, state = CAL.forward(vol_d, p)                     # allocates the adjoint workspace once
+    CAL.backward(state, ((2.0 / vol_d.numel()) * (Tc - G)).contiguous(), p)
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e[0].record()
+    Tc, state = CAL.forward(vol_d, p, reuse=state)
+    e[1].record()
+    torch.cuda.synchronize()
+    e[2].record()
+    Tc, state = CAL.forward(vol_d, p, reuse=state)
+    gI, dmu, dsig = CAL.backward(state, ((2.0 / Tc.numel()) * (Tc - G)).contiguous(), p)
+    e[3].record()
+    torch.cuda.synchronize()
+    fwd, both = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    C = state["checkpoint_every"]
+    out["fwd_adjoint"] = {"storage": st, "iterations": K, "checkpoint_every": C,
+                          "adjoint_workspace_gb": round(state["gvf_ws"].numel() / 1e9, 2),
+                          "full_tape_gb": round(K * state_bytes / 1e9, 1),
+                          "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
+                          "dmu": float(dmu), "dsigma": float(dsig), "grad_finite": bool(torch.isfinite(gI).all())}
+    return out
+
+
 def run_adjoint(args):
     """Forward + adjoint timing alone on the vessel-tree volume (the same
     measurement the default run reports under fwd_adjoint)."""
@@ -953,6 +1016,9 @@ def main():
         return
     if args.adjoint:
         print(json.dumps(run_adjoint(args)))
+        return
+    if args.mra:
+        print(json.dumps(run_mra(args)))
         return
     if args.stage:
         print(json.dumps(run_stage(args)))

@@ -12,7 +12,9 @@ Backward: the library's adjoints (tsf_tdf_circle_backward at the forward's
 arg-max radii, tsf_gvf_adjoint with memory-budgeted checkpointing,
 tsf_vector_field_backward, tsf_blur_backward) give
 dL/dI, dL/dmu and dL/dsigma; torch is only the glue (elementwise products and
-the combine mask).  FP32 storage and arithmetic.
+the combine mask).  FP32 arithmetic; the fields are stored in FP32 or, with
+Params.storage, a 16-bit format (the adjoints then treat the rounding as the
+identity, straight through).
 """
 from __future__ import annotations
 
@@ -24,14 +26,16 @@ import tsf_gb300 as T
 class Params:
     """checkpoint_every: GVF adjoint checkpoint interval; 0 = the smallest
     interval whose workspace fits in 60 % of the free device memory (1, no
-    recomputation, whenever all states fit), else sqrt(K)."""
+    recomputation, whenever all states fit), else sqrt(K).  storage: the
+    fields' storage format ("f32", "f16", "bf16", "snorm16")."""
 
     def __init__(self, mu=0.05, sigma=0.5, iterations=300, fmax=0.2, vsign=1, rmin=1.0, rmax=7.0, rstep=0.5,
-                 checkpoint_every=0):
+                 checkpoint_every=0, storage="f32"):
         self.mu, self.sigma, self.iterations = mu, sigma, iterations
         self.fmax, self.vsign = fmax, vsign
         self.rmin, self.rmax, self.rstep = rmin, rmax, rstep
         self.checkpoint_every = checkpoint_every
+        self.storage = storage
 
 
 def forward(vol, p: Params, reuse=None):
@@ -39,7 +43,7 @@ def forward(vol, p: Params, reuse=None):
     previous state whose GVF adjoint workspace (possibly ~100 GB) is taken
     over when the size matches, so repeated calls do not allocate."""
     import torch
-    st = "f32"
+    st = p.storage
     s = {}
     _, f_s = T.vector_field(vol, p.fmax, p.vsign, st, planar=False, field4=True)
     Ts, Rs = T.tdf_circle(f_s, p.rmin, 3.0, 0.5, st)
@@ -69,7 +73,7 @@ def backward(state, gT, p: Params, mark=None):
     """dL/dI (tensor), dL/dmu, dL/dsigma for dL/dT = gT.  mark(name), if
     given, is called after each stage (timing)."""
     import torch
-    st = "f32"
+    st = p.storage
     mark = mark or (lambda name: None)
     vol = state["vol"]
     small = state["small"]
