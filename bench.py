@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
+    ap.add_argument("--calibrate", action="store_true",
+                    help="instead of the default workload: the differentiation configuration (192^3 vessel tree, "
+                         "300 GVF iterations, checkpoint every 17, FP32) -- timing, dL/dmu against an FP64 central "
+                         "difference, and 20 Adam steps on mu and the blur sigma")
     ap.add_argument("--mra", action="store_true",
                     help="instead of the default workload: the 512^3 MRA-like volume, 1000 GVF iterations in FP16 "
                          "storage -- the full pipeline step, and forward + adjoint with memory-budgeted checkpointing")
@@ -674,6 +678,86 @@ def run_stage(args):
     return out
 
 
+def run_calibrate(args):
+    """The differentiation configuration: 192^3 vessel tree (the 128^3
+    generator), loss mean((TDF - G)^2) against the generator's Gaussian
+    centerline map (sigma 1), adjoint of 300 GVF iterations with a checkpoint
+    every 17, FP32.  Reports forward and forward + adjoint times, dL/dmu
+    against a central difference of the FP64 oracle of the same method (with
+    the step halved until the difference is smooth: slopes and curvatures at h
+    and 2h agree), and 20 Adam steps on (mu, sigma)."""
+    import torch
+    import synthetic
+    import calibration as CAL
+    import oracle as O
+    n = 192 if args.size == 256 else args.size
+    K = 300 if args.iters == 500 else args.iters
+    shape = (n, n, n)
+    vol, truth = synthetic.vascular_tree(shape, seed=args.seed, with_truth=True)
+    G = synthetic.centerline_gaussian(shape, truth["points"], 1.0)
+    mk = lambda: CAL.Params(mu=args.mu, sigma=PARAMS["large_blur"], iterations=K, fmax=PARAMS["fmax"],
+                            rmin=PARAMS["rmin"], rmax=PARAMS["rmax"], rstep=PARAMS["rstep"], checkpoint_every=17)
+    p = mk()
+    vd, Gd = torch.from_numpy(vol).cuda(), torch.from_numpy(G).cuda()
+    L, gI, dmu, dsig, state = CAL.loss_and_grad(vd, Gd, p)          # warm-up, allocates the workspace
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    e[0].record()
+    CAL.forward(vd, p, reuse=state)
+    e[1].record()
+    torch.cuda.synchronize()
+    e[2].record()
+    L, gI, dmu, dsig, state = CAL.loss_and_grad(vd, Gd, p, state)
+    e[3].record()
+    torch.cuda.synchronize()
+    fwd, both = e[0].elapsed_time(e[1]), e[2].elapsed_time(e[3])
+    out = {"workload": "vessel tree %d^3, GVF %d iterations (checkpoint every 17), FP32, loss mean((TDF - G)^2)"
+                       % (n, K),
+           "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
+           "loss": L, "dmu": dmu, "dsigma": dsig, "grad_volume_finite": bool(torch.isfinite(gI).all())}
+    del state
+    torch.cuda.empty_cache()
+
+    vol64 = vol.astype(np.float64)
+    fs = O.vector_field(vol64, PARAMS["fmax"], PARAMS["vsign"], "f32", f64=True)
+    Ts64, _ = O.tdf_circle(fs, PARAMS["rmin"], 3.0, 0.5, f64=True)
+    f4 = O.vector_field(O.blur(vol, PARAMS["large_blur"], f64=True), PARAMS["fmax"], PARAMS["vsign"], "f32", f64=True)
+
+    def Lo(dm):
+        mu = float(np.float32(args.mu + dm))
+        F = O.gvf_finish(O.gvf(f4, mu, K, f64=True), f64=True)
+        Tl, _ = O.tdf_circle(F, max(2.5, PARAMS["rmin"]), PARAMS["rmax"], PARAMS["rstep"], f64=True)
+        T64 = np.where(Tl < Ts64, Ts64, Tl)
+        return float(((T64 - G) ** 2).mean())
+
+    t0 = time.perf_counter()
+    f0 = Lo(0.0)
+    fd, used = None, None
+    for h in (1e-4, 2.5e-5):
+        fp, fm, fp2, fm2 = Lo(h), Lo(-h), Lo(2 * h), Lo(-2 * h)
+        d1, d2 = (fp - fm) / (2 * h), (fp2 - fm2) / (4 * h)
+        c1, c2 = (fp + fm - 2 * f0) / (h * h), (fp2 + fm2 - 2 * f0) / (4 * h * h)
+        smooth = abs(d1 - d2) <= 1e-3 * max(abs(d1), 1e-9) and abs(c1 - c2) <= 0.05 * max(abs(c1), abs(c2)) + \
+            1e-13 * max(1.0, abs(f0)) / (h * h)
+        fd, used = d1, {"h": h, "smooth": bool(smooth), "d_h": d1, "d_2h": d2}
+        if smooth:
+            break
+    out["dmu_fp64_central_difference"] = fd
+    out["dmu_fd_detail"] = used
+    out["dmu_rel_err"] = abs(dmu - fd) / max(abs(fd), 1e-30)
+    out["fd_oracle_s"] = round(time.perf_counter() - t0, 1)
+
+    p = mk()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p, hist = CAL.calibrate(vd, Gd, p, steps=20)
+    torch.cuda.synchronize()
+    out["adam"] = {"steps": 20, "s_per_step": round((time.perf_counter() - t0) / 21, 4),
+                   "loss_first": hist[0]["loss"], "loss_last": hist[-1]["loss"],
+                   "mu": [hist[0]["mu"], p.mu], "sigma": [hist[0]["sigma"], p.sigma]}
+    return out
+
+
 def run_mra(args):
     """The MRA-like workload (bright tubes of radii 5 -> 0.8 on 0.1, Rician
     noise sigma 0.08; 512^3, FP16 field storage, 1000 GVF iterations): the
@@ -1019,6 +1103,9 @@ def main():
         return
     if args.mra:
         print(json.dumps(run_mra(args)))
+        return
+    if args.calibrate:
+        print(json.dumps(run_calibrate(args)))
         return
     if args.stage:
         print(json.dumps(run_stage(args)))
