@@ -30,11 +30,11 @@ def test_cpp_api_cpu_checks(api_tests):
     assert " 0 failures" in out.stdout
 
 
-def _write_mhd(path, vol_u8):
+def _write_mhd(path, vol_u8, element="MET_UCHAR"):
     Z, Y, X = vol_u8.shape
     with open(path + ".mhd", "w") as f:
-        f.write("ObjectType = Image\nNDims = 3\nDimSize = %d %d %d\nElementType = MET_UCHAR\n"
-                "ElementDataFile = %s.raw\n" % (X, Y, Z, os.path.basename(path)))
+        f.write("ObjectType = Image\nNDims = 3\nDimSize = %d %d %d\nElementType = %s\n"
+                "ElementDataFile = %s.raw\n" % (X, Y, Z, element, os.path.basename(path)))
     vol_u8.tofile(path + ".raw")
 
 
@@ -64,6 +64,38 @@ def _read_vtk(path):
     nl = int(lines[k + 1].split()[1])
     edges = np.array([list(map(int, l.split()))[1:] for l in lines[k + 2:k + 2 + nl]], np.int32).reshape(-1, 2)
     return pts, edges
+
+
+@pytest.mark.gpu
+def test_run_aaa_preset(api_tests, oracle, synth, tmp_path):
+    """run() with the AAA-Vessels-CT preset on an int16 volume (no cropping
+    option): the preset's fixed in-plane crop (15 % of x and y per side, then
+    multiples of 4; the shift vector stays zero as in the reference), toFloat
+    with minimum 50 / maximum 150, blur 2, the vector field (fmax 0.3), the
+    multigrid GVF (10 cycles, mu 0.2) and the spline TDF from max(1.5, 3.5) to
+    90 in steps of 1, in the 16-bit mode -- the TDF equals the oracle's."""
+    pytest.importorskip("torch")
+    rng = np.random.default_rng(4)
+    vol = synth.vascular_tree((40, 64, 72), seed=12)
+    hu = np.round(vol * 180.0 + rng.normal(scale=8.0, size=vol.shape)).astype(np.int16)
+    base = str(tmp_path / "ct")
+    _write_mhd(base, hu, "MET_SHORT")
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "AAA-Vessels-CT",
+            "--centerline-method", "gpu", "--tdf-only"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    ox, oy = int(np.floor(72 * np.float32(0.15) + 0.5)), int(np.floor(64 * np.float32(0.15) + 0.5))
+    SX, SY, SZ = (72 - 2 * ox) // 4 * 4, (64 - 2 * oy) // 4 * 4, 40
+    assert tuple(map(int, open(tmp_path / "size.txt").read().split())) == (SX, SY, SZ)
+    assert tuple(map(int, open(tmp_path / "shift.txt").read().split())) == (0, 0, 0)
+    crop = np.ascontiguousarray(hu[:SZ, oy:oy + SY, ox:ox + SX])
+    v = (np.clip(crop.astype(np.float32), np.float32(50), np.float32(150)) - np.float32(50)) / np.float32(100)
+    f4 = oracle.vector_field(oracle.blur(v, 2.0), 0.3, 1, "snorm16")
+    field = oracle.fmg_gvf(f4, 0.2, 10, "snorm16")
+    T, _ = oracle.tdf_spline(field, 3.5, 90.0, 1.0)
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(SZ, SY, SX)
+    assert np.array_equal(tdf, oracle.from_unorm16(oracle.to_unorm16(T)))
+    assert (tdf > 0).any()
 
 
 @pytest.mark.gpu
