@@ -99,6 +99,42 @@ def test_run_aaa_preset(api_tests, oracle, synth, tmp_path):
 
 
 @pytest.mark.gpu
+def test_run_lung_preset(api_tests, oracle, tmp_path):
+    """run() with the Lung-Airways-CT preset (lung cropping with the "middle"
+    z search and 128 minimum scan lines, dark tubes, HU window -1024..-400,
+    small blur 0.5, large blur 1, fmax 0.3, 250 GVF iterations) on a chest
+    phantom in int16 HU: the crop box and shift vector follow the oracle's
+    scan-line counts and the reference's host rule, and the TDF of the cropped
+    volume equals the oracle's."""
+    pytest.importorskip("torch")
+    import test_crop
+    import test_gpu_crop
+    hu = np.round(test_gpu_crop.chest((200, 200, 360), 2)).astype(np.int16)
+    base = str(tmp_path / "chest")
+    _write_mhd(base, hu, "MET_SHORT")
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Lung-Airways-CT",
+            "--centerline-method", "gpu", "--tdf-only"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    cx, cy, cz = oracle.crop_scan_lines(hu, 1)
+    x1, y1, z1, SX, SY, SZ = test_crop.py_crop_bounds(cx, cy, cz, 128, True)
+    assert SX < 360 and SY < 200 and SZ < 200
+    assert tuple(map(int, open(tmp_path / "size.txt").read().split())) == (SX, SY, SZ)
+    assert tuple(map(int, open(tmp_path / "shift.txt").read().split())) == (x1, y1, z1)
+    crop = np.ascontiguousarray(hu[z1:z1 + SZ, y1:y1 + SY, x1:x1 + SX])
+    v = (np.clip(crop.astype(np.float32), np.float32(-1024), np.float32(-400)) - np.float32(-1024)) / np.float32(624)
+    st = "snorm16"
+    Ts, Rs = oracle.tdf_circle(oracle.vector_field(oracle.blur(v, 0.5), 0.3, -1, st), 0.5, 3.0, 0.5)
+    f4 = oracle.vector_field(oracle.blur(v, 1.0), 0.3, -1, st)
+    field = oracle.gvf_finish(oracle.gvf(f4, 0.05, 250, st), st)
+    Tl, _ = oracle.tdf_circle(field, 2.5, 15.0, 1.0)
+    us, ul = oracle.to_unorm16(Ts), oracle.to_unorm16(Tl)
+    T = oracle.from_unorm16(np.where(ul < us, us, ul))
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(SZ, SY, SX)
+    assert np.array_equal(tdf, T)
+
+
+@pytest.mark.gpu
 def test_run_spline_tdf(api_tests, oracle, synth, tmp_path):
     """run() with use-spline-tdf: the combined TDF (small-radius circle fit,
     large-radius spline TDF) matches the oracle's, and the pipeline links and
