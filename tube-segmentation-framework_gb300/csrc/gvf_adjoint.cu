@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(256) gvf_adjoint_step_kernel(const float *__re
 // x, then y, then z it turns lambda' into fold(lambda') (the rule is separable).
 // One thread per (component, face position); only the boundary planes move.
 __global__ void fold_axis_kernel(float *__restrict__ g, int X, int Y, int Z, int axis) {
+    pdl_trigger();
+    pdl_wait();                     // launched with pdl_config: the previous kernel wrote g
     const int64_t n = (int64_t)X * Y * Z;
     int A, B;                       // extents of the face
     int64_t sa, sb, sn;             // strides: face coordinates, folded axis
@@ -439,7 +441,10 @@ int run_gvf_adjoint(const void *d_f0, int X, int Y, int Z, float mu, int K, int 
                 // kernel does the x part itself), then the stencil
                 for (int axis = zs ? 1 : 0; axis < 3; axis++) {
                     const int64_t faces = 3 * (axis == 0 ? (int64_t)Y * Z : axis == 1 ? (int64_t)X * Z : (int64_t)X * Y);
-                    fold_axis_kernel<<<(unsigned)((faces + 255) / 256), 256, 0, s>>>(lam, X, Y, Z, axis);
+                    cudaLaunchAttribute attr[1];
+                    const cudaLaunchConfig_t cfg =
+                        pdl_config(dim3((unsigned)((faces + 255) / 256)), dim3(256), 0, s, attr);
+                    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, fold_axis_kernel, lam, X, Y, Z, axis));
                 }
                 TSF_CHECK_LAUNCHES("fold_axis_kernel", zs ? 2 : 3);
                 if (zs) {

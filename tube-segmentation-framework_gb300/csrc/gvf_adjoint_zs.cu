@@ -117,6 +117,7 @@ __global__ void __launch_bounds__(AdjZsCfg<ST>::THREADS, 1)
             pt_k = 0;
         }
     };
+    pdl_trigger();
     if (tid == 0) {
         tma_prefetch_desc(&tg);
         tma_prefetch_desc(&tv);
@@ -125,6 +126,9 @@ __global__ void __launch_bounds__(AdjZsCfg<ST>::THREADS, 1)
         for (int i = 0; i < RG; i++) mbar_init(gbar + i, 1);
         for (int i = 0; i < RT; i++) mbar_init(tbar + i, 1);
         fence_mbar_init();
+        // the previous kernel (the fold of g) has completed; every other global
+        // access of this CTA follows the barrier below
+        pdl_wait();
         while (gseq < RG && more_g()) issue_g();
         while (tseq < RT && more_t()) issue_t();
     }
@@ -334,8 +338,10 @@ int launch_gvf_adjoint_zs(int st, const float *g, const void *v, const void *f, 
         if (!encode_planar(&mg, g, X, Y, Z, 4, C::BW, C::TY + 2) || !encode_planar(&mv, v, X, Y, Z, C::ES, C::TX, C::TY) ||
             !encode_planar(&mf, f, X, Y, Z, C::ES, C::TX, C::TY) || !encode_planar(&mgf, gf, X, Y, Z, 4, C::TX, C::TY))
             return fail(TSF_ERR_CUDA, "tensor map encoding failed");
-        gvf_adjoint_zs_kernel<ST><<<grid, C::THREADS, C::SMEM, s>>>(mg, mv, mf, mgf, lam_out, gf, dmu_block, X, Y, Z,
-                                                                    mu, ntx, W);
+        cudaLaunchAttribute attr[1];
+        const cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)grid), dim3(C::THREADS), C::SMEM, s, attr);
+        TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_adjoint_zs_kernel<ST>, mg, mv, mf, mgf, lam_out, gf, dmu_block, X,
+                                        Y, Z, mu, ntx, W));
     });
     TSF_CHECK_LAUNCH("gvf_adjoint_zs_kernel");
     return r;

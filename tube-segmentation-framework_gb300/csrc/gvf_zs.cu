@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
     int issued_v = 0, issued_f = 0;                       // meaningful in thread 0 only
     // The next iteration's CTAs may be scheduled as this grid's CTAs exit
     // (programmatic dependent launch): they run this prologue, then wait below.
-    asm volatile("griddepcontrol.launch_dependents;");
+    pdl_trigger();
     if (tid == 0) {
         tma_prefetch_desc(&tv);
         tma_prefetch_desc(&tf);
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
         // the previous grid (which wrote src and reads dst) has completed and its
         // writes are visible; every other global access of this CTA follows the
         // barrier below
-        asm volatile("griddepcontrol.wait;" ::: "memory");
+        pdl_wait();
         for (; issued_v < RV && issued_v < nv; issued_v++)
             zs_issue(vring + issued_v * C::VSLOT, vbar + issued_v, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + issued_v);
         for (; issued_f < RF && issued_f < nf; issued_f++)
@@ -323,16 +323,8 @@ int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, i
         if (!encode_planar(&tv, src, X, Y, Z, C::ES, C::BW, C::TY + 2) ||
             !encode_planar(&tf, d_f0, X, Y, Z, C::ES, C::TX, C::TY))
             return fail(TSF_ERR_CUDA, "tensor map encoding failed");
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)g.grid);
-        cfg.blockDim = dim3(C::THREADS);
-        cfg.dynamicSmemBytes = C::SMEM;
-        cfg.stream = s;
         cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        attr[0].val.programmaticStreamSerializationAllowed = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
+        const cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS), C::SMEM, s, attr);
         TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
     });
     TSF_CHECK_LAUNCH("gvf_zs_kernel");

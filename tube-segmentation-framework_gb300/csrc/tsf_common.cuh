@@ -158,4 +158,29 @@ __host__ __device__ __forceinline__ int64_t lin(int x, int y, int z, int X, int 
 
 inline size_t storage_bytes(int st) { return st == TSF_STORE_F32 ? 4 : (valid_storage(st) ? 2 : 0); }
 
+// ---------------------------------------------------------------------------
+// programmatic dependent launch
+// ---------------------------------------------------------------------------
+// A kernel launched with pdl_config may be scheduled while the kernel before
+// it in the stream is still finishing.  It must call pdl_wait() before its
+// first access to global memory that the previous kernel writes or reads
+// (the wait returns once that grid has completed and its writes are
+// visible); pdl_trigger() lets the next such kernel be scheduled as this
+// grid's CTAs exit.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+inline cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, size_t smem, cudaStream_t s, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+
 }  // namespace tsf
