@@ -66,6 +66,8 @@ __device__ __forceinline__ float ldc(const ST_T<ST> *a, Dim d, int x, int y, int
 // createSqrMag (kernels.cl:1868-1878)
 template <int ST>
 __global__ void sqrmag_kernel(const void *F, Dim d, ST_T<ST> *sq) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(d);
     const int64_t i = lin(x, y, z, d.x, d.y);
     const float4 q = Vec4Load<ST>::load(F, i);
@@ -75,6 +77,8 @@ __global__ void sqrmag_kernel(const void *F, Dim d, ST_T<ST> *sq) {
 // fmgResidual (kernels.cl:2008-2053), spacing 1
 template <int ST>
 __global__ void fmg_residual_kernel(const void *F, const ST_T<ST> *f, Dim d, int comp, float mu, ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(d);
     const int px = mirror(x, d.x), py = mirror(y, d.y), pz = mirror(z, d.z);
     const float4 q = Vec4Load<ST>::load(F, lin(px, py, pz, d.x, d.y));
@@ -97,6 +101,8 @@ __global__ void fmg_residual_kernel(const void *F, const ST_T<ST> *f, Dim d, int
 template <int ST, bool RED>
 __global__ void gs_kernel(const ST_T<ST> *src, ST_T<ST> *dst, const ST_T<ST> *r, const ST_T<ST> *sq, Dim d,
                           float two_mu, float twelve_mu, float hh, float two_hh) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(d);
     const int px = mirror(x, d.x), py = mirror(y, d.y), pz = mirror(z, d.z);
     const bool red = ((px + py + pz) % 2) == 0;
@@ -123,6 +129,8 @@ __global__ void gs_kernel(const ST_T<ST> *src, ST_T<ST> *dst, const ST_T<ST> *r,
 template <int ST>
 __global__ void residual_kernel(const ST_T<ST> *r, const ST_T<ST> *v, const ST_T<ST> *sq, Dim d, float mu, float h,
                                 ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(d);
     const int px = mirror(x, d.x), py = mirror(y, d.y), pz = mirror(z, d.z);
     const float vc = ld0<ST>(v, d, px, py, pz);
@@ -141,6 +149,8 @@ __global__ void residual_kernel(const ST_T<ST> *r, const ST_T<ST> *v, const ST_T
 // restrictVolume (kernels.cl:1923-1951)
 template <int ST>
 __global__ void restrict_kernel(const ST_T<ST> *fine, Dim fd, Dim cd, ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(cd);
     int px = 2 * x, py = 2 * y, pz = 2 * z;
     if (px >= 2 * cd.x - 1) px = 2 * cd.x - 3;
@@ -160,6 +170,8 @@ __global__ void restrict_kernel(const ST_T<ST> *fine, Dim fd, Dim cd, ST_T<ST> *
 // prolongate (ADD) / prolongate2 (kernels.cl:1953-1970)
 template <int ST, bool ADD>
 __global__ void prolong_kernel(const ST_T<ST> *fine_in, const ST_T<ST> *coarse, Dim fd, Dim cd, ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_THREAD_XYZ(fd);
     const float c = ld0<ST>(coarse, cd, x / 2, y / 2, z / 2);
     const int64_t i = lin(x, y, z, fd.x, fd.y);
@@ -170,6 +182,8 @@ __global__ void prolong_kernel(const ST_T<ST> *fine_in, const ST_T<ST> *coarse, 
 // addTwoImages (kernels.cl:1857-1865), in place on a
 template <int ST>
 __global__ void add_kernel(ST_T<ST> *a, const ST_T<ST> *b, int64_t n) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     a[i] = Store<ST>::store(Store<ST>::load(a[i]) + Store<ST>::load(b[i]));
@@ -178,6 +192,8 @@ __global__ void add_kernel(ST_T<ST> *a, const ST_T<ST> *b, int64_t n) {
 // MGGVFFinish (kernels.cl:1907-1921): w = |v| (no special case for 0)
 template <int ST>
 __global__ void fmg_finish_kernel(const ST_T<ST> *fx, const ST_T<ST> *fy, const ST_T<ST> *fz, void *out, int64_t n) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float x = Store<ST>::load(fx[i]), y = Store<ST>::load(fy[i]), z = Store<ST>::load(fz[i]);
@@ -233,6 +249,8 @@ template <int ST, bool RED>
 __global__ void __launch_bounds__(256) gs_vec_kernel(const ST_T<ST> *src, ST_T<ST> *dst, const ST_T<ST> *r,
                                                      const ST_T<ST> *sq, Dim d, float two_mu, float twelve_mu,
                                                      float hh, float two_hh) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_VEC_PROLOGUE(d);
     float c[VX], yp[VX], ym[VX], zp[VX], zm[VX], rr[VX], qq[VX];
     fmg_load<ST>(src, p, act, c);
@@ -274,6 +292,8 @@ __global__ void __launch_bounds__(256) gs_vec_kernel(const ST_T<ST> *src, ST_T<S
 template <int ST>
 __global__ void __launch_bounds__(256) residual_vec_kernel(const ST_T<ST> *r, const ST_T<ST> *v, const ST_T<ST> *sq,
                                                            Dim d, float mu, float h, ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_VEC_PROLOGUE(d);
     float c[VX], yp[VX], ym[VX], zp[VX], zm[VX], rr[VX], qq[VX];
     fmg_load<ST>(v, p, act, c);
@@ -310,6 +330,8 @@ __global__ void __launch_bounds__(256) residual_vec_kernel(const ST_T<ST> *r, co
 template <int ST>
 __global__ void __launch_bounds__(256) fmg_residual_vec_kernel(const void *F, const ST_T<ST> *f, Dim d, int comp,
                                                                float mu, ST_T<ST> *out) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_VEC_PROLOGUE(d);
     float c[VX], yp[VX], ym[VX], zp[VX], zm[VX];
     fmg_load<ST>(f, p, act, c);
@@ -347,6 +369,8 @@ __global__ void __launch_bounds__(256) fmg_residual_vec_kernel(const void *F, co
 // take coarse x0/2 .. (x0+VX-1)/2 (0 outside the coarse image)
 template <int ST, bool ADD>
 __global__ void __launch_bounds__(256) prolong_vec_kernel(const ST_T<ST> *coarse, Dim fd, Dim cd, ST_T<ST> *v) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     using P = typename FmgVec<ST>::P;
     constexpr int VX = FmgVec<ST>::VX;
     const int lane = threadIdx.x;
@@ -368,6 +392,8 @@ __global__ void __launch_bounds__(256) prolong_vec_kernel(const ST_T<ST> *coarse
 // addTwoImages, vectorised (n a multiple of VX)
 template <int ST>
 __global__ void __launch_bounds__(256) add_vec_kernel(ST_T<ST> *a, const ST_T<ST> *b, int64_t nvec) {
+    pdl_trigger();
+    pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     using P = typename FmgVec<ST>::P;
     constexpr int VX = FmgVec<ST>::VX;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -416,6 +442,16 @@ static FmgLayout fmg_layout(int X, int Y, int Z, int st) {
 
 size_t fmg_workspace_size(int X, int Y, int Z, int st) { return fmg_layout(X, Y, Z, st).bytes; }
 
+// Every level kernel is launched with programmatic dependent launch (the
+// V-cycles are hundreds of small launches); each kernel waits for its
+// predecessor before touching memory.
+template <typename K, typename... A>
+static cudaError_t fmg_launch(K kernel, dim3 grid, dim3 block, cudaStream_t s, A... args) {
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = pdl_config(grid, block, 0, s, attr);
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int ST> struct FmgRun {
     using T = ST_T<ST>;
     const FmgLayout &L;
@@ -440,11 +476,11 @@ template <int ST> struct FmgRun {
         const float two_mu = 2.0f * mu, twelve_mu = 12.0f * mu, hh = h * h, two_hh = (2.0f * h) * h;
         for (int i = 0; i < iterations; i++) {
             if (vec(d)) {
-                gs_vec_kernel<ST, true><<<vgrd(d), vblk(), 0, s>>>(v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh);
-                gs_vec_kernel<ST, false><<<vgrd(d), vblk(), 0, s>>>(v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+                TSF_TRY_CUDA(fmg_launch(gs_vec_kernel<ST, true>, vgrd(d), vblk(), s, v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh));
+                TSF_TRY_CUDA(fmg_launch(gs_vec_kernel<ST, false>, vgrd(d), vblk(), s, v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh));
             } else {
-                gs_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh);
-                gs_kernel<ST, false><<<grd(d), blk(), 0, s>>>(v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh);
+                TSF_TRY_CUDA(fmg_launch(gs_kernel<ST, true>, grd(d), blk(), s, v, v2, r, sq, d, two_mu, twelve_mu, hh, two_hh));
+                TSF_TRY_CUDA(fmg_launch(gs_kernel<ST, false>, grd(d), blk(), s, v2, v, r, sq, d, two_mu, twelve_mu, hh, two_hh));
             }
         }
         TSF_CHECK_LAUNCHES("gs_kernel", 2 * iterations);
@@ -458,20 +494,20 @@ template <int ST> struct FmgRun {
         if (l < kLevels - 1) {
             const Dim d = L.d[l], nd = L.d[l + 1];
             T *p = buf(L.p[l]);
-            if (vec(d)) residual_vec_kernel<ST><<<vgrd(d), vblk(), 0, s>>>(r, v, buf(L.sq[l]), d, mu, h, p);
-            else residual_kernel<ST><<<grd(d), blk(), 0, s>>>(r, v, buf(L.sq[l]), d, mu, h, p);
+            if (vec(d)) TSF_TRY_CUDA(fmg_launch(residual_vec_kernel<ST>, vgrd(d), vblk(), s, r, v, buf(L.sq[l]), d, mu, h, p));
+            else TSF_TRY_CUDA(fmg_launch(residual_kernel<ST>, grd(d), blk(), s, r, v, buf(L.sq[l]), d, mu, h, p));
             T *r1 = buf(L.r[l + 1]);
-            restrict_kernel<ST><<<grd(nd), blk(), 0, s>>>(p, d, nd, r1);
+            TSF_TRY_CUDA(fmg_launch(restrict_kernel<ST>, grd(nd), blk(), s, p, d, nd, r1));
             T *v1 = buf(L.v[l + 1]);
             TSF_TRY_CUDA(cudaMemsetAsync(v1, 0, sizeof(T) * (size_t)nvox(nd), s));
             TSF_CHECK_LAUNCHES("residual/restrict", 2);
             e = vcycle(l + 1, r1, v1, h * 2.0f);
             if (e) return e;
             if (vec(d)) {
-                prolong_vec_kernel<ST, true><<<vgrd(d), vblk(), 0, s>>>(v1, d, nd, v);   // in place
+                TSF_TRY_CUDA(fmg_launch(prolong_vec_kernel<ST, true>, vgrd(d), vblk(), s, v1, d, nd, v));   // in place
                 TSF_CHECK_LAUNCH("prolong_vec_kernel");
             } else {
-                prolong_kernel<ST, true><<<grd(d), blk(), 0, s>>>(v, v1, d, nd, p);
+                TSF_TRY_CUDA(fmg_launch(prolong_kernel<ST, true>, grd(d), blk(), s, v, v1, d, nd, p));
                 TSF_CHECK_LAUNCH("prolong_kernel");
                 TSF_TRY_CUDA(cudaMemcpyAsync(v, p, sizeof(T) * (size_t)nvox(d), cudaMemcpyDeviceToDevice, s));
             }
@@ -485,12 +521,12 @@ template <int ST> struct FmgRun {
         T *v = buf(L.v[l]);
         if (l < kLevels - 1) {
             const Dim nd = L.d[l + 1];
-            restrict_kernel<ST><<<grd(nd), blk(), 0, s>>>(buf(L.r[l]), d, nd, buf(L.r[l + 1]));
+            TSF_TRY_CUDA(fmg_launch(restrict_kernel<ST>, grd(nd), blk(), s, buf(L.r[l]), d, nd, buf(L.r[l + 1])));
             TSF_CHECK_LAUNCH("restrict_kernel");
             int e = full(l + 1, h * 2.0f);
             if (e) return e;
-            if (vec(d)) prolong_vec_kernel<ST, false><<<vgrd(d), vblk(), 0, s>>>(buf(L.v[l + 1]), d, nd, v);
-            else prolong_kernel<ST, false><<<grd(d), blk(), 0, s>>>(nullptr, buf(L.v[l + 1]), d, nd, v);
+            if (vec(d)) TSF_TRY_CUDA(fmg_launch(prolong_vec_kernel<ST, false>, vgrd(d), vblk(), s, buf(L.v[l + 1]), d, nd, v));
+            else TSF_TRY_CUDA(fmg_launch(prolong_kernel<ST, false>, grd(d), blk(), s, nullptr, buf(L.v[l + 1]), d, nd, v));
             TSF_CHECK_LAUNCH("prolong_kernel");
         } else {
             TSF_TRY_CUDA(cudaMemsetAsync(v, 0, sizeof(T) * (size_t)nvox(d), s));
@@ -501,30 +537,30 @@ template <int ST> struct FmgRun {
     int run(const void *F, void *out, int iterations) {
         const Dim d0 = L.d[0];
         const int64_t n0 = nvox(d0);
-        sqrmag_kernel<ST><<<grd(d0), blk(), 0, s>>>(F, d0, buf(L.sq[0]));
+        TSF_TRY_CUDA(fmg_launch(sqrmag_kernel<ST>, grd(d0), blk(), s, F, d0, buf(L.sq[0])));
         for (int l = 1; l < kLevels; l++)
-            restrict_kernel<ST><<<grd(L.d[l]), blk(), 0, s>>>(buf(L.sq[l - 1]), L.d[l - 1], L.d[l], buf(L.sq[l]));
+            TSF_TRY_CUDA(fmg_launch(restrict_kernel<ST>, grd(L.d[l]), blk(), s, buf(L.sq[l - 1]), L.d[l - 1], L.d[l], buf(L.sq[l])));
         TSF_CHECK_LAUNCHES("sqrmag/restrict", kLevels);
         const unsigned nb = (unsigned)((n0 + 255) / 256);
         for (int c = 0; c < 3; c++) {
             T *f = buf(L.comp[c]);
             TSF_TRY_CUDA(cudaMemsetAsync(f, 0, sizeof(T) * (size_t)n0, s));
             for (int it = 0; it < iterations; it++) {
-                if (vec(d0)) fmg_residual_vec_kernel<ST><<<vgrd(d0), vblk(), 0, s>>>(F, f, d0, c, mu, buf(L.r[0]));
-                else fmg_residual_kernel<ST><<<grd(d0), blk(), 0, s>>>(F, f, d0, c, mu, buf(L.r[0]));
+                if (vec(d0)) TSF_TRY_CUDA(fmg_launch(fmg_residual_vec_kernel<ST>, vgrd(d0), vblk(), s, F, f, d0, c, mu, buf(L.r[0])));
+                else TSF_TRY_CUDA(fmg_launch(fmg_residual_kernel<ST>, grd(d0), blk(), s, F, f, d0, c, mu, buf(L.r[0])));
                 TSF_CHECK_LAUNCH("fmg_residual_kernel");
                 int e = full(0, 1.0f);
                 if (e) return e;
                 if (vec(d0)) {
                     const int64_t nvec = n0 / VX;
-                    add_vec_kernel<ST><<<(unsigned)((nvec + 255) / 256), 256, 0, s>>>(f, buf(L.v[0]), nvec);
+                    TSF_TRY_CUDA(fmg_launch(add_vec_kernel<ST>, (unsigned)((nvec + 255) / 256), 256, s, f, buf(L.v[0]), nvec));
                 } else {
-                    add_kernel<ST><<<nb, 256, 0, s>>>(f, buf(L.v[0]), n0);
+                    TSF_TRY_CUDA(fmg_launch(add_kernel<ST>, nb, 256, s, f, buf(L.v[0]), n0));
                 }
                 TSF_CHECK_LAUNCH("add_kernel");
             }
         }
-        fmg_finish_kernel<ST><<<nb, 256, 0, s>>>(buf(L.comp[0]), buf(L.comp[1]), buf(L.comp[2]), out, n0);
+        TSF_TRY_CUDA(fmg_launch(fmg_finish_kernel<ST>, nb, 256, s, buf(L.comp[0]), buf(L.comp[1]), buf(L.comp[2]), out, n0));
         TSF_CHECK_LAUNCH("fmg_finish_kernel");
         return TSF_OK;
     }
