@@ -10,9 +10,10 @@ hot path over the volume, with inputs resident in HBM:
 value = voxel-iterations of GVF per step (N * 500) / step time, in
 Gvoxel-iter/s: the metric of the workload, measured over the whole step.
 
-e2e: the same step driven through the C ABI from pinned HOST memory: the
-volume is copied host->device and the TDF, radius and vertex list device->host
-inside the timed region.
+e2e: the same step driven through the C ABI from pinned HOST memory: every
+step's volume is copied host->device and its TDF, radius and vertex list
+device->host inside the timed region, on a copy stream overlapped with the
+neighbouring steps' compute.
 
 Multi-GPU: the path does not shard here; --gpus N runs N independent
 replicas (one volume per GPU), value = sum over ranks.
@@ -356,28 +357,64 @@ def run_tsf(args, rank, world):
     achieved = algo_bytes / launch_s / 1e9
 
     # ---- e2e through the C ABI with host buffers --------------------------------------
+    # Every step copies its volume in from pinned host memory and its TDF, radius
+    # and vertex list out; the copies run on a second stream, overlapped with the
+    # neighbouring steps' compute: the volume of step j + 1 is uploaded into the
+    # other of two input buffers while step j computes (once step j - 1, which
+    # read that buffer, is done), and step j's results are copied device to
+    # device into staging buffers and downloaded while step j + 1 computes.
     out_T = torch.empty(shape, dtype=torch.float32).pin_memory()
     out_R = torch.empty(shape, dtype=torch.float32).pin_memory()
     out_V = torch.empty((pipe.max_vertices, 3), dtype=torch.int32).pin_memory()
+    main, copy = torch.cuda.current_stream(), torch.cuda.Stream()
+    vols = [pipe.vol, torch.empty_like(pipe.vol)]
+    stage_T, stage_R, stage_V = torch.empty_like(pipe.Tl), torch.empty_like(pipe.Rl), torch.empty_like(pipe.verts)
 
-    def e2e_step():
-        pipe.vol.copy_(host, non_blocking=True)
-        pipe.step()
-        out_T.copy_(pipe.Tl, non_blocking=True)
-        out_R.copy_(pipe.Rl, non_blocking=True)
-        nv = min(pipe.last["n_vertices"], pipe.max_vertices)
-        if nv:
-            out_V[:nv].copy_(pipe.verts[:nv], non_blocking=True)
-        return nv
+    def e2e_run(nsteps):
+        ev_in = torch.cuda.Event()
+        with torch.cuda.stream(copy):
+            vols[0].copy_(host, non_blocking=True)
+        ev_in.record(copy)
+        ev_out = None
+        nvs = []
+        for j in range(nsteps):
+            main.wait_event(ev_in)                       # this step's volume has landed
+            pipe.vol = vols[j % 2]
+            if j + 1 < nsteps:                           # next volume, into the buffer step j - 1 read
+                ev_free = torch.cuda.Event()
+                ev_free.record(main)
+                copy.wait_event(ev_free)
+                with torch.cuda.stream(copy):
+                    vols[(j + 1) % 2].copy_(host, non_blocking=True)
+                ev_in = torch.cuda.Event()
+                ev_in.record(copy)
+            pipe.step()
+            nv = min(pipe.last["n_vertices"], pipe.max_vertices)
+            if ev_out is not None:
+                main.wait_event(ev_out)                  # the previous download has left the staging buffers
+            stage_T.copy_(pipe.Tl)
+            stage_R.copy_(pipe.Rl)
+            if nv:
+                stage_V[:nv].copy_(pipe.verts[:nv])
+            ev_done = torch.cuda.Event()
+            ev_done.record(main)
+            copy.wait_event(ev_done)
+            with torch.cuda.stream(copy):
+                out_T.copy_(stage_T, non_blocking=True)
+                out_R.copy_(stage_R, non_blocking=True)
+                if nv:
+                    out_V[:nv].copy_(stage_V[:nv], non_blocking=True)
+            ev_out = torch.cuda.Event()
+            ev_out.record(copy)
+            nvs.append(nv)
+        torch.cuda.synchronize()
+        return nvs
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    e2e_run(max(1, args.warmup))
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
-    nvs = []
-    for _ in range(args.steps):
-        nvs.append(e2e_step())
+    nvs = e2e_run(args.steps)
     torch.cuda.synchronize()
     e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, world)
     e2e_value = replica_throughput(N * args.iters, e2e_s, world) / 1e9
