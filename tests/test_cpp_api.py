@@ -38,17 +38,21 @@ def _write_mhd(path, vol_u8, element="MET_UCHAR"):
     vol_u8.tofile(path + ".raw")
 
 
-def _oracle_run(oracle, vol_u8, iters, spline=False):
+def _oracle_run(oracle, vol_u8, iters, spline=False, sixteen_bit=True):
     """run() with the Synthetic-Vascusynth preset, restated with the oracle
-    (spline: the large-radius TDF is the spline TDF from max(1.5, radius-min))."""
+    (spline: the large-radius TDF is the spline TDF from max(1.5, radius-min);
+    sixteen_bit False: the 32-bit mode, FP32 fields and a float TDF)."""
     v = np.clip(vol_u8.astype(np.float32), np.float32(0), np.float32(75)) / np.float32(75)   # toFloat
-    st = "snorm16"
+    st = "snorm16" if sixteen_bit else "f32"
     f_small = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                          # small-blur 1.0
     Ts, Rs = oracle.tdf_circle(f_small, 0.5, 3.0, 0.5)
     f4 = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                               # large-blur 1.0
     vv = oracle.gvf(f4, 0.05, iters - iters % 2, st)
     field = oracle.gvf_finish(vv, st)
     Tl, Rl = oracle.tdf_spline(field, 1.5, 4.0, 1.0) if spline else oracle.tdf_circle(field, 2.5, 4.0, 1.0)
+    if not sixteen_bit:
+        m = Tl < Ts
+        return np.where(m, Ts, Tl).astype(np.float32), np.where(m, Rs, Rl).astype(np.float32), field
     us, ul = oracle.to_unorm16(Ts), oracle.to_unorm16(Tl)
     m = ul < us
     T16 = np.where(m, us, ul)
@@ -64,6 +68,28 @@ def _read_vtk(path):
     nl = int(lines[k + 1].split()[1])
     edges = np.array([list(map(int, l.split()))[1:] for l in lines[k + 2:k + 2 + nl]], np.int32).reshape(-1, 2)
     return pts, edges
+
+
+@pytest.mark.gpu
+def test_run_32bit_vectors(api_tests, oracle, synth, tmp_path):
+    """run() in the 32-bit mode (32bit-vectors: FP32 fields, a float TDF):
+    the TDF and the vertex list equal the oracle's."""
+    pytest.importorskip("torch")
+    vol_u8 = np.round(synth.vascular_tree((44, 52, 60), seed=11) * 90.0).astype(np.uint8)
+    base = str(tmp_path / "vol")
+    _write_mhd(base, vol_u8)
+    iters = 21
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
+            "--centerline-method", "gpu", "--gvf-iterations", str(iters), "--32bit-vectors", "true",
+            "--16bit-vectors", "false", "--no-segmentation", "true"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    T, R, field = _oracle_run(oracle, vol_u8, iters, sixteen_bit=False)
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(T.shape)
+    assert np.array_equal(tdf, T)
+    ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
+    got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
+    assert len(got) > 20 and np.array_equal(got, ref["vertices"])
 
 
 @pytest.mark.gpu
