@@ -28,9 +28,15 @@
 // tiles are shifted inward); in x the vector holding x = 0 / X-1 copies the
 // result of x = 2 / X-3; the plane q = 2 (Z-3) is also written to plane 0
 // (Z-1).  Per voxel the arithmetic is exactly gvf_plain_kernel's, so the
-// result is bit-identical to the other GVF kernels.  Packed f32x2 sums were
-// tried and lost: they do not raise FP32 throughput here, and the assembler
-// fuses packed multiply-add pairs, which changes the rounding.
+// result is bit-identical to the other GVF kernels.  For FP16 and BF16 the
+// y neighbours, the outer x neighbours and f0 enter the arithmetic through
+// mixed-precision add / subtract / fma (16-bit source, FP32 result, one
+// rounding), which saves the separate half -> float conversions: the
+// conversion is exact, so each such instruction rounds like convert-then-op,
+// and (f0 - v)|f0|^2 added equals (v - f0)|f0|^2 subtracted bit for bit.
+// Packed f32x2 sums were tried and lost: they do not raise FP32 throughput
+// here, and the assembler fuses packed multiply-add pairs, which changes the
+// rounding.
 #include <mutex>
 
 #include "packed.cuh"
@@ -53,6 +59,7 @@ template <int ST> struct ZsCfg {
     static constexpr int FSLOT = (FBOX + 127) / 128 * 128;
     static constexpr int SMEM = RV * VSLOT + RF * FSLOT + (RV + RF) * 8 + 16;
     static constexpr int THREADS = 32 * TY;
+    static constexpr int MIN_CTAS = ES == 2 ? 3 : 2;       // resident CTAs per SM the shared memory allows
     static constexpr int BYTES = 4 * ES;                   // one lane's 4 voxels
 };
 
@@ -67,13 +74,16 @@ __device__ __forceinline__ void zs_issue(unsigned char *slot, uint64_t *bar, int
 }
 
 template <int ST>
-__global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
+__global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
                                                                    const __grid_constant__ CUtensorMap tf,
                                                                    typename Store<ST>::T *__restrict__ dst, int X,
                                                                    int Y, int Z, float mu, int ntx, int K) {
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     using P = PackedV<ST, C::BYTES>;
+    // FP16 / BF16: 16-bit operands enter the sums through mixed-precision
+    // instructions instead of separate conversions (same bits)
+    constexpr bool MIX = ST == TSF_STORE_F16 || ST == TSF_STORE_BF16;
     constexpr int TX = C::TX, TY = C::TY, H = C::H, BW = C::BW, RV = C::RV, RF = C::RF;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *vring = smem;
@@ -149,32 +159,82 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS) gvf_zs_kernel(const __grid
         const bool dup_lo = q == 2, dup_hi = q == Z - 3;
 
         float fv[3][4], sqr[4];
+        typename P::Raw fr[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) P::unpack(P::load_plain(fs + c * TY * TX), fv[c]);
+        for (int c = 0; c < 3; c++) fr[c] = P::load_plain(fs + c * TY * TX);
+        if constexpr (MIX && ST == TSF_STORE_F16) {
+            sqr[0] = sqadd16v<0>(fr[2].u, sqadd16v<0>(fr[1].u, sqadd16v<0>(fr[0].u, -0.0f)));
+            sqr[1] = sqadd16v<1>(fr[2].u, sqadd16v<1>(fr[1].u, sqadd16v<1>(fr[0].u, -0.0f)));
+            sqr[2] = sqadd16v<2>(fr[2].u, sqadd16v<2>(fr[1].u, sqadd16v<2>(fr[0].u, -0.0f)));
+            sqr[3] = sqadd16v<3>(fr[2].u, sqadd16v<3>(fr[1].u, sqadd16v<3>(fr[0].u, -0.0f)));
+        } else {
 #pragma unroll
-        for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+            for (int c = 0; c < 3; c++) P::unpack(fr[c], fv[c]);
+#pragma unroll
+            for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const T *pc = vc + c * vstride;
-            float yp[4], ym[4], zp[4];
+            float zp[4], res[4];
             P::unpack(P::load_plain(vp + c * vstride), zp);
-            P::unpack(P::load_plain(pc + BW), yp);
-            P::unpack(P::load_plain(pc - BW), ym);
-            const float xr = Store<ST>::load(pc[4]);
-            const float xl = Store<ST>::load(pc[-1]);
-            float res[4];
+            if constexpr (MIX) {
+                // the y neighbours, the outer x neighbours and f0 enter the
+                // sums unconverted (mixed-precision add / subtract, same bits)
+                const typename P::Raw yp = P::load_plain(pc + BW), ym = P::load_plain(pc - BW);
+                const unsigned xr = *reinterpret_cast<const unsigned short *>(pc + 4);
+                const unsigned xl = *reinterpret_cast<const unsigned short *>(pc - 1);
+                float lap[4];
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                const float v = cc[c][i];
-                float lap = -6.0f * v;
-                lap = lap + (i == 3 ? xr : cc[c][i < 3 ? i + 1 : i]);
-                lap = lap + (i == 0 ? xl : cc[c][i > 0 ? i - 1 : 0]);
-                lap = lap + yp[i];
-                lap = lap + ym[i];
-                lap = lap + zp[i];
-                lap = lap + cm[c][i];
-                const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
-                res[i] = v + upd;
+                for (int i = 0; i < 4; i++) lap[i] = -6.0f * cc[c][i];
+                lap[0] = lap[0] + cc[c][1];
+                lap[1] = lap[1] + cc[c][2];
+                lap[2] = lap[2] + cc[c][3];
+                lap[3] = add16<ST, 0>(xr, lap[3]);
+                lap[0] = add16<ST, 0>(xl, lap[0]);
+                lap[1] = lap[1] + cc[c][0];
+                lap[2] = lap[2] + cc[c][1];
+                lap[3] = lap[3] + cc[c][2];
+                lap[0] = add16v<ST, 0>(yp.u, lap[0]);
+                lap[1] = add16v<ST, 1>(yp.u, lap[1]);
+                lap[2] = add16v<ST, 2>(yp.u, lap[2]);
+                lap[3] = add16v<ST, 3>(yp.u, lap[3]);
+                lap[0] = add16v<ST, 0>(ym.u, lap[0]);
+                lap[1] = add16v<ST, 1>(ym.u, lap[1]);
+                lap[2] = add16v<ST, 2>(ym.u, lap[2]);
+                lap[3] = add16v<ST, 3>(ym.u, lap[3]);
+                // (f0 - v) * |f0|^2 added is (v - f0) * |f0|^2 subtracted, bit for bit
+                float d[4];
+                d[0] = sub16v<ST, 0>(fr[c].u, cc[c][0]);
+                d[1] = sub16v<ST, 1>(fr[c].u, cc[c][1]);
+                d[2] = sub16v<ST, 2>(fr[c].u, cc[c][2]);
+                d[3] = sub16v<ST, 3>(fr[c].u, cc[c][3]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    float l = lap[i] + zp[i];
+                    l = l + cm[c][i];
+                    const float upd = mu * l + d[i] * sqr[i];
+                    res[i] = cc[c][i] + upd;
+                }
+            } else {
+                float yp[4], ym[4];
+                P::unpack(P::load_plain(pc + BW), yp);
+                P::unpack(P::load_plain(pc - BW), ym);
+                const float xr = Store<ST>::load(pc[4]);
+                const float xl = Store<ST>::load(pc[-1]);
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const float v = cc[c][i];
+                    float lap = -6.0f * v;
+                    lap = lap + (i == 3 ? xr : cc[c][i < 3 ? i + 1 : i]);
+                    lap = lap + (i == 0 ? xl : cc[c][i > 0 ? i - 1 : 0]);
+                    lap = lap + yp[i];
+                    lap = lap + ym[i];
+                    lap = lap + zp[i];
+                    lap = lap + cm[c][i];
+                    const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
+                    res[i] = v + upd;
+                }
             }
             if (fix_lo) res[0] = res[2];
             if (fix_hi) res[3] = res[1];
@@ -310,22 +370,29 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
 
 // One iteration src -> dst with the streaming kernel (caller checked
 // gvf_zs_eligible).
+template <int ST>
+static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
+                           cudaStream_t s) {
+    using C = ZsCfg<ST>;
+    using T = typename Store<ST>::T;
+    ZsLaunch<ST> g;
+    int r = zs_geometry<ST>(X, Y, Z, g);
+    if (r) return r;
+    CUtensorMap tv, tf;
+    if (!encode_planar(&tv, src, X, Y, Z, C::ES, C::BW, C::TY + 2) ||
+        !encode_planar(&tf, d_f0, X, Y, Z, C::ES, C::TX, C::TY))
+        return fail(TSF_ERR_CUDA, "tensor map encoding failed");
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS), C::SMEM, s, attr);
+    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+    return TSF_OK;
+}
+
 int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
                   cudaStream_t s) {
     int r = TSF_OK;
     TSF_DISPATCH_STORAGE(st, ST, {
-        using C = ZsCfg<ST>;
-        using T = typename Store<ST>::T;
-        ZsLaunch<ST> g;
-        r = zs_geometry<ST>(X, Y, Z, g);
-        if (r) return r;
-        CUtensorMap tv, tf;
-        if (!encode_planar(&tv, src, X, Y, Z, C::ES, C::BW, C::TY + 2) ||
-            !encode_planar(&tf, d_f0, X, Y, Z, C::ES, C::TX, C::TY))
-            return fail(TSF_ERR_CUDA, "tensor map encoding failed");
-        cudaLaunchAttribute attr[1];
-        const cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS), C::SMEM, s, attr);
-        TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+        r = launch_zs_typed<ST>(d_f0, src, dst, X, Y, Z, mu, s);
     });
     TSF_CHECK_LAUNCH("gvf_zs_kernel");
     return r;

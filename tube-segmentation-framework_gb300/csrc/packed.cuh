@@ -84,5 +84,69 @@ template <int ST, int BYTES> struct PackedV {
     }
 };
 
+// Mixed-precision arithmetic on one 16-bit half of a 32-bit word (K = 0: the
+// low half, element 2k of a packed vector; K = 1: the high half), with a
+// single rounding to FP32 (PTX add / sub / fma with .f16 / .bf16 sources and
+// an .f32 destination, sm_100 and later).  A 16-bit value converts to FP32
+// exactly, so
+//   add16(u, c)    == RN(float(h) + c)      == convert, then add
+//   sub16(u, c)    == RN(float(h) - c)      == convert, then subtract
+// and, for FP16 only, the square of an FP16 value is exact in FP32 (11-bit
+// significands, product within FP32's normal range), so
+//   sqadd16(u, c)  == RN(float(h)^2 + c)    == convert, square, then add.
+// (BF16 squares can leave FP32's normal range, so BF16 uses no sqadd16.)
+template <int ST, int K> __device__ __forceinline__ float add16(unsigned u, float c) {
+    static_assert(ST == TSF_STORE_F16 || ST == TSF_STORE_BF16, "16-bit float storage only");
+    float d;
+    if constexpr (ST == TSF_STORE_F16) {
+        if constexpr (K == 0)
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tadd.rn.f32.f16 %0, l, %2;}" : "=f"(d) : "r"(u), "f"(c));
+        else
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tadd.rn.f32.f16 %0, h, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    } else {
+        if constexpr (K == 0)
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tadd.rn.f32.bf16 %0, l, %2;}" : "=f"(d) : "r"(u), "f"(c));
+        else
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tadd.rn.f32.bf16 %0, h, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    }
+    return d;
+}
+
+template <int ST, int K> __device__ __forceinline__ float sub16(unsigned u, float c) {
+    static_assert(ST == TSF_STORE_F16 || ST == TSF_STORE_BF16, "16-bit float storage only");
+    float d;
+    if constexpr (ST == TSF_STORE_F16) {
+        if constexpr (K == 0)
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tsub.rn.f32.f16 %0, l, %2;}" : "=f"(d) : "r"(u), "f"(c));
+        else
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tsub.rn.f32.f16 %0, h, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    } else {
+        if constexpr (K == 0)
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tsub.rn.f32.bf16 %0, l, %2;}" : "=f"(d) : "r"(u), "f"(c));
+        else
+            asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tsub.rn.f32.bf16 %0, h, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    }
+    return d;
+}
+
+template <int K> __device__ __forceinline__ float sqadd16(unsigned u, float c) {
+    float d;
+    if constexpr (K == 0)
+        asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tfma.rn.f32.f16 %0, l, l, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    else
+        asm("{.reg .b16 l, h;\n\tmov.b32 {l, h}, %1;\n\tfma.rn.f32.f16 %0, h, h, %2;}" : "=f"(d) : "r"(u), "f"(c));
+    return d;
+}
+
+// Element i (0..3) of a packed 4-element 16-bit vector.
+template <int ST, int I> __device__ __forceinline__ float add16v(const unsigned *u, float c) {
+    return add16<ST, I & 1>(u[I >> 1], c);
+}
+template <int ST, int I> __device__ __forceinline__ float sub16v(const unsigned *u, float c) {
+    return sub16<ST, I & 1>(u[I >> 1], c);
+}
+template <int I> __device__ __forceinline__ float sqadd16v(const unsigned *u, float c) {
+    return sqadd16<I & 1>(u[I >> 1], c);
+}
 
 }  // namespace tsf

@@ -73,11 +73,22 @@ template <> struct Store<TSF_STORE_BF16> {
 
 // OpenCL CL_SNORM_INT16: write convert_short_sat_rte(v * 32767), read
 // max(-1, s / 32767) (kernels_no_3d_write.cl:9-21, OpenCL 1.1 section 8.3).
+//
+// The read divides without a division instruction: q0 = RN(s * r) with
+// r = RN(1 / 32767); the residual s - q0 * 32767 is exact in one fma, and
+// RN(q0 + residual * r) is the correctly rounded quotient -- Markstein's
+// correction step (P. W. Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  It is
+// checked against exact rational arithmetic for all 65,536 inputs
+// (tests/test_snorm16_read.py), so it gives the bits of s / 32767.
 template <> struct Store<TSF_STORE_SNORM16> {
     using T = int16_t;
     static __device__ __forceinline__ float load(T v) {
-        float f = __fdiv_rn((float)v, 32767.0f);
-        return fmaxf(-1.0f, f);
+        const float x = (float)v;
+        const float r = __uint_as_float(0x38000100u);      // RN(1 / 32767)
+        const float q0 = __fmul_rn(x, r);
+        const float e = __fmaf_rn(-q0, 32767.0f, x);
+        return fmaxf(-1.0f, __fmaf_rn(e, r, q0));
     }
     static __device__ __forceinline__ T store(float v) {
         float f = __fmul_rn(v, 32767.0f);
