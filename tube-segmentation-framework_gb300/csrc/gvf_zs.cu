@@ -135,41 +135,45 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
     const int voff = lr * BW + e, vstride = (TY + 2) * BW;    // component c at voff + c * vstride
     const int foff = fr * TX + 4 * lane;
     bool ok = true;
-    // The lane's z column: centre values of planes q-1 and q, carried from
-    // the previous plane so each stored value is loaded and converted once as
-    // a centre.
+    // FP32 / snorm16: the lane's z column (centre values of planes q-1 and
+    // q) is carried from the previous plane so each stored value is loaded
+    // and converted once as a centre.  FP16 / BF16 read planes q-1 and q+1
+    // from the ring each plane: they enter the sums unconverted.
     float cm[3][4], cc[3][4];
-    int sc = 1, sp = 2, sf = 0;                           // slots of v planes q, q+1 and f plane q
+    int sm = 0, sc = 1, sp = 2, sf = 0;                   // slots of v planes q-1, q, q+1 and f plane q
     uint32_t pp = 0, pf = 0;                              // phase parity of the waits on sp, sf
     ok &= mbar_wait(vbar + 0, 0);
     ok &= mbar_wait(vbar + 1, 0);
+    if constexpr (!MIX) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        P::unpack(P::load_plain(reinterpret_cast<const T *>(vring) + voff + c * vstride), cm[c]);
-        P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), cc[c]);
+        for (int c = 0; c < 3; c++) {
+            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring) + voff + c * vstride), cm[c]);
+            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), cc[c]);
+        }
     }
 
     for (int k = 0; k < nf; k++) {
         const int q = qa + k;
         ok &= mbar_wait(vbar + sp, pp);
         ok &= mbar_wait(fbar + sf, pf);
+        const T *vm = reinterpret_cast<const T *>(vring + sm * C::VSLOT) + voff;
         const T *vc = reinterpret_cast<const T *>(vring + sc * C::VSLOT) + voff;
         const T *vp = reinterpret_cast<const T *>(vring + sp * C::VSLOT) + voff;
         const T *fs = reinterpret_cast<const T *>(fring + sf * C::FSLOT) + foff;
         const bool dup_lo = q == 2, dup_hi = q == Z - 3;
 
         float fv[3][4], sqr[4];
-        typename P::Raw fr[3];
+        typename P::Raw fraw[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) fr[c] = P::load_plain(fs + c * TY * TX);
+        for (int c = 0; c < 3; c++) fraw[c] = P::load_plain(fs + c * TY * TX);
         if constexpr (MIX && ST == TSF_STORE_F16) {
-            sqr[0] = sqadd16v<0>(fr[2].u, sqadd16v<0>(fr[1].u, sqadd16v<0>(fr[0].u, -0.0f)));
-            sqr[1] = sqadd16v<1>(fr[2].u, sqadd16v<1>(fr[1].u, sqadd16v<1>(fr[0].u, -0.0f)));
-            sqr[2] = sqadd16v<2>(fr[2].u, sqadd16v<2>(fr[1].u, sqadd16v<2>(fr[0].u, -0.0f)));
-            sqr[3] = sqadd16v<3>(fr[2].u, sqadd16v<3>(fr[1].u, sqadd16v<3>(fr[0].u, -0.0f)));
+            sqr[0] = sqadd16v<0>(fraw[2].u, sqadd16v<0>(fraw[1].u, sqadd16v<0>(fraw[0].u, -0.0f)));
+            sqr[1] = sqadd16v<1>(fraw[2].u, sqadd16v<1>(fraw[1].u, sqadd16v<1>(fraw[0].u, -0.0f)));
+            sqr[2] = sqadd16v<2>(fraw[2].u, sqadd16v<2>(fraw[1].u, sqadd16v<2>(fraw[0].u, -0.0f)));
+            sqr[3] = sqadd16v<3>(fraw[2].u, sqadd16v<3>(fraw[1].u, sqadd16v<3>(fraw[0].u, -0.0f)));
         } else {
 #pragma unroll
-            for (int c = 0; c < 3; c++) P::unpack(fr[c], fv[c]);
+            for (int c = 0; c < 3; c++) P::unpack(fraw[c], fv[c]);
 #pragma unroll
             for (int i = 0; i < 4; i++) sqr[i] = (fv[0][i] * fv[0][i] + fv[1][i] * fv[1][i]) + fv[2][i] * fv[2][i];
         }
@@ -177,24 +181,28 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
         for (int c = 0; c < 3; c++) {
             const T *pc = vc + c * vstride;
             float zp[4], res[4];
-            P::unpack(P::load_plain(vp + c * vstride), zp);
             if constexpr (MIX) {
-                // the y neighbours, the outer x neighbours and f0 enter the
-                // sums unconverted (mixed-precision add / subtract, same bits)
-                const typename P::Raw yp = P::load_plain(pc + BW), ym = P::load_plain(pc - BW);
+                // The centre plane q is converted once; its y neighbours, the
+                // outer x neighbours, planes q -+ 1 and f0 enter the sums
+                // unconverted (mixed-precision add / subtract, same bits).
+                const T *pm = vm + c * vstride;
+                const typename P::Raw cr = P::load_plain(pc), zr = P::load_plain(vp + c * vstride),
+                                      mr = P::load_plain(pm), yp = P::load_plain(pc + BW),
+                                      ym = P::load_plain(pc - BW);
                 const unsigned xr = *reinterpret_cast<const unsigned short *>(pc + 4);
                 const unsigned xl = *reinterpret_cast<const unsigned short *>(pc - 1);
-                float lap[4];
+                float cen[4], lap[4];
+                P::unpack(cr, cen);
 #pragma unroll
-                for (int i = 0; i < 4; i++) lap[i] = -6.0f * cc[c][i];
-                lap[0] = lap[0] + cc[c][1];
-                lap[1] = lap[1] + cc[c][2];
-                lap[2] = lap[2] + cc[c][3];
+                for (int i = 0; i < 4; i++) lap[i] = -6.0f * cen[i];
+                lap[0] = lap[0] + cen[1];
+                lap[1] = lap[1] + cen[2];
+                lap[2] = lap[2] + cen[3];
                 lap[3] = add16<ST, 0>(xr, lap[3]);
                 lap[0] = add16<ST, 0>(xl, lap[0]);
-                lap[1] = lap[1] + cc[c][0];
-                lap[2] = lap[2] + cc[c][1];
-                lap[3] = lap[3] + cc[c][2];
+                lap[1] = lap[1] + cen[0];
+                lap[2] = lap[2] + cen[1];
+                lap[3] = lap[3] + cen[2];
                 lap[0] = add16v<ST, 0>(yp.u, lap[0]);
                 lap[1] = add16v<ST, 1>(yp.u, lap[1]);
                 lap[2] = add16v<ST, 2>(yp.u, lap[2]);
@@ -203,21 +211,28 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
                 lap[1] = add16v<ST, 1>(ym.u, lap[1]);
                 lap[2] = add16v<ST, 2>(ym.u, lap[2]);
                 lap[3] = add16v<ST, 3>(ym.u, lap[3]);
+                lap[0] = add16v<ST, 0>(zr.u, lap[0]);
+                lap[1] = add16v<ST, 1>(zr.u, lap[1]);
+                lap[2] = add16v<ST, 2>(zr.u, lap[2]);
+                lap[3] = add16v<ST, 3>(zr.u, lap[3]);
+                lap[0] = add16v<ST, 0>(mr.u, lap[0]);
+                lap[1] = add16v<ST, 1>(mr.u, lap[1]);
+                lap[2] = add16v<ST, 2>(mr.u, lap[2]);
+                lap[3] = add16v<ST, 3>(mr.u, lap[3]);
                 // (f0 - v) * |f0|^2 added is (v - f0) * |f0|^2 subtracted, bit for bit
                 float d[4];
-                d[0] = sub16v<ST, 0>(fr[c].u, cc[c][0]);
-                d[1] = sub16v<ST, 1>(fr[c].u, cc[c][1]);
-                d[2] = sub16v<ST, 2>(fr[c].u, cc[c][2]);
-                d[3] = sub16v<ST, 3>(fr[c].u, cc[c][3]);
+                d[0] = sub16v<ST, 0>(fraw[c].u, cen[0]);
+                d[1] = sub16v<ST, 1>(fraw[c].u, cen[1]);
+                d[2] = sub16v<ST, 2>(fraw[c].u, cen[2]);
+                d[3] = sub16v<ST, 3>(fraw[c].u, cen[3]);
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
-                    float l = lap[i] + zp[i];
-                    l = l + cm[c][i];
-                    const float upd = mu * l + d[i] * sqr[i];
-                    res[i] = cc[c][i] + upd;
+                    const float upd = mu * lap[i] + d[i] * sqr[i];
+                    res[i] = cen[i] + upd;
                 }
             } else {
                 float yp[4], ym[4];
+                P::unpack(P::load_plain(vp + c * vstride), zp);
                 P::unpack(P::load_plain(pc + BW), yp);
                 P::unpack(P::load_plain(pc - BW), ym);
                 const float xr = Store<ST>::load(pc[4]);
@@ -241,16 +256,21 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
             if (out_ok) {
                 T *oc = o + c * n;
                 P::store(oc, res);
-                if (dup_lo) P::store(oc - 2 * plane, res);
-                if (dup_hi) P::store(oc + 2 * plane, res);
+                if (__builtin_expect(dup_lo | dup_hi, 0)) {     // uniform: two planes of the volume
+                    if (dup_lo) P::store(oc - 2 * plane, res);
+                    if (dup_hi) P::store(oc + 2 * plane, res);
+                }
             }
+            if constexpr (!MIX) {
 #pragma unroll
-            for (int i = 0; i < 4; i++) {
-                cm[c][i] = cc[c][i];
-                cc[c][i] = zp[i];
+                for (int i = 0; i < 4; i++) {
+                    cm[c][i] = cc[c][i];
+                    cc[c][i] = zp[i];
+                }
             }
         }
         o += plane;
+        sm = sc;
         sc = sp;
         sp = sp + 1 == RV ? 0 : sp + 1;
         pp ^= sp == 0;
