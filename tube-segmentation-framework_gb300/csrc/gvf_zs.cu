@@ -6,8 +6,14 @@
 // loads, waits, computes and exits; the resident blocks of an SM move through
 // those phases together, so HBM idles while they compute and the issue slots
 // idle while they wait.  Here a CTA owns an x-y tile and a run of z planes;
-// one thread keeps the copies of the next planes in flight while all threads
-// compute the current one, so memory traffic and arithmetic overlap.
+// one thread keeps the copies of the next planes in flight while the compute
+// warps work on the current one, so memory traffic and arithmetic overlap.
+// Synchronisation (template flag WS): FP32 / snorm16 -- thread 0 of the
+// compute warps issues the copies and the CTA meets at a barrier after every
+// plane, which frees that plane's slots; FP16 / BF16 -- a ninth warp issues
+// the copies and each compute warp releases a slot on the slot's "empty"
+// mbarrier (arrival count 8) when done with it, so warps drift up to three
+// planes apart instead of waiting for the slowest every plane.
 //
 // Work: tile TX x TY = 128 x 8 outputs, one warp per tile row, 4 consecutive
 // voxels per lane.  The tiles of
@@ -57,7 +63,7 @@ template <int ST> struct ZsCfg {
     static constexpr int FBOX = TX * TY * 3 * ES;
     static constexpr int VSLOT = (VBOX + 127) / 128 * 128;
     static constexpr int FSLOT = (FBOX + 127) / 128 * 128;
-    static constexpr int SMEM = RV * VSLOT + RF * FSLOT + (RV + RF) * 8 + 16;
+    static constexpr int SMEM = RV * VSLOT + RF * FSLOT + 2 * (RV + RF) * 8 + 16;
     static constexpr int THREADS = 32 * TY;
     static constexpr int MIN_CTAS = ES == 2 ? 3 : 2;       // resident CTAs per SM the shared memory allows
     static constexpr int BYTES = 4 * ES;                   // one lane's 4 voxels
@@ -73,8 +79,8 @@ __device__ __forceinline__ void zs_issue(unsigned char *slot, uint64_t *bar, int
     tma_load_4d(slot, map, bar, x, y, z, 0);
 }
 
-template <int ST>
-__global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
+template <int ST, bool WS>
+__global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
                                                                    const __grid_constant__ CUtensorMap tf,
                                                                    typename Store<ST>::T *__restrict__ dst, int X,
                                                                    int Y, int Z, float mu, int ntx, int K) {
@@ -90,6 +96,8 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
     unsigned char *fring = smem + RV * C::VSLOT;
     uint64_t *vbar = reinterpret_cast<uint64_t *>(fring + RF * C::FSLOT);
     uint64_t *fbar = vbar + RV;
+    uint64_t *vemp = fbar + RF;                           // WS: slot released by the 8 compute warps
+    uint64_t *femp = vemp + RV;
 
     // this CTA's tile and plane range
     const int col = blockIdx.x / K, chunk = blockIdx.x % K;
@@ -102,11 +110,18 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
     const int tid = threadIdx.x;
 
     // v load j = plane qa-1+j into slot j % RV; f load j = plane qa+j into slot j % RF
-    int issued_v = 0, issued_f = 0;                       // meaningful in thread 0 only
+    int issued_v = 0, issued_f = 0;                       // meaningful in the issuing thread only
     // The next iteration's CTAs may be scheduled as this grid's CTAs exit
     // (programmatic dependent launch): they run this prologue, then wait below.
     pdl_trigger();
-    if (tid == 0) {
+    if (WS && tid == 0) {
+        for (int i = 0; i < RV; i++) mbar_init(vbar + i, 1);
+        for (int i = 0; i < RF; i++) mbar_init(fbar + i, 1);
+        for (int i = 0; i < RV; i++) mbar_init(vemp + i, TY);
+        for (int i = 0; i < RF; i++) mbar_init(femp + i, TY);
+        fence_mbar_init();
+    }
+    if (!WS && tid == 0) {
         tma_prefetch_desc(&tv);
         tma_prefetch_desc(&tf);
         for (int i = 0; i < RV; i++) mbar_init(vbar + i, 1);
@@ -124,6 +139,51 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
     __syncthreads();
 
     const int lane = tid & 31, r = tid >> 5;
+    if constexpr (WS) {
+        if (r == TY) {
+            // the copy warp: one lane issues v load j (plane qa-1+j) into slot
+            // j % RV and f load j (plane qa+j) into slot j % RF, each once the
+            // compute warps have released the slot's previous load; order v0,
+            // v1, then (v_{i+2}, f_i), the order of need
+            if (lane == 0) {
+                tma_prefetch_desc(&tv);
+                tma_prefetch_desc(&tf);
+                // the previous grid (which wrote src and reads dst) has
+                // completed and its writes are visible; the compute warps
+                // touch global memory only after copies issued below land
+                pdl_wait();
+                bool pok = true;
+                for (int i = -2; pok && i < nf; i++) {
+                    const int j = i + 2, sv = j % RV;
+                    if (j >= RV) pok = mbar_wait(vemp + sv, ((j / RV) - 1) & 1);
+                    if (!pok) break;
+                    fence_proxy_async_smem();
+                    zs_issue(vring + sv * C::VSLOT, vbar + sv, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + j);
+                    issued_v = j + 1;
+                    if (i < 0) continue;
+                    const int sf_ = i % RF;
+                    if (i >= RF) pok = mbar_wait(femp + sf_, ((i / RF) - 1) & 1);
+                    if (!pok) break;
+                    fence_proxy_async_smem();
+                    zs_issue(fring + sf_ * C::FSLOT, fbar + sf_, C::FBOX, &tf, x0, y0, qa + i);
+                    issued_f = i + 1;
+                }
+                if (!pok) {
+                    // record the failure and wait (bounded) for the copies in flight
+                    atomicOr(&g_gvf_zs_error, 1);
+                    for (int sl = 0; sl < RV; sl++) {
+                        int j = issued_v - 1 - ((issued_v - 1 - sl) % RV + RV) % RV;
+                        if (j >= 0) mbar_wait(vbar + sl, (j / RV) & 1);
+                    }
+                    for (int sl = 0; sl < RF; sl++) {
+                        int j = issued_f - 1 - ((issued_f - 1 - sl) % RF + RF) % RF;
+                        if (j >= 0) mbar_wait(fbar + sl, (j / RF) & 1);
+                    }
+                }
+            }
+            return;
+        }
+    }
     const int xc = x0 + 4 * lane, y = y0 + r;
     const bool out_ok = xc < X && y < Y;
     const bool fix_lo = xc == 0, fix_hi = xc + 4 == X;   // vectors holding x = 0 / X-1
@@ -156,6 +216,12 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
         const int q = qa + k;
         ok &= mbar_wait(vbar + sp, pp);
         ok &= mbar_wait(fbar + sf, pf);
+        if constexpr (WS) {
+            if (__any_sync(0xffffffffu, !ok)) {
+                ok = false;
+                break;
+            }
+        }
         const T *vm = reinterpret_cast<const T *>(vring + sm * C::VSLOT) + voff;
         const T *vc = reinterpret_cast<const T *>(vring + sc * C::VSLOT) + voff;
         const T *vp = reinterpret_cast<const T *>(vring + sp * C::VSLOT) + voff;
@@ -270,12 +336,21 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
             }
         }
         o += plane;
+        if constexpr (WS) {
+            // this warp is done with v load k (plane q-1) and f load k
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(vemp + sm);
+                mbar_arrive(femp + sf);
+            }
+        }
         sm = sc;
         sc = sp;
         sp = sp + 1 == RV ? 0 : sp + 1;
         pp ^= sp == 0;
         sf = sf + 1 == RF ? 0 : sf + 1;
         pf ^= sf == 0;
+        if constexpr (WS) continue;
         // slots k % RV (v) and k % RF (f) are free once every thread is here
         if (__syncthreads_or(!ok)) {
             ok = false;
@@ -295,9 +370,9 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS, ZsCfg<ST>::MIN_CTAS) gvf_z
             }
         }
     }
-    if (!ok && tid == 0) {
-        // record the failure and wait (bounded) for this CTA's copies in flight
-        atomicOr(&g_gvf_zs_error, 1);
+    if (!ok && lane == 0) atomicOr(&g_gvf_zs_error, 1);
+    if (!WS && !ok && tid == 0) {
+        // wait (bounded) for this CTA's copies in flight
         for (int s = 0; s < RV; s++) {
             int j = issued_v - 1 - ((issued_v - 1 - s) % RV + RV) % RV;
             if (j >= 0) mbar_wait(vbar + s, (j / RV) & 1);
@@ -354,7 +429,7 @@ template <int ST> struct ZsLaunch {
     int grid = 0, ntx = 0, K = 0;
 };
 
-template <int ST>
+template <int ST, bool WS>
 static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
     using C = ZsCfg<ST>;
     static int blocks_per_sm[4] = {-1, -1, -1, -1};
@@ -363,10 +438,10 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
     {
         std::lock_guard<std::mutex> lock(mu);
         if (blocks_per_sm[ST] < 0) {
-            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               C::SMEM));
             int bps = 0;
-            TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST>, C::THREADS,
+            TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST, WS>, C::THREADS + 32 * WS,
                                                                        C::SMEM));
             int dev = 0;
             TSF_TRY_CUDA(cudaGetDevice(&dev));
@@ -390,29 +465,35 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
 
 // One iteration src -> dst with the streaming kernel (caller checked
 // gvf_zs_eligible).
-template <int ST>
+template <int ST, bool WS>
 static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
                            cudaStream_t s) {
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     ZsLaunch<ST> g;
-    int r = zs_geometry<ST>(X, Y, Z, g);
+    int r = zs_geometry<ST, WS>(X, Y, Z, g);
     if (r) return r;
     CUtensorMap tv, tf;
     if (!encode_planar(&tv, src, X, Y, Z, C::ES, C::BW, C::TY + 2) ||
         !encode_planar(&tf, d_f0, X, Y, Z, C::ES, C::TX, C::TY))
         return fail(TSF_ERR_CUDA, "tensor map encoding failed");
     cudaLaunchAttribute attr[1];
-    const cudaLaunchConfig_t cfg = pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS), C::SMEM, s, attr);
-    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+    const cudaLaunchConfig_t cfg =
+        pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS + 32 * WS), C::SMEM, s, attr);
+    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
     return TSF_OK;
 }
 
 int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
                   cudaStream_t s) {
     int r = TSF_OK;
+    // 16-bit float formats: a copy warp and per-slot release barriers (the
+    // compute warps drift up to three planes apart instead of meeting at a
+    // CTA barrier every plane).  FP32 and snorm16 measured faster with the
+    // CTA barrier (FP32 is at the copy bandwidth; snorm16's extra warp
+    // pushes its registers into spills).
     TSF_DISPATCH_STORAGE(st, ST, {
-        r = launch_zs_typed<ST>(d_f0, src, dst, X, Y, Z, mu, s);
+        r = launch_zs_typed<ST, ST == TSF_STORE_F16 || ST == TSF_STORE_BF16>(d_f0, src, dst, X, Y, Z, mu, s);
     });
     TSF_CHECK_LAUNCH("gvf_zs_kernel");
     return r;
