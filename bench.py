@@ -688,6 +688,20 @@ def run_stage(args):
             e.record()
             torch.cuda.synchronize()
             out[name + "_us_per_iteration"] = round(a.elapsed_time(e) * 1e3 / args.iters, 2)
+        # the low-memory variant (three one-component passes; 4 stored values moved
+        # per component-voxel-iteration: v, f0_c and |f0|^2 read, v written)
+        _, f4 = T.vector_field(b, P["fmax"], P["vsign"], storage=st, planar=False, field4=True)
+        ows = T.workspace(T.load().tsf_gvf_one_component_workspace_size(n, n, n, T.STORAGE[st]))
+        T.gvf_one_component(f4, args.mu, args.iters, st, ws=ows)
+        torch.cuda.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        T.gvf_one_component(f4, args.mu, args.iters, st, ws=ows)
+        e.record()
+        torch.cuda.synchronize()
+        us = a.elapsed_time(e) * 1e3 / args.iters
+        out["one_component_us_per_iteration"] = round(us, 2)
+        out["one_component_gb_s"] = round(12 * (4 if st == "f32" else 2) * n ** 3 / (us * 1e-6) / 1e9, 1)
         return out
     v = T.gvf(f0, args.mu, args.iters, storage=st)
     field = T.gvf_finish(v, storage=st)

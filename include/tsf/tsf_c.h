@@ -206,6 +206,20 @@ int tsf_gvf_checkpointed(const void *d_f0, void *d_v, int X, int Y, int Z, float
 int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int storage,
                    void *stream);
 
+/* The reference's low-memory GVF (runLowMemoryGVF, gradientVectorFlow.cpp:1172-1300,
+ * kernels GVF3D{Init,Iteration,Finish}_one_component, kernels.cl:1392-1462 and
+ * kernels_no_3d_write.cl:1669-1741; chosen by the reference when the RGBA field
+ * exceeds the device's largest allocation, tube-segmentation.cpp:742-762): one
+ * component at a time, with |f0|^2 stored in the field's format (rounded to it in
+ * 16-bit formats), then the finish pass.  d_field4_in: the initial field4 image
+ * (tsf_vector_field's d_field4); d_field4_out: the result with w = |v|.  Workspace
+ * (6 N stored values) from tsf_gvf_one_component_workspace_size.  With FP32
+ * storage the result equals tsf_gvf + tsf_gvf_finish bit for bit. */
+size_t tsf_gvf_one_component_workspace_size(int X, int Y, int Z, int storage);
+int tsf_gvf_one_component(const void *d_field4_in, int X, int Y, int Z, float mu, int iterations,
+                          int storage, void *d_field4_out, void *d_workspace, size_t workspace_bytes,
+                          void *stream);
+
 /* ---------------------------------------------------------------------------
  * Tube detection filter
  * ------------------------------------------------------------------------- */

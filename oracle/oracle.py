@@ -83,6 +83,7 @@ def _declare(L):
         getattr(L, "orc_gvf_init" + s).argtypes = [_p, _i64, _p, _p]
         getattr(L, "orc_gvf" + s).argtypes = [_p, _p, _i, _i, _i, _f, _i, _i]
         getattr(L, "orc_gvf_finish" + s).argtypes = [_p, _i64, _i, _p]
+        getattr(L, "orc_gvf_one_component" + s).argtypes = [_p, _i, _i, _i, _f, _i, _i, _p]
         getattr(L, "orc_eig3" + s).argtypes = [_p, _p, _p]
         getattr(L, "orc_tdf_circle" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
         getattr(L, "orc_tdf_spline" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
@@ -212,6 +213,20 @@ def gvf_finish(v: np.ndarray, storage: str = "f32", f64: bool = False) -> np.nda
     _, Z, Y, X = v.shape
     out = np.empty((Z, Y, X, 4), dt)
     getattr(lib(), "orc_gvf_finish" + s)(_ptr(v), X * Y * Z, STORAGE[storage], _ptr(out))
+    return out
+
+
+def gvf_one_component(field4: np.ndarray, mu: float, iterations: int, storage: str = "f32",
+                      f64: bool = False) -> np.ndarray:
+    """runLowMemoryGVF (gradientVectorFlow.cpp:1172-1300, kernels
+    kernels_no_3d_write.cl:1669-1741): one component at a time with |f0|^2
+    stored, then the finish pass -> field4 [Z,Y,X,4]."""
+    dt, s = _real(f64)
+    field4 = np.ascontiguousarray(field4, dtype=dt)
+    Z, Y, X = field4.shape[:3]
+    out = np.empty((Z, Y, X, 4), dt)
+    getattr(lib(), "orc_gvf_one_component" + s)(_ptr(field4), X, Y, Z, float(mu), int(iterations),
+                                                STORAGE[storage], _ptr(out))
     return out
 
 

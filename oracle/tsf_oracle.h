@@ -81,6 +81,8 @@ int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, in
     void orc_gvf##S(const R *f_planar, R *v_planar, int X, int Y, int Z, float mu,       \
                     int iterations, int storage);                                       \
     void orc_gvf_finish##S(const R *v_planar, int64_t n, int storage, R *field4);       \
+    void orc_gvf_one_component##S(const R *field4, int X, int Y, int Z, float mu,        \
+                                  int iterations, int storage, R *out4);                \
     void orc_eig3##S(const R A[9], R V[9], R d[3]);                                     \
     void orc_tdf_circle##S(const R *field4, int X, int Y, int Z, float rMin, float rMax,  \
                            float rStep, R *T, R *radius);                               \

@@ -164,6 +164,57 @@ void FN(orc_gvf_finish)(const REAL *v, int64_t n, int storage, REAL *field4) {
     }
 }
 
+/* Low-memory GVF, one component at a time (runLowMemoryGVF,
+ * gradientVectorFlow.cpp:1172-1300; GVF3DInit_one_component /
+ * GVF3DIteration_one_component / GVF3DFinish_one_component,
+ * kernels_no_3d_write.cl:1669-1741, image variant kernels.cl:1392-1462):
+ * per component c, v = f0_c and the init pair (f0_c, |f0|^2) are stored in
+ * `storage`, then
+ *   v <- v + (mu L - (v - f0_c) sq),  sq = the stored |f0|^2,
+ * `iterations` times with the mirror rule; finally w = |v| as GVF3DFinish. */
+void FN(orc_gvf_one_component)(const REAL *field4, int X, int Y, int Z, float mu_, int iterations,
+                               int storage, REAL *out4) {
+    const int64_t n = (int64_t)X * Y * Z;
+    const REAL mu = (REAL)mu_;
+    REAL *v = (REAL *)malloc(sizeof(REAL) * 3 * (size_t)n);
+    REAL *w = (REAL *)malloc(sizeof(REAL) * (size_t)n);
+    REAL *f = (REAL *)malloc(sizeof(REAL) * (size_t)n);
+    REAL *sq = (REAL *)malloc(sizeof(REAL) * (size_t)n);
+    for (int c = 0; c < 3; c++) {
+        REAL *vc = v + c * n;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) {
+            const REAL a = field4[4 * i + 0], b = field4[4 * i + 1], d = field4[4 * i + 2];
+            vc[i] = f[i] = Q_(field4[4 * i + c], storage);
+            sq[i] = Q_((a * a + b * b) + d * d, storage);
+        }
+        REAL *src = vc, *dst = w;
+        for (int it = 0; it < iterations; it++) {
+#pragma omp parallel for schedule(static)
+            for (int z = 0; z < Z; z++)
+                for (int y = 0; y < Y; y++)
+                    for (int x = 0; x < X; x++) {
+                        int px = FN(mirror)(x, X), py = FN(mirror)(y, Y), pz = FN(mirror)(z, Z);
+                        int64_t p = IDX(px, py, pz);
+                        REAL vv = src[p];
+                        REAL lap = (REAL)(-6) * vv;
+                        lap = lap + src[IDX(FN(clampi)(px + 1, X), py, pz)];
+                        lap = lap + src[IDX(FN(clampi)(px - 1, X), py, pz)];
+                        lap = lap + src[IDX(px, FN(clampi)(py + 1, Y), pz)];
+                        lap = lap + src[IDX(px, FN(clampi)(py - 1, Y), pz)];
+                        lap = lap + src[IDX(px, py, FN(clampi)(pz + 1, Z))];
+                        lap = lap + src[IDX(px, py, FN(clampi)(pz - 1, Z))];
+                        REAL upd = mu * lap - (vv - f[p]) * sq[p];
+                        dst[IDX(x, y, z)] = Q_(vv + upd, storage);
+                    }
+            REAL *t = src; src = dst; dst = t;
+        }
+        if (src != vc) memcpy(vc, src, sizeof(REAL) * (size_t)n);
+    }
+    FN(orc_gvf_finish)(v, n, storage, out4);
+    free(v); free(w); free(f); free(sq);
+}
+
 /* ---------------------------------------------------------------------------
  * 3x3 symmetric eigen-decomposition: Householder tridiagonalisation followed by
  * the implicit QL method (the EISPACK tred2/tql2 procedures of Bowdler, Martin,

@@ -34,6 +34,9 @@ size_t gvf_workspace_size(int X, int Y, int Z, int st);
 int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st, void *ws,
             size_t ws_bytes, int mode, cudaStream_t s);
 int launch_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int st, cudaStream_t s);
+size_t gvf_one_workspace_size(int X, int Y, int Z, int st);
+int run_gvf_one_component(const void *d_field4_in, int X, int Y, int Z, float mu, int iterations, int st,
+                          void *d_field4_out, void *ws, size_t ws_bytes, cudaStream_t s);
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
                       void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, void *ws = nullptr,
                       size_t ws_bytes = 0);
@@ -100,6 +103,17 @@ int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int
 
 int tsf_gvf_finish(const void *d_v, void *d_field4, int X, int Y, int Z, int storage, void *stream) {
     return launch_gvf_finish(d_v, d_field4, X, Y, Z, storage, S(stream));
+}
+
+size_t tsf_gvf_one_component_workspace_size(int X, int Y, int Z, int storage) {
+    if (!valid_storage(storage) || X <= 0 || Y <= 0 || Z <= 0) return 0;
+    return gvf_one_workspace_size(X, Y, Z, storage);
+}
+
+int tsf_gvf_one_component(const void *d_field4_in, int X, int Y, int Z, float mu, int iterations, int storage,
+                          void *d_field4_out, void *d_workspace, size_t workspace_bytes, void *stream) {
+    return run_gvf_one_component(d_field4_in, X, Y, Z, mu, iterations, storage, d_field4_out, d_workspace,
+                                 workspace_bytes, S(stream));
 }
 
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,

@@ -107,6 +107,8 @@ def _declare(L):
         "tsf_compact_workspace_size": (_sz, [_i, _i, _i]),
         "tsf_compact_mask": (_i, [_p, _i, _i, _i, _p, _i64, _p, _p, _sz, _p]),
         "tsf_gvf_fmg_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_gvf_one_component_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_gvf_one_component": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
     }
     for name, (res, args) in sig.items():
@@ -542,6 +544,19 @@ def gvf_fmg(field4, mu: float, iterations: int, storage: str = "f32", ws=None, s
     out = torch.empty_like(field4)
     _check(L.tsf_gvf_fmg(_ptr(field4), _ptr(out), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
                          _ptr(ws), ws.numel(), _stream(stream)))
+    return out
+
+
+def gvf_one_component(field4, mu: float, iterations: int, storage: str = "f32", ws=None, stream=None):
+    """The low-memory GVF (tsf_gvf_one_component): field4 in, field4 (w = |v|) out."""
+    torch = _torch()
+    Z, Y, X = field4.shape[:3]
+    L = load()
+    need = L.tsf_gvf_one_component_workspace_size(X, Y, Z, STORAGE[storage])
+    ws = workspace(need) if ws is None else ws
+    out = torch.empty_like(field4)
+    _check(L.tsf_gvf_one_component(_ptr(field4), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
+                                   _ptr(out), _ptr(ws), ws.numel(), _stream(stream)))
     return out
 
 
