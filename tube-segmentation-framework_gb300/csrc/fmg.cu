@@ -201,14 +201,16 @@ __global__ void fmg_finish_kernel(const ST_T<ST> *fx, const ST_T<ST> *fy, const 
 }
 
 // ---------------------------------------------------------------------------
-// vectorised level kernels: one thread per 16-byte vector of a row (8 voxels
-// of a 16-bit format, 4 of FP32), loads issued together, x-neighbours by
+// vectorised level kernels: one thread per 4 voxels of a row (an 8-byte vector
+// of a 16-bit format, 16 bytes of FP32; 8-byte vectors measured 5 % faster
+// than 16-byte ones for 16-bit formats: half the registers per thread, twice
+// the resident warps), loads issued together, x-neighbours by
 // shuffles.  Rows evaluate at mirror(y), planes at mirror(z); the vector
 // holding x = 0 / X-1 copies the result of x = 2 / X-3.  Per voxel the
 // arithmetic is exactly the scalar kernels', so the results are identical.
 // ---------------------------------------------------------------------------
 template <int ST> struct FmgVec {
-    using P = PackedV<ST, 16>;
+    using P = PackedV<ST, ST == TSF_STORE_F32 ? 16 : 8>;
     using Raw = typename P::Raw;
     static constexpr int VX = P::VX;
 };
@@ -462,7 +464,7 @@ template <int ST> struct FmgRun {
     T *buf(size_t off) const { return reinterpret_cast<T *>(ws + off); }
     static dim3 blk() { return dim3(32, 4, 2); }
     static dim3 grd(Dim d) { return dim3((d.x + 31) / 32, (d.y + 3) / 4, (d.z + 1) / 2); }
-    // vectorised kernels: rows that split into at least two 16-byte vectors
+    // vectorised kernels: rows that split into at least two vectors
     static constexpr int VX = FmgVec<ST>::VX;
     static bool vec(Dim d) { return d.x % VX == 0 && d.x >= 2 * VX; }
     static dim3 vblk() { return dim3(32, 8, 1); }
