@@ -839,6 +839,17 @@ def run_mra(args):
     out["step"] = {"ms": round(total, 3), "volumes_per_s": round(1000.0 / total, 4), "stages_ms": stages,
                    "gvox_iter_s": round(n ** 3 * K / (stages.get("gvf", total) * 1e-3) / 1e9, 1),
                    "n_vertices": int(pipe.last["n_vertices"])}
+    if args.accuracy:
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        field64, T64, R64, refv = fp64_vessel_method(O, vol, K, args.mu)
+        nv = min(pipe.last["n_vertices"], pipe.max_vertices)
+        out["fp64_agreement"] = dict(
+            fp64_agreement(T.to_float(pipe.field, st).cpu().numpy(), pipe.Tl.cpu().numpy(), pipe.Rl.cpu().numpy(),
+                           pipe.verts[:nv].cpu().numpy(), field64, T64, R64, refv),
+            oracle_s=round(time.perf_counter() - t0, 1))
+        del field64, T64, R64
     vol_d = pipe.vol.clone()
     del pipe
     torch.cuda.empty_cache()
@@ -980,6 +991,40 @@ def run_reference(args):
     return line
 
 
+def fp64_agreement(field4, Tg, Rg, verts, field64, T64, R64, ref_vertices):
+    """Errors of a GPU run (field4 as float [Z,Y,X,4], combined T and R, vertex
+    list) against the FP64 oracle run of the same method: GVF field (xyz) max
+    abs error, TDF abs errors (T in [0, 1]), radius agreement where both T are
+    positive, and the centerpoint (vertex) agreement."""
+    dF = np.abs(field4[..., :3].astype(np.float64) - field64[..., :3])
+    dT = np.abs(Tg.astype(np.float64) - T64)
+    both = (Tg > 0) & (T64 > 0)
+    vset, gset = set(map(tuple, ref_vertices.tolist())), set(map(tuple, verts.tolist()))
+    inter = len(vset & gset)
+    return {"gvf_max_abs_err": float(dF.max()), "gvf_mean_abs_err": float(dF.mean()),
+            "tdf_max_abs_err": float(dT.max()), "tdf_p999_abs_err": float(np.quantile(dT, 0.999)),
+            "tdf_mean_abs_err": float(dT.mean()), "tdf_frac_within_1e-3": float((dT <= 1e-3).mean()),
+            "radius_equal_frac": float((Rg[both] == R64[both]).mean()) if both.any() else 1.0,
+            "vertices": int(len(gset)), "fp64_vertices": int(len(vset)), "vertices_equal_fp64": inter,
+            "vertex_jaccard": round(inter / max(1, len(vset | gset)), 5),
+            "same_vertex_list": bool(np.array_equal(verts, ref_vertices))}
+
+
+def fp64_vessel_method(O, vol, iters, mu):
+    """The FP64 oracle run of the vessel-tree step (blur, vector field, small
+    and large TDF, combine, candidates) with the bench's parameters."""
+    P = PARAMS
+    b64 = O.blur(vol, P["large_blur"], f64=True)
+    f64 = O.vector_field(b64, P["fmax"], P["vsign"], "f32", f64=True)
+    field64 = O.gvf_finish(O.gvf(f64, mu, iters, f64=True), f64=True)
+    fs64 = O.vector_field(vol.astype(np.float64), P["fmax"], P["vsign"], "f32", f64=True)
+    Ts64, Rs64 = O.tdf_circle(fs64, P["rmin"], 3.0, 0.5, f64=True)
+    Tl64, Rl64 = O.tdf_circle(field64, max(2.5, P["rmin"]), P["rmax"], P["rstep"], f64=True)
+    T64, R64 = O.combine(Ts64, Rs64, Tl64, Rl64, f64=True)
+    ref = O.centerpoints(T64, R64, field64, P["tdf_high"], P["cube_size"], f64=True)
+    return field64, T64, R64, ref["vertices"]
+
+
 def run_accuracy(args):
     """GVF field, TDF, centerpoint, centerline and segmentation agreement of the
     GPU path for each storage format against the FP64 oracle run of the same
@@ -1110,10 +1155,31 @@ def run_fmg_workload(args):
     names = ["tdf_small_and_fields", "fmg_gvf", "tdf_large", "candidates"]
     stages = {k: round(evs[i].elapsed_time(evs[i + 1]), 3) for i, k in enumerate(names)}
     total = evs[0].elapsed_time(evs[-1])
-    return {"workload": "lung-airway CT 512x512x400, FMG GVF %d cycles x 3 components, FP16 storage" % args.fmg_cycles,
-            "ms_per_volume": round(total, 3), "volumes_per_s": round(1000.0 / total, 3), "stages_ms": stages,
-            "kernel_launches": int(launches), "n_candidates": nc, "n_vertices": nv,
-            "lung_cropping": crop_timing(torch, T, hu, not args.no_cpu_baseline)}
+    res = {"workload": "lung-airway CT 512x512x400, FMG GVF %d cycles x 3 components, FP16 storage" % args.fmg_cycles,
+           "ms_per_volume": round(total, 3), "volumes_per_s": round(1000.0 / total, 3), "stages_ms": stages,
+           "kernel_launches": int(launches), "n_candidates": nc, "n_vertices": nv,
+           "lung_cropping": crop_timing(torch, T, hu, not args.no_cpu_baseline)}
+    if args.accuracy:
+        # the FP64 oracle run of the same method: small TDF on the unblurred
+        # field, blur, FMG GVF, large TDF, combine, candidates
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        v32 = synthetic.window_to_unit(hu)
+        fs64 = O.vector_field(v32.astype(np.float64), P["fmax"], P["vsign"], "f32", f64=True)
+        Ts64, Rs64 = O.tdf_circle(fs64, P["rmin"], 3.0, 0.5, f64=True)
+        del fs64
+        f64 = O.vector_field(O.blur(v32, P["blur"], f64=True), P["fmax"], P["vsign"], "f32", f64=True)
+        field64 = O.fmg_gvf(f64, 0.2, args.fmg_cycles, "f32", f64=True)
+        del f64
+        Tl64, Rl64 = O.tdf_circle(field64, 2.5, P["rmax"], P["rstep"], f64=True)
+        T64, R64 = O.combine(Ts64, Rs64, Tl64, Rl64, f64=True)
+        refv = O.centerpoints(T64, R64, field64, P["tdf_high"], P["cube_size"], f64=True)["vertices"]
+        res["fp64_agreement"] = dict(
+            fp64_agreement(T.to_float(out, st).cpu().numpy(), Tl.cpu().numpy(), Rl.cpu().numpy(),
+                           verts[: min(nv, 1 << 16)].cpu().numpy(), field64, T64, R64, refv),
+            oracle_s=round(time.perf_counter() - t0, 1))
+    return res
 
 
 def crop_timing(torch, T, hu, with_cpu):
