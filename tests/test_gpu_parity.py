@@ -104,6 +104,20 @@ def test_gvf_modes_identical(torch_dev, tsf, synth, oracle, storage, shape):
     assert tsf.gvf_device_error() == 0
 
 
+@pytest.mark.parametrize("storage", ["f16", "f32"])
+def test_gvf_many_waves(torch_dev, tsf, oracle, synth, storage):
+    """256 tiles of 128 x 8 (X = 256, Y = 1024) fill few of the resident-CTA
+    slots in one wave, so the streaming kernel cuts each tile's planes into
+    several shorter z-chunks (several waves)."""
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, (40, 1024, 256), 6), 0.5)
+    ref4 = oracle.vector_field(vol, 0.2, 1, storage)
+    p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
+    v = tsf.gvf(p, 0.05, 6, storage)
+    assert np.array_equal(_np_stored(v, storage), oracle.gvf(ref4, 0.05, 6, storage))
+    assert tsf.gvf_device_error() == 0
+
+
 def test_gvf_minimum_extent(torch_dev, tsf, oracle):
     torch = torch_dev
     rng = np.random.default_rng(0)
