@@ -6,7 +6,9 @@ No GPU: the oracle's restatement is pinned against a pure-Python restatement
 of the three kernel texts on a small volume in every storage format, and, with
 FP32 storage, against the three-component GVF (identical by construction: only
 the stored |f0|^2 differs, and FP32 stores it exactly).
-GPU: tsf_gvf_one_component against the oracle, bit for bit."""
+GPU: tsf_gvf_one_component against the oracle, bit for bit -- rows that split
+into 16-byte vectors (X = 136: a ragged last warp; X = 256: whole warps) and
+rows that do not (X = 12 for 16-bit formats, 33)."""
 import numpy as np
 import pytest
 
@@ -74,7 +76,7 @@ def test_16bit_differs_only_by_the_stored_square(oracle, storage):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("storage", STORAGES)
-@pytest.mark.parametrize("shape", [(9, 10, 12), (20, 17, 33), (6, 40, 136)])
+@pytest.mark.parametrize("shape", [(9, 10, 12), (20, 17, 33), (6, 40, 136), (7, 12, 256)])
 def test_gpu_bitexact(tsf, oracle, storage, shape):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
