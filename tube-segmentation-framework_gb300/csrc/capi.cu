@@ -94,8 +94,9 @@ int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
     return run_gvf(d_f0, d_v, X, Y, Z, mu, iterations, storage, d_workspace, workspace_bytes, 0, S(stream));
 }
 
-// Same as tsf_gvf with a forced kernel choice (1 = one iteration per launch,
-// 2 = temporal blocking).  Used by the tests to show both give one result.
+// Same as tsf_gvf with a forced kernel choice (0 = default, 1 = the
+// register-vector / per-voxel kernels, 2 = same as 0).  Used by the tests to
+// show every kernel gives one result.
 int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int storage,
                  void *d_workspace, size_t workspace_bytes, int mode, void *stream) {
     return run_gvf(d_f0, d_v, X, Y, Z, mu, iterations, storage, d_workspace, workspace_bytes, mode, S(stream));
