@@ -181,7 +181,7 @@ __global__ void gvf_finish_kernel(const typename Store<ST>::T *__restrict__ v, v
 
 bool gvf_zs_eligible(int st, const void *d_f0, const void *a, const void *b, int X, int Y, int Z);
 int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
-                  cudaStream_t s);
+                  cudaStream_t s, int rev = 0);
 
 size_t gvf_workspace_size(int X, int Y, int Z, int st) {
     return (size_t)3 * (size_t)X * (size_t)Y * (size_t)Z * storage_bytes(st);
@@ -255,7 +255,11 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
     void *a = d_v, *b = ws;
     const bool zs = mode != 1 && gvf_zs_eligible(st, d_f0, a, b, X, Y, Z);
     for (int left = iterations; left > 0; left--) {
-        r = zs ? launch_gvf_zs(st, d_f0, a, b, X, Y, Z, mu, s) : launch_gvf_plain(st, d_f0, a, b, X, Y, Z, mu, s);
+        // alternate the streaming direction (16-bit float formats): each
+        // iteration starts on the planes the previous one wrote last, which
+        // are still in L2
+        const int rev = mode == 2 ? 0 : (iterations - left) & 1;
+        r = zs ? launch_gvf_zs(st, d_f0, a, b, X, Y, Z, mu, s, rev) : launch_gvf_plain(st, d_f0, a, b, X, Y, Z, mu, s);
         if (r) return r;
         void *t = a; a = b; b = t;
     }

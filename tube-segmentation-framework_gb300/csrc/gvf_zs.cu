@@ -13,7 +13,9 @@
 // plane, which frees that plane's slots; FP16 / BF16 -- a ninth warp issues
 // the copies and each compute warp releases a slot on the slot's "empty"
 // mbarrier (arrival count 8) when done with it, so warps drift up to three
-// planes apart instead of waiting for the slowest every plane.
+// planes apart instead of waiting for the slowest every plane; these also
+// stream downwards (rev) on every other iteration, so each iteration starts
+// on the planes the previous one wrote last, which are still in L2.
 //
 // Work: tile TX x TY = 128 x 8 outputs, one warp per tile row, 4 consecutive
 // voxels per lane.  The tiles of
@@ -84,13 +86,15 @@ template <int ST, bool WS>
 __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
                                                                    const __grid_constant__ CUtensorMap tf,
                                                                    typename Store<ST>::T *__restrict__ dst, int X,
-                                                                   int Y, int Z, float mu, int ntx, int K) {
+                                                                   int Y, int Z, float mu, int ntx, int K,
+                                                                   int rev) {
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     using P = PackedV<ST, C::BYTES>;
     // FP16 / BF16: 16-bit operands enter the sums through mixed-precision
     // instructions instead of separate conversions (same bits)
     constexpr bool MIX = ST == TSF_STORE_F16 || ST == TSF_STORE_BF16;
+    if constexpr (!WS) rev = 0;                           // the CTA-barrier variant streams upwards only
     constexpr int TX = C::TX, TY = C::TY, H = C::H, BW = C::BW, RV = C::RV, RF = C::RF;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *vring = smem;
@@ -159,14 +163,15 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     if (j >= RV) pok = mbar_wait(vemp + sv, ((j / RV) - 1) & 1);
                     if (!pok) break;
                     fence_proxy_async_smem();
-                    zs_issue(vring + sv * C::VSLOT, vbar + sv, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + j);
+                    zs_issue(vring + sv * C::VSLOT, vbar + sv, C::VBOX, &tv, x0 - H, y0 - 1,
+                             rev ? qb + 1 - j : qa - 1 + j);
                     issued_v = j + 1;
                     if (i < 0) continue;
                     const int sf_ = i % RF;
                     if (i >= RF) pok = mbar_wait(femp + sf_, ((i / RF) - 1) & 1);
                     if (!pok) break;
                     fence_proxy_async_smem();
-                    zs_issue(fring + sf_ * C::FSLOT, fbar + sf_, C::FBOX, &tf, x0, y0, qa + i);
+                    zs_issue(fring + sf_ * C::FSLOT, fbar + sf_, C::FBOX, &tf, x0, y0, rev ? qb - i : qa + i);
                     issued_f = i + 1;
                 }
                 if (!pok) {
@@ -192,7 +197,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     const int lr = ey - y0 + 1, fr = ey - y0;            // row in the v box / f box
     const int e = H + 4 * lane;                           // column of xc in the v box
     const int64_t n = (int64_t)X * Y * Z, plane = (int64_t)X * Y;
-    T *o = dst + (int64_t)y * X + xc + (int64_t)qa * plane;   // component 0, plane q
+    T *o = dst + (int64_t)y * X + xc + (int64_t)(rev ? qb : qa) * plane;   // component 0, plane q
     const int voff = lr * BW + e, vstride = (TY + 2) * BW;    // component c at voff + c * vstride
     const int foff = fr * TX + 4 * lane;
     bool ok = true;
@@ -214,7 +219,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     }
 
     for (int k = 0; k < nf; k++) {
-        const int q = qa + k;
+        const int q = rev ? qb - k : qa + k;
         ok &= mbar_wait(vbar + sp, pp);
         ok &= mbar_wait(fbar + sf, pf);
         if constexpr (WS) {
@@ -252,9 +257,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                 // The centre plane q is converted once; its y neighbours, the
                 // outer x neighbours, planes q -+ 1 and f0 enter the sums
                 // unconverted (mixed-precision add / subtract, same bits).
-                const T *pm = vm + c * vstride;
-                const typename P::Raw cr = P::load_plain(pc), zr = P::load_plain(vp + c * vstride),
-                                      mr = P::load_plain(pm), yp = P::load_plain(pc + BW),
+                // planes q+1 and q-1: the newest and the oldest slot upwards,
+                // the other way round downwards (rev)
+                const T *pzp = (rev ? vm : vp) + c * vstride, *pzm = (rev ? vp : vm) + c * vstride;
+                const typename P::Raw cr = P::load_plain(pc), zr = P::load_plain(pzp),
+                                      mr = P::load_plain(pzm), yp = P::load_plain(pc + BW),
                                       ym = P::load_plain(pc - BW);
                 const unsigned xr = *reinterpret_cast<const unsigned short *>(pc + 4);
                 const unsigned xl = *reinterpret_cast<const unsigned short *>(pc - 1);
@@ -336,7 +343,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                 }
             }
         }
-        o += plane;
+        o += rev ? -plane : plane;
         if constexpr (WS) {
             // this warp is done with v load k (plane q-1) and f load k
             __syncwarp();
@@ -475,7 +482,7 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
 // gvf_zs_eligible).
 template <int ST, bool WS>
 static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
-                           cudaStream_t s) {
+                           cudaStream_t s, int rev) {
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     ZsLaunch<ST> g;
@@ -488,12 +495,13 @@ static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, 
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg =
         pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS + 32 * WS), C::SMEM, s, attr);
-    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K,
+                                    WS ? rev : 0));
     return TSF_OK;
 }
 
 int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
-                  cudaStream_t s) {
+                  cudaStream_t s, int rev) {
     int r = TSF_OK;
     // 16-bit float formats: a copy warp and per-slot release barriers (the
     // compute warps drift up to three planes apart instead of meeting at a
@@ -501,7 +509,7 @@ int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, i
     // CTA barrier (FP32 is at the copy bandwidth; snorm16's extra warp
     // pushes its registers into spills).
     TSF_DISPATCH_STORAGE(st, ST, {
-        r = launch_zs_typed<ST, ST == TSF_STORE_F16 || ST == TSF_STORE_BF16>(d_f0, src, dst, X, Y, Z, mu, s);
+        r = launch_zs_typed<ST, ST == TSF_STORE_F16 || ST == TSF_STORE_BF16>(d_f0, src, dst, X, Y, Z, mu, s, rev);
     });
     TSF_CHECK_LAUNCH("gvf_zs_kernel");
     return r;
