@@ -255,9 +255,8 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
     void *a = d_v, *b = ws;
     const bool zs = mode != 1 && gvf_zs_eligible(st, d_f0, a, b, X, Y, Z);
     for (int left = iterations; left > 0; left--) {
-        // alternate the streaming direction (16-bit float formats): each
-        // iteration starts on the planes the previous one wrote last, which
-        // are still in L2
+        // alternate the streaming direction: each iteration starts on the
+        // planes the previous one wrote last, which are still in L2
         const int rev = mode == 2 ? 0 : (iterations - left) & 1;
         r = zs ? launch_gvf_zs(st, d_f0, a, b, X, Y, Z, mu, s, rev) : launch_gvf_plain(st, d_f0, a, b, X, Y, Z, mu, s);
         if (r) return r;

@@ -13,9 +13,11 @@
 // plane, which frees that plane's slots; FP16 / BF16 -- a ninth warp issues
 // the copies and each compute warp releases a slot on the slot's "empty"
 // mbarrier (arrival count 8) when done with it, so warps drift up to three
-// planes apart instead of waiting for the slowest every plane; these also
-// stream downwards (rev) on every other iteration, so each iteration starts
-// on the planes the previous one wrote last, which are still in L2.
+// planes apart instead of waiting for the slowest every plane.  Both stream
+// downwards (rev) on every other iteration, so each iteration starts on the
+// planes the previous one wrote last, which are still in L2; downwards the
+// newest ring slot holds plane q-1 and the oldest plane q+1, and the sums
+// keep the reference's order (z+1 before z-1).
 //
 // Work: tile TX x TY = 128 x 8 outputs, one warp per tile row, 4 consecutive
 // voxels per lane.  The tiles of
@@ -82,19 +84,18 @@ __device__ __forceinline__ void zs_issue(unsigned char *slot, uint64_t *bar, int
     tma_load_4d(slot, map, bar, x, y, z, 0);
 }
 
-template <int ST, bool WS>
+template <int ST, bool WS, bool REV>
 __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
                                                                    const __grid_constant__ CUtensorMap tf,
                                                                    typename Store<ST>::T *__restrict__ dst, int X,
-                                                                   int Y, int Z, float mu, int ntx, int K,
-                                                                   int rev) {
+                                                                   int Y, int Z, float mu, int ntx, int K) {
+    constexpr bool rev = REV;   // stream downwards (compile-time: no selects in the sums)
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     using P = PackedV<ST, C::BYTES>;
     // FP16 / BF16: 16-bit operands enter the sums through mixed-precision
     // instructions instead of separate conversions (same bits)
     constexpr bool MIX = ST == TSF_STORE_F16 || ST == TSF_STORE_BF16;
-    if constexpr (!WS) rev = 0;                           // the CTA-barrier variant streams upwards only
     constexpr int TX = C::TX, TY = C::TY, H = C::H, BW = C::BW, RV = C::RV, RF = C::RF;
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *vring = smem;
@@ -137,9 +138,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
         // barrier below
         pdl_wait();
         for (; issued_v < RV && issued_v < nv; issued_v++)
-            zs_issue(vring + issued_v * C::VSLOT, vbar + issued_v, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + issued_v);
+            zs_issue(vring + issued_v * C::VSLOT, vbar + issued_v, C::VBOX, &tv, x0 - H, y0 - 1,
+                     rev ? qb + 1 - issued_v : qa - 1 + issued_v);
         for (; issued_f < RF && issued_f < nf; issued_f++)
-            zs_issue(fring + issued_f * C::FSLOT, fbar + issued_f, C::FBOX, &tf, x0, y0, qa + issued_f);
+            zs_issue(fring + issued_f * C::FSLOT, fbar + issued_f, C::FBOX, &tf, x0, y0,
+                     rev ? qb - issued_f : qa + issued_f);
     }
     __syncthreads();
 
@@ -201,12 +204,13 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     const int voff = lr * BW + e, vstride = (TY + 2) * BW;    // component c at voff + c * vstride
     const int foff = fr * TX + 4 * lane;
     bool ok = true;
-    // FP32 / snorm16: the lane's z column (centre values of planes q-1 and
-    // q) is carried from the previous plane so each stored value is loaded
-    // and converted once as a centre.  FP16 / BF16 read planes q-1 and q+1
-    // from the ring each plane: they enter the sums unconverted.
+    // FP32 / snorm16: the lane's z column (centre values of the previous and
+    // the current plane) is carried from plane to plane so each stored value
+    // is loaded and converted once as a centre.  FP16 / BF16 read both
+    // neighbour planes from the ring each plane: they enter the sums
+    // unconverted.
     float cm[3][4], cc[3][4];
-    int sm = 0, sc = 1, sp = 2, sf = 0;                   // slots of v planes q-1, q, q+1 and f plane q
+    int sm = 0, sc = 1, sp = 2, sf = 0;                   // slots: previous, current, next v plane; f plane
     uint32_t pp = 0, pf = 0;                              // phase parity of the waits on sp, sf
     ok &= mbar_wait(vbar + 0, 0);
     ok &= mbar_wait(vbar + 1, 0);
@@ -319,8 +323,8 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     lap = lap + (i == 0 ? xl : cc[c][i > 0 ? i - 1 : 0]);
                     lap = lap + yp[i];
                     lap = lap + ym[i];
-                    lap = lap + zp[i];
-                    lap = lap + cm[c][i];
+                    lap = lap + (rev ? cm[c][i] : zp[i]);   // plane q+1
+                    lap = lap + (rev ? zp[i] : cm[c][i]);   // plane q-1
                     const float upd = mu * lap - (v - fv[c][i]) * sqr[i];
                     res[i] = v + upd;
                 }
@@ -368,12 +372,14 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
             fence_proxy_async_smem();
             if (issued_v < nv) {                          // issued_v == k + RV: the slot just freed
                 const int sl = issued_v % RV;
-                zs_issue(vring + sl * C::VSLOT, vbar + sl, C::VBOX, &tv, x0 - H, y0 - 1, qa - 1 + issued_v);
+                zs_issue(vring + sl * C::VSLOT, vbar + sl, C::VBOX, &tv, x0 - H, y0 - 1,
+                         rev ? qb + 1 - issued_v : qa - 1 + issued_v);
                 issued_v++;
             }
             if (issued_f < nf) {
                 const int sl = issued_f % RF;
-                zs_issue(fring + sl * C::FSLOT, fbar + sl, C::FBOX, &tf, x0, y0, qa + issued_f);
+                zs_issue(fring + sl * C::FSLOT, fbar + sl, C::FBOX, &tf, x0, y0,
+                         rev ? qb - issued_f : qa + issued_f);
                 issued_f++;
             }
         }
@@ -446,10 +452,12 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
     {
         std::lock_guard<std::mutex> lock(mu);
         if (blocks_per_sm[ST] < 0) {
-            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              C::SMEM));
+            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS, false>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
+            TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS, true>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
             int bps = 0;
-            TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST, WS>, C::THREADS + 32 * WS,
+            TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST, WS, false>, C::THREADS + 32 * WS,
                                                                        C::SMEM));
             int dev = 0;
             TSF_TRY_CUDA(cudaGetDevice(&dev));
@@ -495,8 +503,8 @@ static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, 
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg =
         pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS + 32 * WS), C::SMEM, s, attr);
-    TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K,
-                                    WS ? rev : 0));
+    if (rev) TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, true>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+    else TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, false>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
     return TSF_OK;
 }
 
