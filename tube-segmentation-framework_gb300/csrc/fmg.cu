@@ -254,12 +254,23 @@ __global__ void __launch_bounds__(256) gs_vec_kernel(const ST_T<ST> *src, ST_T<S
     pdl_trigger();
     pdl_wait();   // launched with pdl_config: the previous kernel's writes are visible
     FMG_VEC_PROLOGUE(d);
+    // FP16 / BF16: the y and z neighbours enter the sum unconverted
+    // (mixed-precision adds, the bits of convert-then-add)
+    constexpr bool MIX = ST == TSF_STORE_F16 || ST == TSF_STORE_BF16;
     float c[VX], yp[VX], ym[VX], zp[VX], zm[VX], rr[VX], qq[VX];
+    typename P::Raw ryp, rym, rzp, rzm;
     fmg_load<ST>(src, p, act, c);
-    fmg_load<ST>(src, p + sy, act, yp);
-    fmg_load<ST>(src, p - sy, act, ym);
-    fmg_load<ST>(src, p + sz, act, zp);
-    fmg_load<ST>(src, p - sz, act, zm);
+    if constexpr (MIX) {
+        ryp = act ? P::load(src + p + sy) : P::zero();
+        rym = act ? P::load(src + p - sy) : P::zero();
+        rzp = act ? P::load(src + p + sz) : P::zero();
+        rzm = act ? P::load(src + p - sz) : P::zero();
+    } else {
+        fmg_load<ST>(src, p + sy, act, yp);
+        fmg_load<ST>(src, p - sy, act, ym);
+        fmg_load<ST>(src, p + sz, act, zp);
+        fmg_load<ST>(src, p - sz, act, zm);
+    }
     fmg_load<ST>(r, p, act, rr);
     fmg_load<ST>(sq, p, act, qq);
     const float el = (act && x0 > 0) ? Store<ST>::load(src[p - 1]) : 0.0f;
@@ -276,10 +287,17 @@ __global__ void __launch_bounds__(256) gs_vec_kernel(const ST_T<ST> *src, ST_T<S
         } else {
             float s = i == VX - 1 ? xr : c[i + 1 < VX ? i + 1 : i];
             s = s + (i == 0 ? xl : c[i > 0 ? i - 1 : 0]);
-            s = s + yp[i];
-            s = s + ym[i];
-            s = s + zp[i];
-            s = s + zm[i];
+            if constexpr (MIX) {
+                s = add16i<ST>(ryp.u, i, s);
+                s = add16i<ST>(rym.u, i, s);
+                s = add16i<ST>(rzp.u, i, s);
+                s = add16i<ST>(rzm.u, i, s);
+            } else {
+                s = s + yp[i];
+                s = s + ym[i];
+                s = s + zp[i];
+                s = s + zm[i];
+            }
             const float num = two_mu * s - two_hh * rr[i];
             const float den = twelve_mu + hh * qq[i];
             res[i] = num / den;

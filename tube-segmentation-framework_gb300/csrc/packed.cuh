@@ -138,6 +138,12 @@ template <int K> __device__ __forceinline__ float sqadd16(unsigned u, float c) {
     return d;
 }
 
+// Element i of a packed 16-bit vector, i a run-time index that unrolling
+// turns into a constant (the branch folds away).
+template <int ST> __device__ __forceinline__ float add16i(const unsigned *u, int i, float c) {
+    return (i & 1) ? add16<ST, 1>(u[i >> 1], c) : add16<ST, 0>(u[i >> 1], c);
+}
+
 // Element i (0..3) of a packed 4-element 16-bit vector.
 template <int ST, int I> __device__ __forceinline__ float add16v(const unsigned *u, float c) {
     return add16<ST, I & 1>(u[I >> 1], c);
