@@ -40,7 +40,7 @@ def _u16(t):
     return t.cpu().numpy().view(np.uint16)
 
 
-@pytest.mark.parametrize("sigma", [0.5, 1.0, 2.5])
+@pytest.mark.parametrize("sigma", [0.5, 1.0, 1.5, 2.0, 2.5])
 def test_blur_bitexact(torch_dev, tsf, oracle, synth, sigma):
     torch = torch_dev
     vol = _vol(synth, (20, 24, 36), 1)

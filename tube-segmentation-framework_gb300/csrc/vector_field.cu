@@ -65,6 +65,45 @@ __global__ void __launch_bounds__(256) blur_kernel(const float *__restrict__ in,
     out[lin(x, y, z, X, Y)] = sum;
 }
 
+// The same blur with the half width fixed at compile time: voxels whose
+// (2M+1)^3 neighbourhood lies inside the volume take fully unrolled loops (the
+// weights become constant operands, the row offsets immediates, no clamps);
+// the others take the clamped loops.  Same weights, same order (z outer, then
+// y, then x), so the same bits as blur_kernel.
+template <int M>
+__global__ void __launch_bounds__(256) blur_m_kernel(const float *__restrict__ in, float *__restrict__ out,
+                                                     int X, int Y, int Z, const BlurMask mask) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= X || y >= Y || z >= Z) return;
+    constexpr int S = 2 * M + 1;
+    float sum = 0.0f;
+    if (x >= M && x + M < X && y >= M && y + M < Y && z >= M && z + M < Z) {
+        const float *base = in + lin(x, y, z, X, Y);
+        const int64_t sy = X, sz = (int64_t)X * Y;
+#pragma unroll
+        for (int c = -M; c <= M; c++) {
+#pragma unroll
+            for (int b = -M; b <= M; b++) {
+                const float *row = base + c * sz + b * sy;
+#pragma unroll
+                for (int a = -M; a <= M; a++) sum = sum + mask.w[(a + M) + (b + M) * S + (c + M) * S * S] * __ldg(row + a);
+            }
+        }
+    } else {
+        for (int c = -M; c <= M; c++) {
+            const int zz = clampi(z + c, Z);
+            for (int b = -M; b <= M; b++) {
+                const float *row = in + lin(0, clampi(y + b, Y), zz, X, Y);
+                const float *wrow = mask.w + (b + M) * S + (c + M) * S * S + M;
+                for (int a = -M; a <= M; a++) sum = sum + wrow[a] * __ldg(row + clampi(x + a, X));
+            }
+        }
+    }
+    out[lin(x, y, z, X, Y)] = sum;
+}
+
 template <int ST>
 __global__ void __launch_bounds__(256) vector_field_kernel(const float *__restrict__ in, int X, int Y, int Z,
                                                            float fmax, float sg, void *planar, void *field4) {
@@ -108,7 +147,15 @@ int launch_blur(const float *d_in, float *d_out, int X, int Y, int Z, float sigm
     BlurMask mask;
     r = host_blur_mask(sigma, mask.w, &mask.m);
     if (r) return r;
-    blur_kernel<<<vox_grid(X, Y, Z), vox_block(), 0, s>>>(d_in, d_out, X, Y, Z, mask);
+    const dim3 g = vox_grid(X, Y, Z), b = vox_block();
+    switch (mask.m) {
+    case 1: blur_m_kernel<1><<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    case 2: blur_m_kernel<2><<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    case 3: blur_m_kernel<3><<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    case 4: blur_m_kernel<4><<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    case 5: blur_m_kernel<5><<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    default: blur_kernel<<<g, b, 0, s>>>(d_in, d_out, X, Y, Z, mask); break;
+    }
     TSF_CHECK_LAUNCH("blur_kernel");
     return TSF_OK;
 }
