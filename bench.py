@@ -19,9 +19,10 @@ Multi-GPU: the path does not shard here; --gpus N runs N independent
 replicas (one volume per GPU), value = sum over ranks.
 
 --impl reference: the CPU restatement of the reference's kernels (the oracle;
-the OpenCL reference cannot run on these machines) on all host cores, on a
-bounded sample of the same workload (full-size volume, GVF iterations reduced
-and extrapolated linearly).
+the OpenCL reference cannot run on these machines) on all host cores, --steps
+timed steps after --warmup untimed ones, each step the whole hot path with all
+GVF iterations on a bounded sample of the volume (a z-slab of it), so that
+the run ends within minutes.  Nothing is extrapolated.
 """
 from __future__ import annotations
 
@@ -55,7 +56,10 @@ def parse():
     ap.add_argument("--mu", type=float, default=0.05)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-gvf-iters", type=int, default=6)
+    ap.add_argument("--cpu-slab-planes-1core", type=int, default=8,
+                    help="z-planes of the one-core CPU baseline sample (0: skip)")
+    ap.add_argument("--reference-slab-planes", type=int, default=16,
+                    help="z-planes of the volume one reference-arm step processes")
     ap.add_argument("--accuracy", action="store_true",
                     help="instead of timing: errors of every storage format against the FP64 oracle")
     ap.add_argument("--fmg", action="store_true",
@@ -466,13 +470,19 @@ def run_tsf(args, rank, world):
     return res
 
 
-def fwd_adjoint_timing(torch, pipe, args):
+def fwd_adjoint_timing(torch, pipe, args, storage=None, checkpoint_every=None):
     """Forward (both TDF passes, GVF K iterations) and forward + hand-written
     adjoint of the loss mean((T - G)^2) with respect to the volume, mu and
-    sigma (sqrt(K) checkpointing), FP32 storage, on the benchmark volume."""
+    sigma, on the benchmark volume, in the benchmark's storage format with a
+    GVF checkpoint every ceil(sqrt(K)) iterations (the adjoint recomputes the
+    states between checkpoints)."""
+    import math
     import calibration as CAL
+    storage = storage or args.storage
+    C = checkpoint_every or int(math.ceil(math.sqrt(args.iters)))
     p = CAL.Params(mu=args.mu, sigma=PARAMS["large_blur"], iterations=args.iters, fmax=PARAMS["fmax"],
-                   rmin=PARAMS["rmin"], rmax=PARAMS["rmax"], rstep=PARAMS["rstep"])
+                   rmin=PARAMS["rmin"], rmax=PARAMS["rmax"], rstep=PARAMS["rstep"], checkpoint_every=C,
+                   storage=storage)
     vol = pipe.vol
     G = torch.zeros_like(vol)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -512,7 +522,7 @@ def fwd_adjoint_timing(torch, pipe, args):
         stages[name] = {"gpu_ms": round(prev.elapsed_time(e), 3), "host_ms": round((th - prev_h) * 1e3, 3)}
         prev, prev_h = e, th
     bw = {k: v["gpu_ms"] for k, v in stages.items() if k not in ("forward", "loss")}
-    return {"storage": "f32", "iterations": args.iters, "volume": list(vol.shape), "backward_ms": bw,
+    return {"storage": storage, "iterations": args.iters, "volume": list(vol.shape), "backward_ms": bw,
             "timed_stages": stages, "host_ms": round(t_host * 1e3, 3), "alloc_retries": int(retries),
             "checkpoint_every": int(state["checkpoint_every"]),
             "adjoint_workspace_gb": round(state["gvf_ws"].numel() / 1e9, 2),
@@ -928,10 +938,49 @@ def _traffic_from_profile(storage):
         return None
 
 
-def cpu_baseline(args, vol=None, reps=1):
-    """The oracle (CPU restatement of the reference kernels) on all host cores,
-    on the full-size volume with the GVF iterations reduced to
-    --cpu-gvf-iters and extrapolated linearly to the workload's count."""
+def cpu_path(O, vol, storage, iters, mu):
+    """One pass of the hot path through the oracle (the CPU restatement of the
+    reference's kernels) on whatever threads the oracle is set to use: blur,
+    vector fields, small-radius TDF, all `iters` GVF iterations, finish,
+    large-radius TDF, combine, candidate stage.  Returns per-stage seconds."""
+    P = PARAMS
+    t = {}
+    t0 = time.perf_counter()
+    b = O.blur(vol, P["large_blur"])
+    f_small = O.vector_field(vol, P["fmax"], P["vsign"], storage)
+    t["blur_vf_small"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    Ts, Rs = O.tdf_circle(f_small, P["rmin"], 3.0, 0.5)
+    t["tdf_small"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f4 = O.vector_field(b, P["fmax"], P["vsign"], storage)
+    t["vector_field"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    v = O.gvf(f4, mu, iters, storage)
+    t["gvf"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    field = O.gvf_finish(v, storage)
+    Tl, Rl = O.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"])
+    Tl, Rl = O.combine(Ts, Rs, Tl, Rl)
+    t["tdf_large"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.centerpoints(Tl, Rl, field, P["tdf_high"], P["cube_size"])
+    t["candidates"] = time.perf_counter() - t0
+    return t
+
+
+def slab(vol, planes):
+    """The middle `planes` z-planes of a volume (a bounded sample of the
+    workload: same rows, same per-voxel work)."""
+    z0 = (vol.shape[0] - planes) // 2
+    return np.ascontiguousarray(vol[z0:z0 + planes])
+
+
+def cpu_baseline(args, vol=None):
+    """The oracle (CPU restatement of the reference kernels) timed on the
+    host: the whole workload -- full volume, every stage, all GVF iterations
+    -- on all host cores, and a z-slab of it (all iterations) on one core.
+    Nothing is extrapolated."""
     import oracle as O
     import synthetic
     O.build()
@@ -939,55 +988,65 @@ def cpu_baseline(args, vol=None, reps=1):
         vol = synthetic.vascular_tree((args.size,) * 3, seed=args.seed)
     n = args.size
     N = n ** 3
-    P = PARAMS
     cores = O.get_threads()
-    k = args.cpu_gvf_iters
-    t = {}
-    t0 = time.perf_counter()
-    b = O.blur(vol, P["large_blur"])
-    f_small = O.vector_field(vol, P["fmax"], P["vsign"], args.storage)
-    t["blur_vf_small"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    Ts, Rs = O.tdf_circle(f_small, P["rmin"], 3.0, 0.5)
-    t["tdf_small"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    f4 = O.vector_field(b, P["fmax"], P["vsign"], args.storage)
-    t["vector_field"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    v = O.gvf(f4, args.mu, k, args.storage)
-    t_gvf_k = time.perf_counter() - t0
-    t["gvf_extrapolated"] = t_gvf_k * args.iters / k
-    t0 = time.perf_counter()
-    field = O.gvf_finish(v, args.storage)
-    Tl, Rl = O.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"])
-    Tl, Rl = O.combine(Ts, Rs, Tl, Rl)
-    t["tdf_large"] = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    try:
-        O.centerpoints(Tl, Rl, field, P["tdf_high"], P["cube_size"])
-    except Exception:
-        pass
-    t["candidates"] = time.perf_counter() - t0
+    t = cpu_path(O, vol, args.storage, args.iters, args.mu)
     total = sum(t.values())
-    measured = total - t["gvf_extrapolated"] + t_gvf_k
+    one = {}
+    planes = args.cpu_slab_planes_1core
+    if planes > 0:
+        sv = slab(vol, planes)
+        O.set_threads(1)
+        try:
+            t1 = cpu_path(O, sv, args.storage, args.iters, args.mu)
+        finally:
+            O.set_threads(cores)
+        tot1 = sum(t1.values())
+        one = {"value": round(sv.size * args.iters / tot1 / 1e9, 5), "unit": UNIT, "cores": 1,
+               "sample": "%dx%dx%d z-slab of the volume, every stage, all %d GVF iterations; %.1f s"
+                         % (n, n, planes, args.iters, tot1),
+               "stage_s": {a: round(b_, 3) for a, b_ in t1.items()}}
     return {"value": round(N * args.iters / total / 1e9, 5), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "full %d^3 volume and stages, GVF timed over %d of %d iterations and extrapolated "
-                      "linearly; %.1f s of CPU work measured" % (n, k, args.iters, measured),
-            "stage_s": {a: round(b_, 3) for a, b_ in t.items()}}
+            "sample": "the whole workload: %d^3 volume, every stage, all %d GVF iterations; %.1f s of CPU work"
+                      % (n, args.iters, total),
+            "stage_s": {a: round(b_, 3) for a, b_ in t.items()}, "one_core": one}
 
 
 def run_reference(args):
-    res = cpu_baseline(args)
-    line = {"metric": METRIC, "impl": "reference", "value": res["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": 1, "warmup": 0, "ms_per_step": round(args.size ** 3 * args.iters / res["value"] / 1e6, 1),
+    """The reference arm: the oracle on all host cores, K timed steps after W
+    warm-up steps, each step one pass of the hot path (all GVF iterations) over
+    a z-slab of the benchmark volume, so that the run stays within minutes."""
+    import oracle as O
+    import synthetic
+    O.build()
+    cores = O.get_threads()
+    n = args.size
+    vol = slab(synthetic.vascular_tree((n, n, n), seed=args.seed), args.reference_slab_planes)
+    for _ in range(args.warmup):
+        cpu_path(O, vol, args.storage, args.iters, args.mu)
+    times, stages = [], {}
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        st = cpu_path(O, vol, args.storage, args.iters, args.mu)
+        times.append(time.perf_counter() - t0)
+        for k_, v_ in st.items():
+            stages[k_] = stages.get(k_, 0.0) + v_ / args.steps
+    step_s = sum(times) / len(times)
+    value = vol.size * args.iters / step_s / 1e9
+    sample = ("%dx%dx%d z-slab of the %d^3 vessel tree per step, every stage, all %d GVF iterations"
+              % (n, n, vol.shape[0], n, args.iters))
+    line = {"metric": METRIC, "impl": "reference", "value": round(value, 5), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(step_s * 1e3, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 arithmetic, %s field storage" % args.storage, "data": "synthetic",
             "config": {"workload": "vessel tree %d^3, GVF %d iterations, mu %.2f, %s storage, full hot path"
-                                   % (args.size, args.iters, args.mu, args.storage),
-                       "implementation": "CPU restatement of the reference kernels (OpenCL reference cannot "
-                                         "run: no OpenCL platform on these machines)"},
-            "cpu_baseline": res,
-            "e2e": {"value": res["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                                   % (n, args.iters, args.mu, args.storage),
+                       "implementation": "CPU restatement of the reference kernels (the oracle); the OpenCL "
+                                         "reference cannot run: no OpenCL platform on these machines",
+                       "sample": sample},
+            "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "stage_s": {a: round(b_, 4) for a, b_ in stages.items()},
+            "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return line
 
 

@@ -52,7 +52,8 @@ enum {
                                   (parallelCenterlineExtraction.cpp:842-844,
                                   895-899)                                      */
     TSF_ERR_NOT_CONVERGED = 5, /* an iteration cap was reached                  */
-    TSF_ERR_CAPACITY = 6       /* an output buffer is too small                 */
+    TSF_ERR_CAPACITY = 6       /* an output buffer is too small, or the volume
+                                  exceeds tsf_gvf_static's fixed scratch array  */
 };
 
 /* Storage formats of vector fields.  F32 and SNORM16 are the reference's
@@ -164,8 +165,9 @@ int tsf_gvf_device_error(int clear);
  * components must fit in 96 MiB (256^3 voxels in a 16-bit format, 8,388,608
  * in FP32); larger volumes return TSF_ERR_CAPACITY.  The first call on a
  * device looks up the array's address with that device current -- make it
- * before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU race.  Allocates nothing. */
+ * before any stream capture; the address is kept for the process, so
+ * cudaDeviceReset between calls is not supported.  All calls share the
+ * array, so calls that overlap on the GPU race.  Allocates nothing. */
 int tsf_gvf_static(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                    int storage, void *stream);
 

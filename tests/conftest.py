@@ -15,7 +15,9 @@ for p in (os.path.join(ROOT, "tube-segmentation-framework_gb300"), os.path.join(
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REFERENCE = "/root/reference"
+# The reference source tree (smistad/Tube-Segmentation-Framework), where one is
+# checked out; tests that read it skip when it is absent.
+REFERENCE = os.environ.get("TSF_REFERENCE_DIR", "/root/reference")
 
 
 def pytest_configure(config):

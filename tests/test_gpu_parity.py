@@ -286,3 +286,21 @@ def test_invalid_arguments(torch_dev, tsf):
     f0 = torch.zeros((3, 8, 8, 8), device="cuda")
     with pytest.raises(tsf.TSFError, match="TSF_ERR_WORKSPACE"):
         tsf.gvf(f0, 0.05, 3, "f32", ws=torch.zeros(16, dtype=torch.uint8, device="cuda"))
+
+
+@pytest.mark.parametrize("storage", ["f16", "f32"])
+def test_gvf_on_two_devices(torch_dev, tsf, oracle, synth, storage):
+    """The streaming kernel's shared-memory attribute and occupancy figures
+    are kept per device: GVF on a second GPU of the same process, after the
+    first, gives the oracle's bits.  Skips with fewer than two GPUs."""
+    torch = torch_dev
+    if torch.cuda.device_count() < 2:
+        pytest.skip("needs two GPUs")
+    vol = oracle.blur(_vol(synth, (20, 24, 64), 11), 0.5)
+    ov = oracle.gvf(oracle.vector_field(vol, 0.2, 1, storage), 0.05, 9, storage)
+    for dev in (0, 1):
+        with torch.cuda.device(dev):
+            p, _ = tsf.vector_field(torch.from_numpy(vol).to(f"cuda:{dev}"), 0.2, 1, storage)
+            v = tsf.gvf(p, 0.05, 9, storage)
+            torch.cuda.synchronize()
+            assert np.array_equal(_np_stored(v, storage), ov)

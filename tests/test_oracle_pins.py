@@ -131,7 +131,8 @@ def test_gvf_f64_and_f32_agree_when_stable(oracle, synth):
 
 def test_gvf_unstable_at_mu_0_1(oracle, synth):
     """The explicit scheme needs 12 mu + |f0|^2 <= 2: at mu = 0.1 the
-    checkerboard mode grows where |f0| = 1 (documented in the design doc)."""
+    checkerboard mode, amplified by 1 - 12 mu - |f0|^2 per iteration, grows
+    where |f0| = 1; at mu = 0.08 it stays bounded."""
     vol = synth.vascular_tree((32, 32, 32), seed=0)
     f4 = oracle.vector_field(oracle.blur(vol, 0.5, f64=True), 0.2, 1, f64=True)
     assert np.abs(oracle.gvf(f4, 0.1, 150, f64=True)).max() > 10.0

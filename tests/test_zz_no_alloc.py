@@ -49,7 +49,11 @@ def test_static_scratch_matches_workspace_gvf(torch_dev, tsf, synth, storage, sh
     torch = torch_dev
     for k, shape in enumerate(shapes):            # two calls in a row
         f0 = _field(torch, tsf, synth, shape, 20 + k, storage)
+        tsf.load().tsf_gvf_device_error(1)
         got = _static(torch, tsf, f0, 0.05, 13, storage)
+        torch.cuda.synchronize()
+        # a copy that timed out in the streaming kernel shows here, not only as a mismatch
+        assert tsf.load().tsf_gvf_device_error(1) == 0
         ref = tsf.gvf(f0, 0.05, 13, storage)
         torch.cuda.synchronize()
         assert torch.equal(got, ref)

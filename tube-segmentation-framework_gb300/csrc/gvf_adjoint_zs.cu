@@ -304,20 +304,23 @@ int gvf_adjoint_zs_max_grid() {
 template <int ST>
 static int adj_zs_slots(int &slots) {
     using C = AdjZsCfg<ST>;
-    static int cached[4] = {-1, -1, -1, -1};
+    // per device: the shared-memory attribute applies to the current device
+    static int cached[kMaxDevices];
     static std::mutex mu;
+    int dev = 0;
+    TSF_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(TSF_ERR_INVALID_ARG, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(mu);
-    if (cached[ST] < 0) {
+    if (cached[dev] <= 0) {
         TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_adjoint_zs_kernel<ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           C::SMEM));
-        int bps = 0, dev = 0, nsm = 0;
+        int bps = 0, nsm = 0;
         TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_adjoint_zs_kernel<ST>, C::THREADS,
                                                                    C::SMEM));
-        TSF_TRY_CUDA(cudaGetDevice(&dev));
         TSF_TRY_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-        cached[ST] = (bps > 0 ? (bps > 4 ? 4 : bps) : 1) * nsm;
+        cached[dev] = (bps > 0 ? (bps > 4 ? 4 : bps) : 1) * nsm;
     }
-    slots = cached[ST];
+    slots = cached[dev];
     return TSF_OK;
 }
 

@@ -446,12 +446,17 @@ template <int ST> struct ZsLaunch {
 template <int ST, bool WS>
 static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
     using C = ZsCfg<ST>;
-    static int blocks_per_sm[4] = {-1, -1, -1, -1};
-    static int nsm = 0;
+    // The shared-memory attribute applies to the device that is current when
+    // it is set, so it and the occupancy figures are kept per device.
+    static int blocks_per_sm[kMaxDevices];
+    static int nsm[kMaxDevices];
     static std::mutex mu;
+    int dev = 0;
+    TSF_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(TSF_ERR_INVALID_ARG, "device ordinal out of range");
     {
         std::lock_guard<std::mutex> lock(mu);
-        if (blocks_per_sm[ST] < 0) {
+        if (blocks_per_sm[dev] <= 0) {
             TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS, false>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
             TSF_TRY_CUDA(cudaFuncSetAttribute(gvf_zs_kernel<ST, WS, true>,
@@ -459,16 +464,14 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
             int bps = 0;
             TSF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, gvf_zs_kernel<ST, WS, false>, C::THREADS + 32 * WS,
                                                                        C::SMEM));
-            int dev = 0;
-            TSF_TRY_CUDA(cudaGetDevice(&dev));
-            TSF_TRY_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-            blocks_per_sm[ST] = bps > 0 ? bps : 1;
+            TSF_TRY_CUDA(cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev));
+            blocks_per_sm[dev] = bps > 0 ? bps : 1;
         }
     }
     g.ntx = (X + C::TX - 1) / C::TX;
     const int nty = (Y + C::TY - 1) / C::TY;
     const int64_t cols = (int64_t)g.ntx * nty;
-    const int64_t slots = (int64_t)blocks_per_sm[ST] * nsm;
+    const int64_t slots = (int64_t)blocks_per_sm[dev] * nsm[dev];
     // One wave (tiles x chunks = the resident-CTA slots) when it fills at
     // least 80 % of the slots; otherwise (e.g. 256 tiles on 456 slots at
     // 512^3) about six waves of shorter chunks, so the scheduler backfills

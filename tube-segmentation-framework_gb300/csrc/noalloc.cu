@@ -16,7 +16,9 @@
 //    voxels in FP32.  Larger volumes are rejected with TSF_ERR_CAPACITY.
 //  * The first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept for the life of the
+//    process, so cudaDeviceReset between calls is not supported (the module
+//    may be loaded again at another address).
 //  * All calls share the one array: calls that overlap on the GPU (other
 //    streams, other host threads) race on it.  The scratch needs no clearing:
 //    the first iteration overwrites all of it.
@@ -32,7 +34,6 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
 size_t gvf_workspace_size(int X, int Y, int Z, int st);
 
 constexpr size_t kStaticScratchBytes = (size_t)96 << 20;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_gvf_static_scratch[kStaticScratchBytes];
 

@@ -46,6 +46,9 @@ inline int check_dims(int X, int Y, int Z) {
     return TSF_OK;
 }
 
+// Device ordinals the per-device caches of this library cover.
+constexpr int kMaxDevices = 64;
+
 inline bool valid_storage(int s) { return s >= TSF_STORE_F32 && s <= TSF_STORE_SNORM16; }
 
 // ---------------------------------------------------------------------------
