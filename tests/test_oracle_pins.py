@@ -1,11 +1,14 @@
 """CPU tests: pin the oracle.
 
 The reference publishes no golden vectors for GVF, TDF, eigen or the pyramid,
-and it cannot run here (OpenCL), so the oracle is pinned by what can be
-checked independently: published algorithms against numpy, the pyramid order
-against its closed form, the format conversions against numpy/IEEE, the
-sample-direction table against the literals in the reference's kernels, and
-method-level invariants.
+and its OpenCL runtime cannot run here.  The oracle is pinned two ways: to the
+reference's own kernel text -- golden vectors written by running kernels.cl
+under an OpenCL C shim on the CPU (tests/golden/, reproduced stage by stage
+below; tests/test_reference_pin.py compares the two directly where the
+reference source is present) -- and by what can be checked independently:
+published algorithms against numpy, the pyramid order against its closed
+form, the format conversions against numpy/IEEE, the sample-direction table
+against the literals in the reference's kernels, and method-level invariants.
 """
 import os
 import re
@@ -241,3 +244,43 @@ def test_link_chain_known_answer(oracle):
     assert (labels == 0).all() and sizes[0] == 12
     cl = oracle.rasterize_trees(v, edges, labels, sizes, 5, T.shape)
     assert cl[6, 6, 3:35].all() and cl.sum() == 32
+
+
+@pytest.mark.parametrize("storage", ["f32", "snorm16"])
+def test_oracle_reproduces_reference_golden(oracle, storage):
+    """The oracle against the golden vectors of the reference's own kernel
+    text (tests/golden/make_golden.py): every stage bit for bit."""
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_%s.npz" % storage))
+    P = dict(zip([str(k) for k in d["param_names"]], d["params"]))
+    unorm = storage == "snorm16"
+
+    def st(a):
+        return oracle.quantize(a, storage) if storage == "snorm16" else a
+
+    def raw(a):
+        return np.rint(a.astype(np.float64) * 32767.0).astype(np.int16) if storage == "snorm16" else a
+
+    vol = d["volume"]
+    b = oracle.blur(vol, P["sigma"])
+    assert np.array_equal(b, d["blurred"])
+    f4 = oracle.vector_field(b, P["fmax"], int(P["vsign"]), storage)
+    assert np.array_equal(raw(f4), d["field"])
+    fs = oracle.vector_field(vol, P["fmax"], int(P["vsign"]), storage)
+    assert np.array_equal(raw(fs), d["field_small"])
+    v = oracle.gvf(f4, P["mu"], int(P["iterations"]), storage)
+    assert np.array_equal(raw(v), d["gvf"])
+    fin = oracle.gvf_finish(v, storage)
+    assert np.array_equal(raw(fin), d["gvf_field"])
+    Ts, Rs = oracle.tdf_circle(fs, 1.0, 3.0, 0.5)
+    Tl, Rl = oracle.tdf_circle(fin, 2.5, 7.0, 0.5)
+    conv = oracle.to_unorm16 if unorm else (lambda a: a)
+    # combine compares the stored TDF values (unorm16 in the 16-bit mode)
+    take = conv(Tl) < conv(Ts)
+    T, R = np.where(take, Ts, Tl), np.where(take, Rs, Rl)
+    assert np.array_equal(conv(Ts), d["T_small"]) and np.array_equal(Rs, d["R_small"])
+    assert np.array_equal(conv(T), d["T"]) and np.array_equal(R, d["R"])
+    T_read = oracle.from_unorm16(d["T"]) if unorm else T
+    c = oracle.centerpoints(T_read, R, fin, P["tdf_high"], int(P["cube"]))
+    assert np.array_equal(c["candidates"], d["candidates"])
+    assert np.array_equal(c["mask2"], d["mask2"])
+    assert np.array_equal(c["vertices"], d["vertices"])
