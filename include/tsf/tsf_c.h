@@ -171,6 +171,42 @@ int tsf_gvf_device_error(int clear);
 int tsf_gvf_static(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                    int storage, void *stream);
 
+/* FP64 norms of the GVF residual (no counterpart in the reference, which
+ * runs a fixed number of iterations and never reduces its residual images;
+ * the per-voxel values are the reference's own).  Per component c, evaluated
+ * in FP32 at the mirrored position of every voxel, in the reference's
+ * operation order:
+ *   kind 0 -- the Jacobi update of GVF3DIteration (kernels.cl:1486-1490),
+ *             r_c = mu L(v_c) - (v_c - f0_c) |f0|^2, i.e. v_{k+1} - v_k before
+ *             rounding to the storage format;
+ *   kind 1 -- fmgResidual on the finest level (kernels.cl:2008-2053,
+ *             spacing 1): r_c = -|f0|^2 f0_c - (mu L(v_c) - |f0|^2 v_c).
+ * layout 0: d_f0 and d_v planar (tsf_gvf's buffers); 1: field4 (e.g.
+ * tsf_gvf_fmg's input and output).  Squares are summed in FP64 in a fixed
+ * order (the same bits on every run and device).  norms (host, 5 doubles):
+ * sqrt(sum r_x^2), sqrt(sum r_y^2), sqrt(sum r_z^2), sqrt of the total, max
+ * |r|.  Workspace: tsf_gvf_residual_workspace_size() bytes, 8-byte aligned.
+ * Synchronises `stream`. */
+size_t tsf_gvf_residual_workspace_size(void);
+int tsf_gvf_residual_norm(const void *d_f0, const void *d_v, int X, int Y, int Z, float mu, int storage,
+                          int kind, int layout, double *norms, void *d_workspace, size_t workspace_bytes,
+                          void *stream);
+
+/* Jacobi GVF (as tsf_gvf) that decides convergence on the residual: every
+ * check_every iterations (and before the first) the RMS of the next update,
+ * sqrt(sum_c |r_c|^2 / (3 N)) of tsf_gvf_residual_norm kind 0, is computed
+ * in FP64; the call stops at the first check where it is <= tolerance.
+ * *iterations_done and *residual_rms (host, may be NULL) receive the
+ * iterations run and the last RMS.  TSF_ERR_NOT_CONVERGED when
+ * max_iterations were run and the RMS is still above the tolerance (d_v then
+ * holds the last iterate).  Synchronises `stream` at every check.  No
+ * counterpart in the reference (fixed iteration count,
+ * gradientVectorFlow.cpp:1137-1151). */
+size_t tsf_gvf_converge_workspace_size(int X, int Y, int Z, int storage);
+int tsf_gvf_converge(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int max_iterations,
+                     int check_every, double tolerance, int storage, int *iterations_done,
+                     double *residual_rms, void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* Workspace bytes for tsf_gvf_adjoint. */
 size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iterations,
                                       int checkpoint_every);

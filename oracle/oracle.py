@@ -75,6 +75,7 @@ def _declare(L):
     L.orc_segment_spheres.restype = None
     L.orc_segment_spheres.argtypes = [_p, _p, _i, _i, _i, _p]
     L.orc_threshold_f32.argtypes = [_p, _i64, _f, _p]
+    L.orc_gvf_residual_norm.argtypes = [_p, _p, _i, _i, _i, _f, _i, _p]
     L.orc_set_threads.argtypes = [_i]
     L.orc_get_threads.restype = _i
     for s in ("_f32", "_f64"):
@@ -204,6 +205,19 @@ def gvf_planar(f: np.ndarray, v0: np.ndarray, mu: float, iterations: int,
     getattr(lib(), "orc_gvf" + s)(_ptr(f), _ptr(v), X, Y, Z, float(mu), int(iterations),
                                   STORAGE[storage])
     return v
+
+
+def gvf_residual_norm(f0: np.ndarray, v: np.ndarray, mu: float, kind: int = 0) -> np.ndarray:
+    """FP64 norms of the GVF residual at every voxel's mirrored position
+    (kind 0: GVF3DIteration's update, kernels.cl:1486-1490; kind 1:
+    fmgResidual, kernels.cl:2008-2053, spacing 1); f0, v planar [3,Z,Y,X]
+    stored values.  Returns [|r_x|, |r_y|, |r_z|, |r|, max |r|]."""
+    f = np.ascontiguousarray(f0, dtype=np.float32)
+    vv = np.ascontiguousarray(v, dtype=np.float32)
+    _, Z, Y, X = f.shape
+    out = np.zeros(5, np.float64)
+    lib().orc_gvf_residual_norm(_ptr(f), _ptr(vv), X, Y, Z, float(mu), int(kind), _ptr(out))
+    return out
 
 
 def gvf_finish(v: np.ndarray, storage: str = "f32", f64: bool = False) -> np.ndarray:

@@ -271,6 +271,54 @@ int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, in
     return sum;
 }
 
+static inline int orc_mirror(int w, int n) {
+    int p = w == 0 ? 2 : w;
+    return p >= n - 1 ? n - 3 : p;
+}
+
+void orc_gvf_residual_norm(const float *f0, const float *v, int X, int Y, int Z, float mu, int kind, double out[5]) {
+    const int64_t n = (int64_t)X * Y * Z, sx = 1, sy = X, sz = (int64_t)X * Y;
+    double acc[3] = {0.0, 0.0, 0.0};
+    float amax = 0.0f;
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < Y; y++)
+            for (int x = 0; x < X; x++) {
+                const int64_t p = orc_mirror(x, X) + (int64_t)X * (orc_mirror(y, Y) + (int64_t)Y * orc_mirror(z, Z));
+                const float fx = f0[p], fy = f0[n + p], fz = f0[2 * n + p];
+                const float sqr = (fx * fx + fy * fy) + fz * fz;
+                for (int c = 0; c < 3; c++) {
+                    const float *vc = v + c * n;
+                    const float fc = c == 0 ? fx : (c == 1 ? fy : fz);
+                    float r;
+                    if (kind == 0) {
+                        float lap = -6.0f * vc[p];
+                        lap = lap + vc[p + sx];
+                        lap = lap + vc[p - sx];
+                        lap = lap + vc[p + sy];
+                        lap = lap + vc[p - sy];
+                        lap = lap + vc[p + sz];
+                        lap = lap + vc[p - sz];
+                        r = mu * lap - (vc[p] - fc) * sqr;
+                    } else {
+                        float s6 = vc[p + sx] + vc[p - sx];
+                        s6 = s6 + vc[p + sy];
+                        s6 = s6 + vc[p - sy];
+                        s6 = s6 + vc[p + sz];
+                        s6 = s6 + vc[p - sz];
+                        const float residue = (mu * (s6 - 6.0f * vc[p])) / 1.0f;
+                        r = -sqr * fc - (residue - sqr * vc[p]);
+                    }
+                    acc[c] += (double)r * (double)r;
+                    if (fabsf(r) > amax) amax = fabsf(r);
+                }
+            }
+    out[0] = sqrt(acc[0]);
+    out[1] = sqrt(acc[1]);
+    out[2] = sqrt(acc[2]);
+    out[3] = sqrt((acc[0] + acc[1]) + acc[2]);
+    out[4] = amax;
+}
+
 void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask) {
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < n; i++) mask[i] = (T[i] < thr) ? 0 : 1;

@@ -99,6 +99,17 @@ int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, in
 ORC_DECLARE(float, _f32)
 ORC_DECLARE(double, _f64)
 
+/* GVF residual norms (no reference counterpart: the reference never reduces
+ * its residuals).  Per component c, at the mirrored position of every voxel,
+ * in float in the reference's operation order:
+ *   kind 0 (GVF3DIteration's update, kernels.cl:1486-1490):
+ *     r = mu * L(v_c) - (v_c - f0_c) |f0|^2
+ *   kind 1 (fmgResidual, kernels.cl:2008-2053, spacing 1):
+ *     r = -|f0|^2 f0_c - (mu * (sum of 6 neighbours - 6 v_c) - |f0|^2 v_c)
+ * f0 and v planar [3][Z][Y][X] (stored values).  out[0..2] = sqrt(sum r_c^2)
+ * (squares and sums in double), out[3] = sqrt of the total, out[4] = max |r|. */
+void orc_gvf_residual_norm(const float *f0, const float *v, int X, int Y, int Z, float mu, int kind, double out[5]);
+
 /* threshold (findCandidateCenterpoints, kernels.cl:1296-1307) */
 void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask);
 

@@ -284,3 +284,27 @@ def test_oracle_reproduces_reference_golden(oracle, storage):
     assert np.array_equal(c["candidates"], d["candidates"])
     assert np.array_equal(c["mask2"], d["mask2"])
     assert np.array_equal(c["vertices"], d["vertices"])
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_residual_norm_matches_numpy(oracle, synth, kind):
+    """The oracle's FP64 residual norms against a float64 numpy evaluation of
+    the same residual (mirror rule, spacing 1): agreement to float rounding."""
+    vol = oracle.blur(synth.vascular_tree((12, 14, 16), seed=3), 0.5)
+    f4 = oracle.vector_field(vol, 0.2, 1)
+    f0 = np.moveaxis(f4[..., :3], -1, 0).copy()
+    v = oracle.gvf(f4, 0.05, 5)
+    got = oracle.gvf_residual_norm(f0, v, 0.05, kind)
+    m = [np.array([2 if i == 0 else (n - 3 if i >= n - 1 else i) for i in range(n)]) for n in v.shape[1:]]
+    V, F = v.astype(np.float64), f0.astype(np.float64)
+    sqr = (F ** 2).sum(0)
+    r = np.zeros_like(V)
+    Vp = np.pad(V, ((0, 0), (1, 1), (1, 1), (1, 1)), mode="edge")
+    lap = (Vp[:, 1:-1, 1:-1, 2:] + Vp[:, 1:-1, 1:-1, :-2] + Vp[:, 1:-1, 2:, 1:-1] + Vp[:, 1:-1, :-2, 1:-1] +
+           Vp[:, 2:, 1:-1, 1:-1] + Vp[:, :-2, 1:-1, 1:-1] - 6 * V)
+    r = 0.05 * lap - (V - F) * sqr if kind == 0 else -sqr * F - (0.05 * lap - sqr * V)
+    r = r[:, m[0]][:, :, m[1]][:, :, :, m[2]]
+    want = [np.sqrt((r[c] ** 2).sum()) for c in range(3)]
+    assert np.allclose(got[:3], want, rtol=1e-5)
+    assert np.isclose(got[3], np.sqrt(sum(w ** 2 for w in want)), rtol=1e-5)
+    assert np.isclose(got[4], np.abs(r).max(), rtol=1e-5)

@@ -110,6 +110,10 @@ def _declare(L):
         "tsf_gvf_one_component_workspace_size": (_sz, [_i, _i, _i, _i]),
         "tsf_gvf_one_component": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
+        "tsf_gvf_residual_workspace_size": (_sz, []),
+        "tsf_gvf_residual_norm": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _p, _sz, _p]),
+        "tsf_gvf_converge_workspace_size": (_sz, [_i, _i, _i, _i]),
+        "tsf_gvf_converge": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, C.c_double, _i, _p, _p, _p, _sz, _p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name, None)
@@ -220,6 +224,39 @@ def gvf(f0, mu: float, iterations: int, storage: str = "f32", v=None, ws=None, m
     _check(L.tsf_gvf_mode(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
                           _ptr(ws), ws.numel(), int(mode), _stream(stream)))
     return v
+
+
+def gvf_residual_norm(f0, v, mu: float, storage: str = "f32", kind: int = 0, field4: bool = False, stream=None):
+    """FP64 residual norms (tsf_gvf_residual_norm): [|r_x|, |r_y|, |r_z|, |r|,
+    max |r|].  f0, v planar (3, Z, Y, X), or field4 (Z, Y, X, 4) when field4;
+    kind 0 = the Jacobi update, 1 = the multigrid residual."""
+    import numpy as np
+    layout = 1 if field4 else 0
+    Z, Y, X = (v.shape[:3] if layout else v.shape[1:])
+    L = load()
+    ws = workspace(L.tsf_gvf_residual_workspace_size())
+    out = np.zeros(5, np.float64)
+    _check(L.tsf_gvf_residual_norm(_ptr(f0), _ptr(v), X, Y, Z, float(mu), STORAGE[storage], int(kind), layout,
+                                   out.ctypes.data_as(C.c_void_p), _ptr(ws), ws.numel(), _stream(stream)))
+    return out
+
+
+def gvf_converge(f0, mu: float, max_iterations: int, check_every: int, tolerance: float, storage: str = "f32",
+                 v=None, stream=None, raise_not_converged=True):
+    """tsf_gvf_converge: Jacobi iterations until the RMS of the next update is
+    <= tolerance (checked every check_every iterations).  Returns (v,
+    iterations run, last RMS, status)."""
+    _, Z, Y, X = f0.shape
+    L = load()
+    v = f0.clone() if v is None else v
+    ws = workspace(L.tsf_gvf_converge_workspace_size(X, Y, Z, STORAGE[storage]))
+    it, rms = C.c_int(0), C.c_double(0.0)
+    code = L.tsf_gvf_converge(_ptr(f0), _ptr(v), X, Y, Z, float(mu), int(max_iterations), int(check_every),
+                              float(tolerance), STORAGE[storage], C.byref(it), C.byref(rms), _ptr(ws), ws.numel(),
+                              _stream(stream))
+    if code != TSF_OK and (raise_not_converged or code != 5):
+        _check(code)
+    return v, it.value, rms.value, code
 
 
 def gvf_adjoint_interval(f0, iterations: int, storage: str = "f32", budget_bytes: int = None) -> int:
