@@ -292,6 +292,31 @@ int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, fl
                       float rstep, void *d_T, int tdf_unorm16, float *d_R, void *d_workspace,
                       size_t workspace_bytes, void *stream);
 
+/* Options of tsf_tdf_circle_ex.  No counterpart in the reference, whose
+ * circleFittingTDF has the sample count and the eigensolver built in. */
+typedef struct {
+    int samples;   /* circle samples per radius: 32 (the reference, kernels.cl:1122)
+                      or another multiple of 4 in [4, 32]                         */
+    int stride;    /* sample j takes entry j * stride of the reference's 32-entry
+                      cos / sin table (angle j * stride radians), as its disabled
+                      sample-count switch does (kernels.cl:1120-1131);
+                      (samples - 1) * stride < 32; 1 for the reference           */
+    int eigen;     /* 0: tred2 + tql2, the reference's (kernels.cl:1519-1773),
+                      bit-exact with it; 1: a closed-form solver in registers (the
+                      trigonometric method with Newton steps for the isolated
+                      root, robust eigenvectors, an FP64 branch when two
+                      eigenvalues nearly coincide); eigenvector signs are
+                      canonical (largest component positive), so T and R agree
+                      with mode 0 to the circle's sampling noise, not bit for bit */
+    int kernel;    /* 0: load-balanced sweeps (default), 1: one voxel per lane    */
+} tsf_tdf_options;
+
+/* tsf_tdf_circle_ws with options (NULL: the reference's 32 samples, tql2,
+ * default kernel -- then identical to tsf_tdf_circle_ws). */
+int tsf_tdf_circle_ex(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
+                      float rstep, const tsf_tdf_options *options, void *d_T, int tdf_unorm16, float *d_R,
+                      void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* splineTDF (kernels.cl:1159-1254, kernels_no_3d_write.cl:1574-1671; driver
  * runSplineTDF, tubeDetectionFilters.cpp:4-55, called with
  * max(1.5, radius-min) at tube-segmentation.cpp:785-786): the normalised

@@ -35,7 +35,7 @@ def build(force: bool = False) -> str:
 def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
     return any(os.path.getmtime(os.path.join(HERE, f)) > t
-               for f in ("tsf_oracle.c", "tsf_oracle_impl.h", "tsf_oracle.h"))
+               for f in ("tsf_oracle.c", "tsf_oracle_impl.h", "tsf_oracle.h", "tsf_oracle_eigc.h"))
 
 
 def lib():
@@ -75,6 +75,7 @@ def _declare(L):
     L.orc_segment_spheres.restype = None
     L.orc_segment_spheres.argtypes = [_p, _p, _i, _i, _i, _p]
     L.orc_threshold_f32.argtypes = [_p, _i64, _f, _p]
+    L.orc_eig3_closed_f32.argtypes = [_p, _p, _p]
     L.orc_gvf_residual_norm.argtypes = [_p, _p, _i, _i, _i, _f, _i, _p]
     L.orc_set_threads.argtypes = [_i]
     L.orc_get_threads.restype = _i
@@ -87,6 +88,7 @@ def _declare(L):
         getattr(L, "orc_gvf_one_component" + s).argtypes = [_p, _i, _i, _i, _f, _i, _i, _p]
         getattr(L, "orc_eig3" + s).argtypes = [_p, _p, _p]
         getattr(L, "orc_tdf_circle" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
+        getattr(L, "orc_tdf_circle_ex" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _i, _i, _i, _p, _p]
         getattr(L, "orc_tdf_spline" + s).argtypes = [_p, _i, _i, _i, _f, _f, _f, _p, _p]
         getattr(L, "orc_combine" + s).argtypes = [_p, _p, _p, _p, _i64]
         getattr(L, "orc_candidates2" + s).argtypes = [_p, _p, _i, _i, _i, _p, _i64, _p]
@@ -255,16 +257,28 @@ def eig3(A: np.ndarray, f64: bool = False):
 
 
 def tdf_circle(field4: np.ndarray, rmin: float, rmax: float, rstep: float,
-               f64: bool = False):
-    """circleFittingTDF, kernels.cl:1071-1157 -> (T, R) float volumes."""
+               f64: bool = False, samples: int = 32, stride: int = 1, eigen: int = 0):
+    """circleFittingTDF, kernels.cl:1071-1157 -> (T, R) float volumes.
+    samples / stride: samples per radius taking table entries j * stride
+    (32 / 1 in the reference); eigen 1: the closed-form eigensolver (float
+    only)."""
     dt, s = _real(f64)
     field4 = np.ascontiguousarray(field4, dtype=dt)
     Z, Y, X = field4.shape[:3]
     T = np.empty((Z, Y, X), dt)
     R = np.empty((Z, Y, X), dt)
-    getattr(lib(), "orc_tdf_circle" + s)(_ptr(field4), X, Y, Z, float(rmin), float(rmax),
-                                         float(rstep), _ptr(T), _ptr(R))
+    getattr(lib(), "orc_tdf_circle_ex" + s)(_ptr(field4), X, Y, Z, float(rmin), float(rmax),
+                                            float(rstep), int(samples), int(stride), int(eigen), _ptr(T), _ptr(R))
     return T, R
+
+
+def eig3_closed(A: np.ndarray):
+    """The closed-form eigensolver of the TDF's eigen mode 1 -> (d, V)."""
+    A = np.ascontiguousarray(A, dtype=np.float32).reshape(3, 3)
+    V = np.empty((3, 3), np.float32)
+    d = np.empty(3, np.float32)
+    lib().orc_eig3_closed_f32(_ptr(A), _ptr(V), _ptr(d))
+    return d, V
 
 
 def tdf_spline(field4: np.ndarray, rmin: float, rmax: float, rstep: float, f64: bool = False):

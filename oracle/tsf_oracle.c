@@ -23,6 +23,64 @@
 #include <omp.h>
 #endif
 
+/* closed-form eigensolver cores (tsf_oracle_eigc.h), float and double */
+#define EIGC_R float
+#define EIGC_SFX _f
+#define EIGC_SQRT sqrtf
+#include "tsf_oracle_eigc.h"
+#undef EIGC_R
+#undef EIGC_SFX
+#undef EIGC_SQRT
+#define EIGC_R double
+#define EIGC_SFX _d
+#define EIGC_SQRT sqrt
+#include "tsf_oracle_eigc.h"
+#undef EIGC_R
+#undef EIGC_SFX
+#undef EIGC_SQRT
+
+/* Closed-form eigen-decomposition as the TDF's eigen mode 1 uses it: the
+ * float core with 5 Newton steps, redone in double with 7 when
+ * 1 - |r| < 1e-3 (two eigenvalues nearly equal); then ascending |lambda| by
+ * the reference's selection sort (strict <, kernels.cl:1742-1761) and each
+ * eigenvector's largest-magnitude component made positive.  A row-major,
+ * Vout[3 * i + k] = component i of eigenvector k. */
+void orc_eig3_closed_f32(const float A[9], float Vout[9], float d[3]) {
+    const float a[6] = {A[0], A[4], A[8], A[3], A[6], A[7]};
+    float lam[3], vec[3][3], r = 0.0f;
+    if (eigc_core_f(a, lam, vec, &r, 5) && 1.0f - (r < 0.0f ? -r : r) < 1e-3f) {
+        const double ad[6] = {a[0], a[1], a[2], a[3], a[4], a[5]};
+        double ld[3], vd[3][3], rd;
+        eigc_core_d(ad, ld, vd, &rd, 7);
+        for (int k = 0; k < 3; k++) {
+            lam[k] = (float)ld[k];
+            for (int i = 0; i < 3; i++) vec[k][i] = (float)vd[k][i];
+        }
+    }
+    int idx[3] = {0, 1, 2};
+    float dv[3] = {lam[0], lam[1], lam[2]};
+    for (int i = 0; i < 2; i++) {
+        int k = i;
+        float p = dv[i];
+        for (int j = i + 1; j < 3; j++)
+            if (fabsf(dv[j]) < fabsf(p)) { k = j; p = dv[j]; }
+        if (k != i) {
+            dv[k] = dv[i];
+            dv[i] = p;
+            const int t = idx[k]; idx[k] = idx[i]; idx[i] = t;
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        const float *e = vec[idx[k]];
+        float big = e[0];
+        if (fabsf(e[1]) > fabsf(big)) big = e[1];
+        if (fabsf(e[2]) > fabsf(big)) big = e[2];
+        const float s = big < 0.0f ? -1.0f : 1.0f;
+        for (int i = 0; i < 3; i++) Vout[3 * i + k] = s * e[i];
+        d[k] = dv[k];
+    }
+}
+
 static int g_threads = 0;
 
 void orc_set_threads(int n) {

@@ -86,6 +86,9 @@ int64_t orc_hp_compact(const int8_t *mask, int X, int Y, int Z, int32_t *pos, in
     void orc_eig3##S(const R A[9], R V[9], R d[3]);                                     \
     void orc_tdf_circle##S(const R *field4, int X, int Y, int Z, float rMin, float rMax,  \
                            float rStep, R *T, R *radius);                               \
+    void orc_tdf_circle_ex##S(const R *field4, int X, int Y, int Z, float rMin, float rMax, \
+                              float rStep, int samples, int stride, int eigen, R *T,     \
+                              R *radius);                                               \
     void orc_tdf_spline##S(const R *field4, int X, int Y, int Z, float rMin, float rMax,  \
                            float rStep, R *T, R *radius);                               \
     void orc_combine##S(const R *Ts, const R *Rs, R *Tl, R *Rl, int64_t n);             \
@@ -109,6 +112,11 @@ ORC_DECLARE(double, _f64)
  * f0 and v planar [3][Z][Y][X] (stored values).  out[0..2] = sqrt(sum r_c^2)
  * (squares and sums in double), out[3] = sqrt of the total, out[4] = max |r|. */
 void orc_gvf_residual_norm(const float *f0, const float *v, int X, int Y, int Z, float mu, int kind, double out[5]);
+
+/* The closed-form eigensolver of the TDF's eigen mode 1 (tsf_oracle_eigc.h,
+ * no reference counterpart): A row-major symmetric, V columns = eigenvectors
+ * (largest component positive), d ascending by |lambda|. */
+void orc_eig3_closed_f32(const float A[9], float V[9], float d[3]);
 
 /* threshold (findCandidateCenterpoints, kernels.cl:1296-1307) */
 void orc_threshold_f32(const float *T, int64_t n, float thr, int8_t *mask);

@@ -460,8 +460,24 @@ static void FN(orc_sample_linear)(const REAL *F, int X, int Y, int Z, REAL u, RE
  * The Hessian is normalised by w when rMax >= 4 (kernels.cl:1083-1091). */
 void FN(orc_tdf_circle)(const REAL *F, int X, int Y, int Z, float rMin, float rMax,
                         float rStep, REAL *T, REAL *Rout) {
-    float cf[32], sf[32];
-    orc_circle_table(cf, sf);
+    FN(orc_tdf_circle_ex)(F, X, Y, Z, rMin, rMax, rStep, 32, 1, 0, T, Rout);
+}
+
+/* circleFittingTDF with the library's options: `samples` samples per radius
+ * taking entries j * stride of the 32-entry table (the reference's disabled
+ * sample-count switch, kernels.cl:1120-1131; 32 / 1 is the reference) and
+ * the eigensolver `eigen` (0: tred2 + tql2; 1: the closed form,
+ * orc_eig3_closed_f32 -- float instantiation only, the double one keeps
+ * tql2). */
+void FN(orc_tdf_circle_ex)(const REAL *F, int X, int Y, int Z, float rMin, float rMax,
+                           float rStep, int samples, int stride, int eigen, REAL *T, REAL *Rout) {
+    float cf32[32], sf32[32], cf[32], sf[32];
+    orc_circle_table(cf32, sf32);
+    for (int j = 0; j < samples; j++) {
+        cf[j] = cf32[j * stride];
+        sf[j] = sf32[j * stride];
+    }
+    (void)eigen;
     const int normalized = !(rMax < 4.0f);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int z = 0; z < Z; z++)
@@ -471,13 +487,18 @@ void FN(orc_tdf_circle)(const REAL *F, int X, int Y, int Z, float rMin, float rM
                 FN(orc_hessian)(F, X, Y, Z, x, y, z, normalized, H);
                 for (int i = 0; i < 3; i++)
                     for (int j = 0; j < 3; j++) A[3 * i + j] = H[i][j];
+#if ORC_IS_F32
+                if (eigen) orc_eig3_closed_f32(A, V, d);
+                else FN(orc_eig3)(A, V, d);
+#else
                 FN(orc_eig3)(A, V, d);
+#endif
                 REAL e2[3] = {V[0 * 3 + 1], V[1 * 3 + 1], V[2 * 3 + 1]};
                 REAL e3[3] = {V[0 * 3 + 2], V[1 * 3 + 2], V[2 * 3 + 2]};
                 REAL maxSum = 0, maxRadius = 0;
                 for (REAL radius = (REAL)rMin; radius <= (REAL)rMax; radius = radius + (REAL)rStep) {
                     REAL rs = 0;
-                    for (int j = 0; j < 32; j++) {
+                    for (int j = 0; j < samples; j++) {
                         REAL c = (REAL)cf[j], s = (REAL)sf[j];
                         REAL va0 = c * e3[0] + s * e2[0];
                         REAL va1 = c * e3[1] + s * e2[1];
@@ -488,7 +509,7 @@ void FN(orc_tdf_circle)(const REAL *F, int X, int Y, int Z, float rMin, float rM
                         REAL dt = ((-smp[0]) * va0 + (-smp[1]) * va1) + (-smp[2]) * va2;
                         rs = rs + dt;
                     }
-                    rs = rs / (REAL)32;
+                    rs = rs / (REAL)samples;
                     if (rs > maxSum) {
                         maxSum = rs;
                         maxRadius = radius;

@@ -39,7 +39,7 @@ int run_gvf_one_component(const void *d_field4_in, int X, int Y, int Z, float mu
                           void *d_field4_out, void *ws, size_t ws_bytes, cudaStream_t s);
 int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
                       void *d_T, int unorm, float *d_R, cudaStream_t s, int tdf_mode, void *ws = nullptr,
-                      size_t ws_bytes = 0);
+                      size_t ws_bytes = 0, int samples = 32, int stride = 1, int eigen = 0);
 size_t tdf_workspace_size(int X, int Y, int Z, int st);
 int launch_tdf_combine(const void *Ts, const float *Rs, void *Tl, float *Rl, int64_t n, int unorm, cudaStream_t s);
 size_t candidates_workspace_size(int X, int Y, int Z);
@@ -129,6 +129,16 @@ int tsf_tdf_circle_ws(const void *d_field4, int X, int Y, int Z, int storage, fl
                       void *stream) {
     return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream), 0,
                              d_workspace, workspace_bytes);
+}
+
+int tsf_tdf_circle_ex(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax, float rstep,
+                      const tsf_tdf_options *options, void *d_T, int tdf_unorm16, float *d_R, void *d_workspace,
+                      size_t workspace_bytes, void *stream) {
+    const tsf_tdf_options def = {32, 1, 0, 0};
+    const tsf_tdf_options &o = options ? *options : def;
+    if (o.kernel != 0 && o.kernel != 1) return fail(TSF_ERR_INVALID_ARG, "kernel must be 0 or 1");
+    return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream),
+                             o.kernel, d_workspace, workspace_bytes, o.samples, o.stride, o.eigen);
 }
 
 // tsf_tdf_circle with the kernel forced (0 = default, 1 = one voxel per lane).

@@ -16,19 +16,24 @@ namespace tsf {
 struct CircleTable {
     float c[32];
     float s[32];
+    int n;      // samples per radius
 };
 
 // cos(j), sin(j), j = 0..31 radians, rounded to 6 significant digits: the
-// sample directions of the reference (kernels.cl:1068-1069).
-inline CircleTable host_circle_table() {
+// sample directions of the reference (kernels.cl:1068-1069).  With fewer
+// samples, entry j holds table entry j * stride (the reference's disabled
+// sample-count switch, kernels.cl:1120-1131, takes its samples that way).
+inline CircleTable host_circle_table(int samples = 32, int stride = 1) {
     CircleTable t;
     char buf[64];
     for (int j = 0; j < 32; j++) {
-        snprintf(buf, sizeof buf, "%.6g", cos((double)j));
+        const int q = j < samples ? j * stride : 0;
+        snprintf(buf, sizeof buf, "%.6g", cos((double)q));
         t.c[j] = strtof(buf, nullptr);
-        snprintf(buf, sizeof buf, "%.6g", sin((double)j));
+        snprintf(buf, sizeof buf, "%.6g", sin((double)q));
         t.s[j] = strtof(buf, nullptr);
     }
+    t.n = samples;
     return t;
 }
 

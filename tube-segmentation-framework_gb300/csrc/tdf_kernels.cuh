@@ -1,0 +1,248 @@
+// tdf_kernels.cuh -- the circle-fitting tube detection filter fused with the
+// Hessian and its eigen-decomposition (reference circleFittingTDF,
+// kernels.cl:1065-1157; driver runCircleFittingTDF,
+// tubeDetectionFilters.cpp:57-73): the kernel templates and their launcher,
+// instantiated for the reference's tred2 + tql2 (eigen mode 0, tdf.cu) and for
+// the closed-form eigensolver (eigen mode 1, tdf_closed.cu) in separate
+// translation units so the two compile in parallel.
+//
+// One thread per voxel (tdf_circle_kernel) or load-balanced sweeps over
+// bricks (tdf_queue_kernel).  The thread reads the six face neighbours of the
+// field4 image (one 16 B or 8 B vector load each), builds the Hessian,
+// decomposes it in registers, then sweeps the radii: per radius tab.n points
+// on the circle spanned by e2 and e3 (32 in the reference, kernels.cl:1122;
+// the table holds entries j * stride of the reference's cos / sin table), each
+// a trilinear read of the x,y,z channels with OpenCL's
+// unnormalised-coordinate convention (i0 = floor(u - 0.5), clamp to edge).
+// The sweep stops at the first radius that does not raise the mean response.
+// Algorithmic HBM traffic is the field read once (4s B/voxel) plus T and R
+// written (8 B or 6 B/voxel); the trilinear gathers are served by L1/L2.
+#pragma once
+
+#include "eigen_closed.cuh"
+#include "tdf_common.cuh"
+
+namespace tsf {
+
+// Eigenvectors e2, e3 (columns 1, 2) of the Hessian H: the reference's
+// tred2 + tql2 (EIG 0) or the closed form (EIG 1).
+template <int EIG> __device__ __forceinline__ void tdf_eigen(const float H[3][3], float V[3][3]) {
+    float d[3];
+    if constexpr (EIG == 0) eig3<float>(H, V, d);
+    else eig3_closed(H, V, d);
+}
+
+// Upper bound on the number of radii one voxel evaluates (a radius step of 0
+// would otherwise repeat the same radius until the response stops growing).
+constexpr int kMaxRadii = 4096;
+
+template <int ST, bool NORM, bool UNORM, int EIG>
+__global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict__ F, int X, int Y, int Z, float rmin,
+                                                         float rmax, float rstep, const CircleTable tab, void *T,
+                                                         float *__restrict__ Rout) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= X || y >= Y || z >= Z) return;
+    float H[3][3], V[3][3];
+    hessian<ST, NORM>(F, X, Y, Z, x, y, z, H);
+    tdf_eigen<EIG>(H, V);
+    const float e2x = V[0][1], e2y = V[1][1], e2z = V[2][1];
+    const float e3x = V[0][2], e3y = V[1][2], e3z = V[2][2];
+    const float fx = (float)x, fy = (float)y, fz = (float)z;
+    float maxSum = 0.0f, maxRadius = 0.0f;
+    int nr = 0;
+    for (float radius = rmin; radius <= rmax && nr < kMaxRadii; radius = radius + rstep, nr++) {
+        float rs = 0.0f;
+#pragma unroll 4
+        for (int j = 0; j < tab.n; j++) {
+            const float c = tab.c[j], s = tab.s[j];
+            const float va0 = c * e3x + s * e2x;
+            const float va1 = c * e3y + s * e2y;
+            const float va2 = c * e3z + s * e2z;
+            const float3 smp = sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
+            const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+            rs = rs + dt;
+        }
+        rs = rs / (float)tab.n;
+        if (rs > maxSum) {
+            maxSum = rs;
+            maxRadius = radius;
+        } else {
+            break;
+        }
+    }
+    const int64_t i = lin(x, y, z, X, Y);
+    if (UNORM) {
+        reinterpret_cast<uint16_t *>(T)[i] = to_unorm16(maxSum);
+    } else {
+        reinterpret_cast<float *>(T)[i] = maxSum;
+    }
+    Rout[i] = maxRadius;
+}
+
+// Same filter with the radius sweeps load-balanced inside each warp.
+//
+// With one voxel per lane, a warp runs as many radii as its slowest voxel
+// needs (about half the voxels stop at the first radius, others go on to 3-6),
+// which left ~60 % of the lanes idle.  Here a warp owns kSeg = 128 voxels: it
+// first decomposes all their Hessians (one voxel per lane, 4 rounds) into
+// shared memory, then treats each voxel's sweep as a task: a lane evaluates
+// one radius (its 32 samples, in order) per round and, when its voxel's sweep
+// ends, takes the next unstarted voxel, in lane order.  Lanes stay busy until
+// the queue drains, and each voxel's arithmetic is exactly that of
+// tdf_circle_kernel.
+//
+// Locality: a warp's voxels form an 8 x 4 x 4 block and a CTA's four warps an
+// 8 x 8 x 8 brick, so the circles sampled by a CTA stay within a
+// (8 + 2 rmax)^3 neighbourhood that L1 can hold (row segments of 128 voxels
+// touched ~5x more distinct lines and missed L1 for about a quarter of the
+// trilinear corners).
+constexpr int kSeg = 128;
+constexpr int kTdfWarps = 4;
+
+// PAIR: interior samples read the x-paired copy P of a 16-bit field (one
+// 16-byte load per corner row, sample_linear_pair_in) instead of F.
+template <int ST, bool NORM, bool UNORM, bool PAIR, int EIG>
+__global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
+                                                                    float rmin, float rmax, float rstep,
+                                                                    const CircleTable tab, void *T,
+                                                                    float *__restrict__ Rout, int fast_ok,
+                                                                    const uint4 *__restrict__ P) {
+    static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
+    __shared__ float se[kTdfWarps][6][kSeg];
+    __shared__ unsigned char sin_[kTdfWarps][kSeg];      // samples stay inside: unclamped sampler
+    const int XY = X * Y, margin = sample_margin(rmax);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // brick of this CTA, block of this warp: task t -> (t & 7, (t >> 3) & 3, t >> 5)
+    const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
+    const int b = blockIdx.x;
+    const int bx0 = (b % nbx) * 8, by0 = ((b / nbx) % nby) * 8 + (w & 1) * 4;
+    const int bz0 = (b / (nbx * nby)) * 8 + (w >> 1) * 4;
+    const int ntask = kSeg;
+    auto tx = [&](int t) { return bx0 + (t & 7); };
+    auto ty = [&](int t) { return by0 + ((t >> 3) & 3); };
+    auto tz = [&](int t) { return bz0 + (t >> 5); };
+    auto inside = [&](int t) { return tx(t) < X && ty(t) < Y && tz(t) < Z; };
+    // phase 1: eigenvectors of the block's voxels
+    for (int t = lane; t < ntask; t += 32) {
+        if (!inside(t)) continue;
+        float H[3][3], V[3][3];
+        hessian<ST, NORM>(F, X, Y, Z, tx(t), ty(t), tz(t), H);
+        tdf_eigen<EIG>(H, V);
+        se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
+        se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
+        const float e2[3] = {V[0][1], V[1][1], V[2][1]}, e3[3] = {V[0][2], V[1][2], V[2][2]};
+        sin_[w][t] = fast_ok && samples_inside(tx(t), ty(t), tz(t), X, Y, Z, margin, e2, e3);
+    }
+    __syncwarp();
+    // phase 2: radius sweeps as tasks
+    const unsigned full = 0xffffffffu;
+    int task = lane < ntask ? lane : -1;
+    int next = 32;                                   // next unstarted task (same in every lane)
+    float radius = rmin, maxSum = 0.0f, maxRadius = 0.0f;
+    int nr = 0;
+    while (__any_sync(full, task >= 0)) {
+        bool done = true;
+        if (task >= 0 && inside(task)) {
+            const float e2x = se[w][0][task], e2y = se[w][1][task], e2z = se[w][2][task];
+            const float e3x = se[w][3][task], e3y = se[w][4][task], e3z = se[w][5][task];
+            const float fx = (float)tx(task), fy = (float)ty(task), fz = (float)tz(task);
+            if (radius <= rmax && nr < kMaxRadii) {
+                float rs = 0.0f;
+                if (sin_[w][task]) {
+#pragma unroll 4
+                    for (int j = 0; j < tab.n; j++) {
+                        const float c = tab.c[j], s = tab.s[j];
+                        const float va0 = c * e3x + s * e2x;
+                        const float va1 = c * e3y + s * e2y;
+                        const float va2 = c * e3z + s * e2z;
+                        float3 smp;
+                        if constexpr (PAIR)
+                            smp = sample_linear_pair_in<ST>(P, X, XY, fx + radius * va0, fy + radius * va1,
+                                                            fz + radius * va2);
+                        else
+                            smp = sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1,
+                                                       fz + radius * va2);
+                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                        rs = rs + dt;
+                    }
+                } else {
+#pragma unroll 4
+                    for (int j = 0; j < tab.n; j++) {
+                        const float c = tab.c[j], s = tab.s[j];
+                        const float va0 = c * e3x + s * e2x;
+                        const float va1 = c * e3y + s * e2y;
+                        const float va2 = c * e3z + s * e2z;
+                        const float3 smp =
+                            sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
+                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                        rs = rs + dt;
+                    }
+                }
+                rs = rs / (float)tab.n;
+                if (rs > maxSum) {
+                    maxSum = rs;
+                    maxRadius = radius;
+                    radius = radius + rstep;
+                    nr++;
+                    done = false;
+                }
+            }
+            if (done) {
+                const int64_t i = lin(tx(task), ty(task), tz(task), X, Y);
+                if (UNORM) reinterpret_cast<uint16_t *>(T)[i] = to_unorm16(maxSum);
+                else reinterpret_cast<float *>(T)[i] = maxSum;
+                Rout[i] = maxRadius;
+            }
+        }
+        // lanes whose sweep ended take the next tasks, in lane order
+        const unsigned want = __ballot_sync(full, task >= 0 && done) | __ballot_sync(full, task < 0 && next < ntask);
+        if ((want >> lane) & 1u) {
+            const int k = next + __popc(want & ((1u << lane) - 1u));
+            task = k < ntask ? k : -1;
+            radius = rmin;
+            maxSum = 0.0f;
+            maxRadius = 0.0f;
+            nr = 0;
+        }
+        next += __popc(want);
+    }
+}
+
+
+// Launches the sweep kernel of eigen mode EIG.  queue: load-balanced sweeps
+// (tdf_queue_kernel) else one voxel per lane; P: the x-paired 16-bit copy of
+// the field (queue only) or null.
+template <int EIG>
+int launch_tdf_kernels(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
+                       const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, bool queue,
+                       const uint4 *P, int fast_ok) {
+    const dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
+    const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
+    const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
+#define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
+    do {                                                                                                             \
+        if (queue && P)                                                                                              \
+            tdf_queue_kernel<ST, NORM, UN, ST != TSF_STORE_F32, EIG><<<qblocks, 32 * kTdfWarps, 0, s>>>(            \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, P);                                    \
+        else if (queue)                                                                                              \
+            tdf_queue_kernel<ST, NORM, UN, false, EIG><<<qblocks, 32 * kTdfWarps, 0, s>>>(                          \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, nullptr);                              \
+        else                                                                                                         \
+            tdf_circle_kernel<ST, NORM, UN, EIG><<<g, b, 0, s>>>(d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T,     \
+                                                                 d_R);                                               \
+    } while (0)
+    TSF_DISPATCH_STORAGE(st, ST, {
+        if (norm) {
+            if (unorm) TSF_TDF_LAUNCH(ST, true, true); else TSF_TDF_LAUNCH(ST, true, false);
+        } else {
+            if (unorm) TSF_TDF_LAUNCH(ST, false, true); else TSF_TDF_LAUNCH(ST, false, false);
+        }
+    });
+#undef TSF_TDF_LAUNCH
+    TSF_CHECK_LAUNCH("tdf_circle_kernel");
+    return TSF_OK;
+}
+
+}  // namespace tsf

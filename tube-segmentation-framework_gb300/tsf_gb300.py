@@ -110,6 +110,7 @@ def _declare(L):
         "tsf_gvf_one_component_workspace_size": (_sz, [_i, _i, _i, _i]),
         "tsf_gvf_one_component": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
+        "tsf_tdf_circle_ex": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _i, _p, _p, _sz, _p]),
         "tsf_gvf_residual_workspace_size": (_sz, []),
         "tsf_gvf_residual_norm": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_converge_workspace_size": (_sz, [_i, _i, _i, _i]),
@@ -346,15 +347,29 @@ def gvf_finish(v, storage: str = "f32", out=None, stream=None):
     return out
 
 
+class TdfOptions(C.Structure):
+    """tsf_tdf_options (include/tsf/tsf_c.h)."""
+    _fields_ = [("samples", C.c_int), ("stride", C.c_int), ("eigen", C.c_int), ("kernel", C.c_int)]
+
+
 def tdf_circle(field4, rmin, rmax, rstep, storage: str = "f32", unorm16: bool = False, mode: int = 0,
-               stream=None, ws=None):
+               stream=None, ws=None, samples: int = None, stride: int = 1, eigen: int = None):
     """Circle-fitting TDF.  ws: a workspace of tsf_tdf_workspace_size bytes
     (tsf_tdf_circle_ws: paired texels for 16-bit storage); mode forces the
-    kernel (tsf_tdf_circle_mode) when ws is None."""
+    kernel (tsf_tdf_circle_mode) when ws is None.  samples / stride / eigen
+    given: tsf_tdf_circle_ex with those options (mode as its kernel)."""
     torch = _torch()
     Z, Y, X = field4.shape[:3]
     T = torch.empty((Z, Y, X), dtype=torch.int16 if unorm16 else torch.float32, device=field4.device)
     R = torch.empty((Z, Y, X), dtype=torch.float32, device=field4.device)
+    if samples is not None or eigen is not None:
+        opt = TdfOptions(32 if samples is None else int(samples), int(stride), 0 if eigen is None else int(eigen),
+                         int(mode))
+        _check(load().tsf_tdf_circle_ex(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
+                                        float(rstep), C.byref(opt), _ptr(T), int(unorm16), _ptr(R),
+                                        _ptr(ws) if ws is not None else None, ws.numel() if ws is not None else 0,
+                                        _stream(stream)))
+        return T, R
     if ws is not None:
         _check(load().tsf_tdf_circle_ws(_ptr(field4), X, Y, Z, STORAGE[storage], float(rmin), float(rmax),
                                         float(rstep), _ptr(T), int(unorm16), _ptr(R), _ptr(ws), ws.numel(),
