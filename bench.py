@@ -723,6 +723,14 @@ def run_stage(args):
         runs["circle"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
         runs["circle_paired"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st,
                                                      ws=ws)
+        runs["circle_paired_closed_eigen"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"],
+                                                                  storage=st, ws=ws, eigen=1)
+        runs["circle_paired_12_samples"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"],
+                                                                storage=st, ws=ws, samples=12)
+        _, fsm = T.vector_field(vol, P["fmax"], P["vsign"], storage=st, planar=False, field4=True)
+        runs["small_paired"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws)
+        runs["small_paired_closed_eigen"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
+                                                                 eigen=1)
     for run in runs.values():
         run()
     torch.cuda.synchronize()
