@@ -155,6 +155,20 @@ int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int
  * in the reference (OpenCL reports no such condition). */
 int tsf_gvf_device_error(int clear);
 
+/* Self-test of the streaming GVF kernel's bounded waits (no counterpart in
+ * the reference).  Launches the kernel once, on the caller's buffers as for
+ * tsf_gvf (d_f0 read; d_v and the workspace of tsf_gvf_workspace_size bytes
+ * receive invalid values), with every shared-memory copy suppressed and each
+ * barrier wait limited to wait_cycles SM clock cycles (> 0; 2,000,000 is about
+ * 1 ms): every wait runs out, the kernel records the timeout in its device
+ * error word and returns, and the GPU stays usable.  Returns that error word
+ * (as tsf_gvf_device_error(1) would: bit 0 set is the expected result), or
+ * minus a TSF_ERR_* code when the kernel cannot run on these buffers (rows
+ * not a multiple of 16 bytes, unaligned) or the launch fails.  Synchronises
+ * `stream`. */
+int tsf_gvf_wait_selftest(const void *d_f0, void *d_v, int X, int Y, int Z, int storage,
+                          long long wait_cycles, void *d_workspace, size_t workspace_bytes, void *stream);
+
 /* tsf_gvf for callers that cannot allocate device memory.  No counterpart in
  * the reference: it exists for hosts that can neither call cudaMalloc nor
  * provide a workspace (plug-in hosts that own the device allocator,

@@ -88,7 +88,8 @@ template <int ST, bool WS, bool REV>
 __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_CTAS) gvf_zs_kernel(const __grid_constant__ CUtensorMap tv,
                                                                    const __grid_constant__ CUtensorMap tf,
                                                                    typename Store<ST>::T *__restrict__ dst, int X,
-                                                                   int Y, int Z, float mu, int ntx, int K) {
+                                                                   int Y, int Z, float mu, int ntx, int K,
+                                                                   long long wait_limit, int no_copies) {
     constexpr bool rev = REV;   // stream downwards (compile-time: no selects in the sums)
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
@@ -137,10 +138,10 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
         // writes are visible; every other global access of this CTA follows the
         // barrier below
         pdl_wait();
-        for (; issued_v < RV && issued_v < nv; issued_v++)
+        for (; !no_copies && issued_v < RV && issued_v < nv; issued_v++)
             zs_issue(vring + issued_v * C::VSLOT, vbar + issued_v, C::VBOX, &tv, x0 - H, y0 - 1,
                      rev ? qb + 1 - issued_v : qa - 1 + issued_v);
-        for (; issued_f < RF && issued_f < nf; issued_f++)
+        for (; !no_copies && issued_f < RF && issued_f < nf; issued_f++)
             zs_issue(fring + issued_f * C::FSLOT, fbar + issued_f, C::FBOX, &tf, x0, y0,
                      rev ? qb - issued_f : qa + issued_f);
     }
@@ -161,9 +162,9 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                 // touch global memory only after copies issued below land
                 pdl_wait();
                 bool pok = true;
-                for (int i = -2; pok && i < nf; i++) {
+                for (int i = -2; pok && !no_copies && i < nf; i++) {
                     const int j = i + 2, sv = j % RV;
-                    if (j >= RV) pok = mbar_wait(vemp + sv, ((j / RV) - 1) & 1);
+                    if (j >= RV) pok = mbar_wait(vemp + sv, ((j / RV) - 1) & 1, wait_limit);
                     if (!pok) break;
                     fence_proxy_async_smem();
                     zs_issue(vring + sv * C::VSLOT, vbar + sv, C::VBOX, &tv, x0 - H, y0 - 1,
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     issued_v = j + 1;
                     if (i < 0) continue;
                     const int sf_ = i % RF;
-                    if (i >= RF) pok = mbar_wait(femp + sf_, ((i / RF) - 1) & 1);
+                    if (i >= RF) pok = mbar_wait(femp + sf_, ((i / RF) - 1) & 1, wait_limit);
                     if (!pok) break;
                     fence_proxy_async_smem();
                     zs_issue(fring + sf_ * C::FSLOT, fbar + sf_, C::FBOX, &tf, x0, y0, rev ? qb - i : qa + i);
@@ -182,11 +183,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     atomicOr(&g_gvf_zs_error, 1);
                     for (int sl = 0; sl < RV; sl++) {
                         int j = issued_v - 1 - ((issued_v - 1 - sl) % RV + RV) % RV;
-                        if (j >= 0) mbar_wait(vbar + sl, (j / RV) & 1);
+                        if (j >= 0) mbar_wait(vbar + sl, (j / RV) & 1, wait_limit);
                     }
                     for (int sl = 0; sl < RF; sl++) {
                         int j = issued_f - 1 - ((issued_f - 1 - sl) % RF + RF) % RF;
-                        if (j >= 0) mbar_wait(fbar + sl, (j / RF) & 1);
+                        if (j >= 0) mbar_wait(fbar + sl, (j / RF) & 1, wait_limit);
                     }
                 }
             }
@@ -212,8 +213,8 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     float cm[3][4], cc[3][4];
     int sm = 0, sc = 1, sp = 2, sf = 0;                   // slots: previous, current, next v plane; f plane
     uint32_t pp = 0, pf = 0;                              // phase parity of the waits on sp, sf
-    ok &= mbar_wait(vbar + 0, 0);
-    ok &= mbar_wait(vbar + 1, 0);
+    ok &= mbar_wait(vbar + 0, 0, wait_limit);
+    ok &= mbar_wait(vbar + 1, 0, wait_limit);
     if constexpr (!MIX) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -224,8 +225,8 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
 
     for (int k = 0; k < nf; k++) {
         const int q = rev ? qb - k : qa + k;
-        ok &= mbar_wait(vbar + sp, pp);
-        ok &= mbar_wait(fbar + sf, pf);
+        ok &= mbar_wait(vbar + sp, pp, wait_limit);
+        ok &= mbar_wait(fbar + sf, pf, wait_limit);
         if constexpr (WS) {
             if (__any_sync(0xffffffffu, !ok)) {
                 ok = false;
@@ -389,11 +390,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
         // wait (bounded) for this CTA's copies in flight
         for (int s = 0; s < RV; s++) {
             int j = issued_v - 1 - ((issued_v - 1 - s) % RV + RV) % RV;
-            if (j >= 0) mbar_wait(vbar + s, (j / RV) & 1);
+            if (j >= 0) mbar_wait(vbar + s, (j / RV) & 1, wait_limit);
         }
         for (int s = 0; s < RF; s++) {
             int j = issued_f - 1 - ((issued_f - 1 - s) % RF + RF) % RF;
-            if (j >= 0) mbar_wait(fbar + s, (j / RF) & 1);
+            if (j >= 0) mbar_wait(fbar + s, (j / RF) & 1, wait_limit);
         }
     }
 }
@@ -493,7 +494,7 @@ static int zs_geometry(int X, int Y, int Z, ZsLaunch<ST> &g) {
 // gvf_zs_eligible).
 template <int ST, bool WS>
 static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
-                           cudaStream_t s, int rev) {
+                           cudaStream_t s, int rev, long long wait_limit = kWaitCycles, int no_copies = 0) {
     using C = ZsCfg<ST>;
     using T = typename Store<ST>::T;
     ZsLaunch<ST> g;
@@ -506,8 +507,12 @@ static int launch_zs_typed(const void *d_f0, const void *src, void *dst, int X, 
     cudaLaunchAttribute attr[1];
     const cudaLaunchConfig_t cfg =
         pdl_config(dim3((unsigned)g.grid), dim3(C::THREADS + 32 * WS), C::SMEM, s, attr);
-    if (rev) TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, true>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
-    else TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, false>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K));
+    if (rev)
+        TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, true>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K,
+                                        wait_limit, no_copies));
+    else
+        TSF_TRY_CUDA(cudaLaunchKernelEx(&cfg, gvf_zs_kernel<ST, WS, false>, tv, tf, (T *)dst, X, Y, Z, mu, g.ntx, g.K,
+                                        wait_limit, no_copies));
     return TSF_OK;
 }
 
@@ -524,6 +529,29 @@ int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, i
     });
     TSF_CHECK_LAUNCH("gvf_zs_kernel");
     return r;
+}
+
+// Self-test of the bounded waits: one launch with every copy suppressed, so
+// each wait runs out after wait_cycles; returns the error word afterwards
+// (cleared), or a negative value if the launch itself failed.
+int gvf_zs_error(int clear);
+int gvf_zs_wait_selftest(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z,
+                         long long wait_cycles, cudaStream_t s) {
+    if (wait_cycles <= 0) return -fail(TSF_ERR_INVALID_ARG, "wait_cycles must be > 0");
+    if (!gvf_zs_eligible(st, d_f0, src, dst, X, Y, Z))
+        return -fail(TSF_ERR_INVALID_ARG, "the streaming GVF kernel cannot run these buffers");
+    if (gvf_zs_error(1) < 0) return -TSF_ERR_CUDA;
+    int r = TSF_OK;
+    TSF_DISPATCH_STORAGE(st, ST, {
+        r = launch_zs_typed<ST, ST == TSF_STORE_F16 || ST == TSF_STORE_BF16>(d_f0, src, dst, X, Y, Z, 0.05f, s, 0,
+                                                                              wait_cycles, 1);
+    });
+    if (r) return -r;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return -check_cuda(e, "GVF wait self-test");
+    count_launches(1);
+    return gvf_zs_error(1);
 }
 
 // Reads (and optionally clears) the streaming kernel's device error word;
@@ -550,6 +578,19 @@ int gvf_zs_error(int clear) {
 
 namespace tsf {
 int gvf_adjoint_zs_error(int clear);
+}
+
+extern "C" int tsf_gvf_wait_selftest(const void *d_f0, void *d_v, int X, int Y, int Z, int storage,
+                                     long long wait_cycles, void *d_workspace, size_t workspace_bytes, void *stream) {
+    using namespace tsf;
+    int r = check_dims(X, Y, Z);
+    if (r) return -r;
+    if (!valid_storage(storage)) return -fail(TSF_ERR_INVALID_ARG, "unknown storage format");
+    if (!d_f0 || !d_v) return -fail(TSF_ERR_INVALID_ARG, "null buffer");
+    const size_t need = (size_t)X * Y * Z * 3 * storage_bytes(storage);
+    if (!d_workspace || workspace_bytes < need) return -fail(TSF_ERR_WORKSPACE, "workspace too small");
+    return gvf_zs_wait_selftest(storage, d_f0, d_v, d_workspace, X, Y, Z, wait_cycles,
+                                reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tsf_gvf_device_error(int clear) {

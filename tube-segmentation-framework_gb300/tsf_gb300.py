@@ -110,6 +110,7 @@ def _declare(L):
         "tsf_gvf_one_component_workspace_size": (_sz, [_i, _i, _i, _i]),
         "tsf_gvf_one_component": (_i, [_p, _i, _i, _i, _f, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
+        "tsf_gvf_wait_selftest": (_i, [_p, _p, _i, _i, _i, _i, C.c_longlong, _p, _sz, _p]),
         "tsf_tdf_circle_ex": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _i, _p, _p, _sz, _p]),
         "tsf_gvf_residual_workspace_size": (_sz, []),
         "tsf_gvf_residual_norm": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _p, _sz, _p]),
