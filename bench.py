@@ -688,7 +688,7 @@ def run_stage(args):
         # each GVF kernel choice: one warm-up call of --iters iterations, then one timed call
         out = {"stage": "gvf", "workload": "vessel tree %d^3, %s storage, %d iterations per call" % (n, st, args.iters)}
         ws = T.workspace(T.load().tsf_gvf_workspace_size(n, n, n, T.STORAGE[st]))
-        for mode, name in ((0, "streaming"), (1, "register_vector")):
+        for mode, name in ((0, "streaming"), (1, "register_vector"), (3, "two_per_launch")):
             v = f0.clone()
             T.gvf(f0, args.mu, args.iters, st, v=v, ws=ws, mode=mode)
             torch.cuda.synchronize()
@@ -723,12 +723,16 @@ def run_stage(args):
         runs["circle"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st)
         runs["circle_paired"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=st,
                                                      ws=ws)
+        runs["circle_paired_sample_per_lane"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"],
+                                                                     storage=st, ws=ws, samples=32, mode=2)
         runs["circle_paired_closed_eigen"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"],
                                                                   storage=st, ws=ws, eigen=1)
         runs["circle_paired_12_samples"] = lambda: T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"],
                                                                 storage=st, ws=ws, samples=12)
         _, fsm = T.vector_field(vol, P["fmax"], P["vsign"], storage=st, planar=False, field4=True)
         runs["small_paired"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws)
+        runs["small_paired_sample_per_lane"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
+                                                                    samples=32, mode=2)
         runs["small_paired_closed_eigen"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
                                                                  eigen=1)
     for run in runs.values():

@@ -142,8 +142,12 @@ int tsf_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
 /* tsf_gvf with the kernel chosen: 0 = the default of tsf_gvf (the
  * z-streaming kernel fed by TMA copies wherever rows are a multiple of 16
  * bytes and the buffers 16-byte aligned, else the register-vector kernel),
- * 1 = the register-vector (or per-voxel) kernel only, 2 = same as 0.  All
- * modes give bit-identical results. */
+ * 1 = the register-vector (or per-voxel) kernel only, 2 = same as 0 with
+ * every iteration streaming upwards, 3 = two iterations per launch (temporal
+ * blocking: the first iteration's result stays in shared memory; volumes
+ * with X >= 128, Y >= 8, Z >= 5 and 16-byte rows, else as 0; an odd count
+ * ends with one launch of the default kernel).  All modes give
+ * bit-identical results. */
 int tsf_gvf_mode(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations,
                  int storage, void *d_workspace, size_t workspace_bytes, int mode, void *stream);
 
@@ -322,7 +326,9 @@ typedef struct {
                       eigenvalues nearly coincide); eigenvector signs are
                       canonical (largest component positive), so T and R agree
                       with mode 0 to the circle's sampling noise, not bit for bit */
-    int kernel;    /* 0: load-balanced sweeps (default), 1: one voxel per lane    */
+    int kernel;    /* 0: load-balanced sweeps (default), 1: one voxel per lane,
+                      2: one circle sample per lane (a warp evaluates one
+                      voxel-radius at a time); all give the same bits            */
 } tsf_tdf_options;
 
 /* tsf_tdf_circle_ws with options (NULL: the reference's 32 samples, tql2,

@@ -66,7 +66,7 @@ def test_vector_field_bitexact(torch_dev, tsf, oracle, synth, storage, vsign):
 @pytest.mark.parametrize("mu,iters", [(0.05, 17), (0.1, 8)])
 @pytest.mark.parametrize("shape", [(21, 26, 33), (19, 22, 40), (35, 9, 136), (5, 6, 8), (7, 5, 264), (6, 7, 130), (9, 10, 256),
                                    (19, 37, 136), (5, 32, 128), (21, 50, 264)])
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 3])
 def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape, mode):
     """mode 0: the z-streaming TMA kernel wherever rows are a multiple of 16
     bytes -- tiles shifted back inside at the +x / +y edges (X = 136, 264;
@@ -75,7 +75,10 @@ def test_gvf_bitexact(torch_dev, tsf, oracle, synth, storage, mu, iters, shape, 
     the 16-bit formats, X = 130 take the other kernels; taller volumes
     (Y = 32, 37, 50) cover several row tiles, the last shifted back inside.
     mode 1: the register-vector kernel (16- or 8-byte vectors, ragged last
-    warps) or, for odd rows, the one-thread-per-voxel kernel."""
+    warps) or, for odd rows, the one-thread-per-voxel kernel.  mode 3: two
+    iterations per launch where X >= 128 (X = 128, 136, 264: edge tiles shifted
+    inside), with a last one-iteration launch for an odd count (17), else as
+    mode 0."""
     torch = torch_dev
     vol = oracle.blur(_vol(synth, shape, 4), 0.5)
     ref4 = oracle.vector_field(vol, 0.2, 1, storage)
@@ -304,3 +307,20 @@ def test_gvf_on_two_devices(torch_dev, tsf, oracle, synth, storage):
             v = tsf.gvf(p, 0.05, 9, storage)
             torch.cuda.synchronize()
             assert np.array_equal(_np_stored(v, storage), ov)
+
+
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("shape,iters", [((5, 8, 128), 4), ((12, 20, 136), 9), ((40, 1024, 256), 6),
+                                          ((33, 37, 264), 10), ((130, 24, 128), 6)])
+def test_gvf_two_iterations_per_launch(torch_dev, tsf, oracle, synth, storage, shape, iters):
+    """The temporal-blocking kernel (tsf_gvf_mode 3): the thinnest volume
+    (Z = 5), edge tiles shifted back inside in x and y, z-chunks over many
+    waves (Y = 1024), a long z range (Z = 130); even and odd counts."""
+    torch = torch_dev
+    vol = oracle.blur(_vol(synth, shape, 12), 0.5)
+    ref4 = oracle.vector_field(vol, 0.2, 1, storage)
+    p, _ = tsf.vector_field(torch.from_numpy(vol).cuda(), 0.2, 1, storage)
+    tsf.gvf_device_error()
+    v = tsf.gvf(p, 0.05, iters, storage, mode=3)
+    assert np.array_equal(_np_stored(v, storage), oracle.gvf(ref4, 0.05, iters, storage))
+    assert tsf.gvf_device_error() == 0

@@ -45,7 +45,7 @@ def _dev(torch, field4, storage):
 
 @pytest.mark.parametrize("storage", ["f32", "f16", "snorm16"])
 @pytest.mark.parametrize("samples,stride", [(12, 1), (8, 4), (16, 2), (32, 1)])
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 def test_sample_count_bitexact(torch_dev, tsf, oracle, synth, storage, samples, stride, kernel):
     torch = torch_dev
     shape = (26, 30, 34)
@@ -74,11 +74,13 @@ def test_invalid_options_rejected(torch_dev, tsf):
     for samples, stride, eigen in [(10, 1, 0), (0, 1, 0), (36, 1, 0), (12, 3, 0), (32, 2, 0), (32, 1, 2)]:
         with pytest.raises(tsf.TSFError, match="TSF_ERR_INVALID_ARG"):
             tsf.tdf_circle(f, 1.0, 3.0, 0.5, samples=samples, stride=stride, eigen=eigen)
+    with pytest.raises(tsf.TSFError, match="TSF_ERR_INVALID_ARG"):
+        tsf.tdf_circle(f, 1.0, 3.0, 0.5, samples=32, mode=3)
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16", "snorm16"])
 @pytest.mark.parametrize("unorm", [False, True])
-@pytest.mark.parametrize("kernel", [0, 1])
+@pytest.mark.parametrize("kernel", [0, 1, 2])
 def test_closed_form_eigen_bitexact(torch_dev, tsf, oracle, synth, storage, unorm, kernel):
     torch = torch_dev
     shape = (28, 32, 36)
@@ -117,3 +119,27 @@ def test_closed_form_agrees_with_tql2(torch_dev, tsf, oracle, synth):
     dT = (T0 - T1).abs().cpu().numpy()
     print("closed form vs tql2 TDF: mean |dT| %.3g, p99 %.3g, max %.3g" % (dT.mean(), np.quantile(dT, 0.99), dT.max()))
     assert dT.mean() < 3e-3 and np.quantile(dT, 0.99) < 5e-2
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16", "snorm16"])
+@pytest.mark.parametrize("unorm", [False, True])
+@pytest.mark.parametrize("shape", [(28, 30, 26), (24, 22, 150), (40, 44, 49)])
+def test_sample_per_lane_kernel_bitexact(torch_dev, tsf, oracle, synth, storage, unorm, shape):
+    """TDF kernel 2 (one circle sample per lane, a warp per voxel-radius):
+    the reference filter's bits in every storage format, both radius passes,
+    with and without the paired-texel workspace; ragged bricks (X = 26, 150,
+    49) and voxels near the faces (clamped sampler)."""
+    torch = torch_dev
+    field = _field(oracle, synth, shape, 7, storage)
+    d4 = _dev(torch, field, storage) if storage != "bf16" else \
+        torch.from_numpy(field.astype(np.float32)).to(torch.bfloat16).cuda()
+    ws = tsf.workspace(tsf.load().tsf_tdf_workspace_size(shape[2], shape[1], shape[0], tsf.STORAGE[storage]))
+    for rng_ in [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)]:
+        oT, oR = oracle.tdf_circle(field, *rng_)
+        for w in (ws, None):
+            T, R = tsf.tdf_circle(d4, *rng_, storage=storage, unorm16=unorm, samples=32, mode=2, ws=w)
+            if unorm:
+                assert np.array_equal(T.cpu().numpy().view(np.uint16), oracle.to_unorm16(oT))
+            else:
+                assert np.array_equal(T.cpu().numpy(), oT)
+            assert np.array_equal(R.cpu().numpy(), oR)

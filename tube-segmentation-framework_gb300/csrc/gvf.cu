@@ -241,6 +241,10 @@ int gvf_step(int st, const void *d_f0, const void *src, void *dst, int X, int Y,
 // launch, ping-ponging with the workspace.  mode: 0 = default (the streaming
 // kernel gvf_zs_kernel where it applies, else gvf_vec_kernel), 1 = the
 // register-vector kernels only, 2 = same as 0.  All give identical results.
+bool gvf_tb2_eligible(int st, const void *d_f0, const void *a, const void *b, int X, int Y, int Z);
+int launch_gvf_tb2(int st, const void *d_f0, const void *src, void *dst, int X, int Y, int Z, float mu,
+                   cudaStream_t s);
+
 int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iterations, int st,
             void *ws, size_t ws_bytes, int mode, cudaStream_t s) {
     int r = check_dims(X, Y, Z);
@@ -248,13 +252,23 @@ int run_gvf(const void *d_f0, void *d_v, int X, int Y, int Z, float mu, int iter
     if (!valid_storage(st)) return fail(TSF_ERR_INVALID_ARG, "unknown storage format");
     if (!d_f0 || !d_v) return fail(TSF_ERR_INVALID_ARG, "null buffer");
     if (iterations < 0) return fail(TSF_ERR_INVALID_ARG, "iterations must be >= 0");
-    if (mode < 0 || mode > 2) return fail(TSF_ERR_INVALID_ARG, "unknown GVF mode");
+    if (mode < 0 || mode > 3) return fail(TSF_ERR_INVALID_ARG, "unknown GVF mode");
     if (iterations == 0) return TSF_OK;
     const size_t need = gvf_workspace_size(X, Y, Z, st);
     if (!ws || ws_bytes < need) return fail(TSF_ERR_WORKSPACE, "GVF workspace too small");
     void *a = d_v, *b = ws;
     const bool zs = mode != 1 && gvf_zs_eligible(st, d_f0, a, b, X, Y, Z);
-    for (int left = iterations; left > 0; left--) {
+    int left = iterations;
+    if (mode == 3 && gvf_tb2_eligible(st, d_f0, a, b, X, Y, Z)) {
+        // two iterations per launch; an odd count ends with one of the
+        // one-iteration kernel
+        for (; left >= 2; left -= 2) {
+            r = launch_gvf_tb2(st, d_f0, a, b, X, Y, Z, mu, s);
+            if (r) return r;
+            void *t = a; a = b; b = t;
+        }
+    }
+    for (; left > 0; left--) {
         // alternate the streaming direction: each iteration starts on the
         // planes the previous one wrote last, which are still in L2
         const int rev = mode == 2 ? 0 : (iterations - left) & 1;

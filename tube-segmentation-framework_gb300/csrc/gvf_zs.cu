@@ -593,8 +593,12 @@ extern "C" int tsf_gvf_wait_selftest(const void *d_f0, void *d_v, int X, int Y, 
                                 reinterpret_cast<cudaStream_t>(stream));
 }
 
+namespace tsf {
+int gvf_tb2_error(int clear);
+}
+
 extern "C" int tsf_gvf_device_error(int clear) {
-    const int a = tsf::gvf_zs_error(clear), b = tsf::gvf_adjoint_zs_error(clear);
-    if (a < 0 || b < 0) return -1;
-    return (a ? 1 : 0) | (b ? 2 : 0);
+    const int a = tsf::gvf_zs_error(clear), b = tsf::gvf_adjoint_zs_error(clear), c = tsf::gvf_tb2_error(clear);
+    if (a < 0 || b < 0 || c < 0) return -1;
+    return (a || c ? 1 : 0) | (b ? 2 : 0);
 }

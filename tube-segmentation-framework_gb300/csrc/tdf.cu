@@ -8,7 +8,7 @@
 namespace tsf {
 
 int launch_tdf_kernels_closed(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                              const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, bool queue,
+                              const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, int kernel,
                               const uint4 *P, int fast_ok);
 
 // The x-paired copy of a 16-bit field4 image: P[i] = (texel i, texel of the
@@ -57,7 +57,8 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
         return fail(TSF_ERR_INVALID_ARG, "samples must be a multiple of 4 in [4, 32] and (samples - 1) * stride < 32");
     if (eigen != 0 && eigen != 1) return fail(TSF_ERR_INVALID_ARG, "eigen mode must be 0 (tql2) or 1 (closed form)");
     const CircleTable tab = host_circle_table(samples, stride);
-    const bool queue = tdf_mode != 1;
+    if (tdf_mode < 0 || tdf_mode > 2) return fail(TSF_ERR_INVALID_ARG, "unknown TDF kernel");
+    const bool queue = tdf_mode != 1;   // the brick kernels (0 and 2) may sample the paired copy
     const int fast_ok = (int64_t)X * Y * Z < ((int64_t)1 << 31) - 1;   // 32-bit texel offsets
     const int64_t n = (int64_t)X * Y * Z;
     const size_t need = tdf_workspace_size(X, Y, Z, st);
@@ -69,9 +70,10 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
         TSF_CHECK_LAUNCH("tdf_pair_kernel");
     }
     if (eigen == 1)
-        return launch_tdf_kernels_closed(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, queue, P,
-                                         fast_ok);
-    return launch_tdf_kernels<0>(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, queue, P, fast_ok);
+        return launch_tdf_kernels_closed(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, tdf_mode,
+                                         P, fast_ok);
+    return launch_tdf_kernels<0>(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, tdf_mode, P,
+                                 fast_ok);
 }
 
 int launch_tdf_combine(const void *Ts, const float *Rs, void *Tl, float *Rl, int64_t n, int unorm, cudaStream_t s) {

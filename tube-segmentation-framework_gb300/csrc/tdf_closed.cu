@@ -6,9 +6,9 @@
 namespace tsf {
 
 int launch_tdf_kernels_closed(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                              const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, bool queue,
+                              const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, int kernel,
                               const uint4 *P, int fast_ok) {
-    return launch_tdf_kernels<1>(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, queue, P, fast_ok);
+    return launch_tdf_kernels<1>(d_field4, X, Y, Z, st, rmin, rmax, rstep, tab, d_T, unorm, d_R, s, kernel, P, fast_ok);
 }
 
 }  // namespace tsf

@@ -211,19 +211,146 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
 }
 
 
-// Launches the sweep kernel of eigen mode EIG.  queue: load-balanced sweeps
-// (tdf_queue_kernel) else one voxel per lane; P: the x-paired 16-bit copy of
-// the field (queue only) or null.
+// Same filter with one circle sample per lane.
+//
+// The load-balanced sweeps above leave lanes idle at the end of each warp's
+// queue (a voxel whose sweep runs to ten radii keeps its lane busy while the
+// others have nothing left) and where a warp mixes voxels near the volume's
+// faces (clamped sampler) with interior ones: about 29 % of the lanes idled
+// in the sweeps.  Here a warp evaluates one voxel-radius at a time with lane j
+// computing sample j of the circle, so every lane has work as long as any
+// voxel-radius is left, and all lanes take the same sampler path.  A batch
+// takes the current radius of every voxel held in the warp's 32 slots (slot v
+// owned by lane v, refilled from the 128-voxel block in lane order as
+// sweeps end); the 32 samples of each voxel-radius go to shared memory and
+// the owning lane then sums them in sample order, so each voxel's arithmetic
+// -- samples, their order of summation, the division, the comparison that
+// ends the sweep -- is exactly tdf_circle_kernel's.
+template <int ST, bool NORM, bool UNORM, bool PAIR, int EIG>
+__global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__restrict__ F, int X, int Y, int Z,
+                                                                   float rmin, float rmax, float rstep,
+                                                                   const CircleTable tab, void *T,
+                                                                   float *__restrict__ Rout, int fast_ok,
+                                                                   const uint4 *__restrict__ P) {
+    static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
+    __shared__ float se[kTdfWarps][6][kSeg];
+    __shared__ unsigned char sin_[kTdfWarps][kSeg];
+    __shared__ float dtb[kTdfWarps][32][33];               // [slot][sample], padded row
+    const int XY = X * Y, margin = sample_margin(rmax);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
+    const int b = blockIdx.x;
+    const int bx0 = (b % nbx) * 8, by0 = ((b / nbx) % nby) * 8 + (w & 1) * 4;
+    const int bz0 = (b / (nbx * nby)) * 8 + (w >> 1) * 4;
+    const int ntask = kSeg;
+    auto tx = [&](int t) { return bx0 + (t & 7); };
+    auto ty = [&](int t) { return by0 + ((t >> 3) & 3); };
+    auto tz = [&](int t) { return bz0 + (t >> 5); };
+    auto inside = [&](int t) { return tx(t) < X && ty(t) < Y && tz(t) < Z; };
+    // phase 1: eigenvectors of the block's voxels (one voxel per lane)
+    for (int t = lane; t < ntask; t += 32) {
+        if (!inside(t)) continue;
+        float H[3][3], V[3][3];
+        hessian<ST, NORM>(F, X, Y, Z, tx(t), ty(t), tz(t), H);
+        tdf_eigen<EIG>(H, V);
+        se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
+        se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
+        const float e2[3] = {V[0][1], V[1][1], V[2][1]}, e3[3] = {V[0][2], V[1][2], V[2][2]};
+        sin_[w][t] = fast_ok && samples_inside(tx(t), ty(t), tz(t), X, Y, Z, margin, e2, e3);
+    }
+    __syncwarp();
+    // phase 2: batches of voxel-radii, one sample per lane
+    const unsigned full = 0xffffffffu;
+    const int ns = tab.n;
+    const float cj = tab.c[lane], sj = tab.s[lane];       // this lane's sample direction (lane < ns)
+    int task = lane < ntask ? lane : -1;
+    int next = 32;
+    float radius = rmin, maxSum = 0.0f, maxRadius = 0.0f;
+    int nr = 0;
+    while (__any_sync(full, task >= 0)) {
+        const bool eval = task >= 0 && inside(task) && radius <= rmax && nr < kMaxRadii;
+        const unsigned M = __ballot_sync(full, eval);
+        for (unsigned m = M; m; m &= m - 1) {
+            const int v = __ffs(m) - 1;
+            const int tv = __shfl_sync(full, task, v);
+            const float rv = __shfl_sync(full, radius, v);
+            const float e2x = se[w][0][tv], e2y = se[w][1][tv], e2z = se[w][2][tv];
+            const float e3x = se[w][3][tv], e3y = se[w][4][tv], e3z = se[w][5][tv];
+            const float fx = (float)tx(tv), fy = (float)ty(tv), fz = (float)tz(tv);
+            float dt = 0.0f;
+            if (lane < ns) {
+                const float va0 = cj * e3x + sj * e2x;
+                const float va1 = cj * e3y + sj * e2y;
+                const float va2 = cj * e3z + sj * e2z;
+                float3 smp;
+                if (sin_[w][tv]) {
+                    if constexpr (PAIR)
+                        smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                    else
+                        smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                } else {
+                    smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                }
+                dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+            }
+            dtb[w][v][lane] = dt;
+        }
+        __syncwarp();
+        bool done = true;
+        if (eval) {
+            float rs = 0.0f;
+            for (int j = 0; j < ns; j++) rs = rs + dtb[w][lane][j];
+            rs = rs / (float)ns;
+            if (rs > maxSum) {
+                maxSum = rs;
+                maxRadius = radius;
+                radius = radius + rstep;
+                nr++;
+                done = false;
+            }
+        }
+        __syncwarp();
+        if (task >= 0 && done && inside(task)) {
+            const int64_t i = lin(tx(task), ty(task), tz(task), X, Y);
+            if (UNORM) reinterpret_cast<uint16_t *>(T)[i] = to_unorm16(maxSum);
+            else reinterpret_cast<float *>(T)[i] = maxSum;
+            Rout[i] = maxRadius;
+        }
+        // lanes whose sweep ended take the next voxels, in lane order
+        const unsigned want = __ballot_sync(full, task >= 0 && done) | __ballot_sync(full, task < 0 && next < ntask);
+        if ((want >> lane) & 1u) {
+            const int k = next + __popc(want & ((1u << lane) - 1u));
+            task = k < ntask ? k : -1;
+            radius = rmin;
+            maxSum = 0.0f;
+            maxRadius = 0.0f;
+            nr = 0;
+        }
+        next += __popc(want);
+    }
+}
+
+// Launches the sweep kernel of eigen mode EIG.  kernel: 0 = load-balanced
+// sweeps (tdf_queue_kernel), 1 = one voxel per lane (tdf_circle_kernel), 2 =
+// one sample per lane (tdf_lane_kernel); P: the x-paired 16-bit copy of the
+// field (kernels 0 and 2) or null.
 template <int EIG>
 int launch_tdf_kernels(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
-                       const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, bool queue,
+                       const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, int kernel,
                        const uint4 *P, int fast_ok) {
+    const bool queue = kernel == 0;
     const dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
     const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
     const unsigned qblocks = (unsigned)(((X + 7) / 8) * ((Y + 7) / 8) * ((Z + 7) / 8));   // 8^3 bricks
 #define TSF_TDF_LAUNCH(ST, NORM, UN)                                                                                 \
     do {                                                                                                             \
-        if (queue && P)                                                                                              \
+        if (kernel == 2 && P)                                                                                        \
+            tdf_lane_kernel<ST, NORM, UN, ST != TSF_STORE_F32, EIG><<<qblocks, 32 * kTdfWarps, 0, s>>>(             \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, P);                                    \
+        else if (kernel == 2)                                                                                        \
+            tdf_lane_kernel<ST, NORM, UN, false, EIG><<<qblocks, 32 * kTdfWarps, 0, s>>>(                           \
+                d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, nullptr);                              \
+        else if (queue && P)                                                                                         \
             tdf_queue_kernel<ST, NORM, UN, ST != TSF_STORE_F32, EIG><<<qblocks, 32 * kTdfWarps, 0, s>>>(            \
                 d_field4, X, Y, Z, rmin, rmax, rstep, tab, d_T, d_R, fast_ok, P);                                    \
         else if (queue)                                                                                              \
