@@ -462,6 +462,7 @@ def run_tsf(args, rank, world):
     res["segmentation"] = segmentation_timing(torch, T, pipe,
                                               rank == 0 and world == 1 and not args.no_cpu_baseline)
     res["spline_tdf"] = spline_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
+    res["run_api"] = run_api_timing(args, vol)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
@@ -528,6 +529,45 @@ def fwd_adjoint_timing(torch, pipe, args, storage=None, checkpoint_every=None):
             "adjoint_workspace_gb": round(state["gvf_ws"].numel() / 1e9, 2),
             "fwd_ms": round(fwd, 3), "fwd_adjoint_ms": round(both, 3), "ratio": round(both / fwd, 3),
             "note": "loss mean((TDF - G)^2); gradients w.r.t. the volume, mu and blur sigma"}
+
+
+def run_api_timing(args, vol, repeats=3):
+    """The drop-in C++ API end to end: run(filename, paramList, kernel_dir)
+    on the benchmark volume written as an .mhd/.raw file (MET_FLOAT,
+    toFloat window [0, 1]) with the workload's parameters (FP16 GVF storage,
+    the reference's 16-bit TDF, linking with the Synthetic-Vascusynth
+    constants, inverse-gradient segmentation), timed on the host clock by the
+    C++ driver (tests/cpp/test_api.cpp bench): file read, uploads, the whole
+    pipeline and the getters' copies of the TDF, centerline and segmentation."""
+    import tempfile
+    import build as tsf_build
+    exe = tsf_build.API_TESTS
+    if not os.path.exists(exe):
+        return {"error": "C++ driver not built"}
+    P = PARAMS
+    n = args.size
+    with tempfile.TemporaryDirectory() as d:
+        base = os.path.join(d, "vol")
+        with open(base + ".mhd", "w") as f:
+            f.write("ObjectType = Image\nNDims = 3\nDimSize = %d %d %d\nElementType = MET_FLOAT\n"
+                    "ElementDataFile = vol.raw\n" % (n, n, n))
+        np.ascontiguousarray(vol, np.float32).tofile(base + ".raw")
+        cmd = [exe, "bench", base + ".mhd", str(repeats), "--minimum", "0", "--maximum", "1", "--mode", "white",
+               "--large-blur", str(P["large_blur"]), "--small-blur", "0", "--fmax", str(P["fmax"]),
+               "--gvf-mu", str(args.mu), "--gvf-iterations", str(args.iters), "--radius-min", str(P["rmin"]),
+               "--radius-max", str(P["rmax"]), "--radius-step", str(P["rstep"]), "--tdf-high", str(P["tdf_high"]),
+               "--cube-size", str(P["cube_size"]), "--gvf-storage", args.storage, "--16bit-vectors", "true",
+               "--min-mean-tdf", "0.3", "--max-distance", "10", "--min-tree-length", "3"]
+        p = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    if p.returncode != 0:
+        return {"error": (p.stdout + p.stderr)[-400:]}
+    r = json.loads(p.stdout.strip().splitlines()[-1])
+    med = float(np.median(r["run_ms"]))
+    return {"ms_per_volume": round(med, 2), "volumes_per_s": round(1e3 / med, 3),
+            "gvox_iter_s": round(n ** 3 * args.iters / (med * 1e-3) / 1e9, 2), "runs_ms": r["run_ms"],
+            "vertices": r["vertices"], "segmented_voxels": r["segmented_voxels"],
+            "note": "run() through the C++ API, host clock, median of %d after one warm-up; includes reading the "
+                    "%d MB .raw file" % (repeats, n ** 3 * 4 // 1000000)}
 
 
 def linking_timing(torch, T, pipe, with_cpu):

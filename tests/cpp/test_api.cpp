@@ -4,12 +4,16 @@
 // assertion layer (GTest is not available).
 //
 //   test_api cpu                 parameter, TSFOutput and I/O tests (no GPU)
+//   test_api bench <file.mhd> <repeats> [--name value ...]
+//                                run() timed end to end (one JSON line)
 //   test_api run <file.mhd> <out_dir> [--name value ...]
 //                                run() on a volume; writes tdf.raw (float),
 //                                centerline.raw (int8), segmentation.raw
 //                                (int8, when there is one), vertices.txt,
 //                                size.txt and shift.txt
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
@@ -209,9 +213,53 @@ static int run_mode(int argc, char **argv) {
     return 0;
 }
 
+// argv: test_api bench <file.mhd> <repeats> [--name value ...]: run() once
+// to warm up, then `repeats` times, each timed end to end on the host clock
+// (the file read, the uploads, the whole pipeline and the copies of the TDF,
+// centerline and segmentation the getters make) and printed as one JSON line.
+static int bench_mode(int argc, char **argv) {
+    std::vector<char *> args;
+    args.push_back(argv[0]);
+    args.push_back(argv[2]);
+    for (int i = 4; i < argc; i++) args.push_back(argv[i]);
+    const int repeats = std::atoi(argv[3]);
+    std::vector<double> ms;
+    size_t vertices = 0, segmented = 0;
+    for (int k = -1; k < repeats; k++) {
+        paramList parameters = getParameters((int)args.size(), args.data());
+        const auto t0 = std::chrono::steady_clock::now();
+        TSFOutput *o = nullptr;
+        try {
+            o = run(argv[2], parameters, KERNELS_DIR);
+        } catch (const SIPL::SIPLException &e) {
+            std::cerr << "SIPLException: " << e.what() << std::endl;
+            return 3;
+        }
+        const SIPL::int3 s = *o->getSize();
+        const size_t n = (size_t)s.x * s.y * s.z;
+        const float *tdf = o->getTDF();
+        const char *cl = o->hasCenterlineVoxels() ? o->getCenterlineVoxels() : nullptr;
+        const char *seg = o->hasSegmentation() ? o->getSegmentation() : nullptr;
+        const auto t1 = std::chrono::steady_clock::now();
+        if (k >= 0) ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+        vertices = o->getCenterpoints().size();
+        segmented = 0;
+        if (seg)
+            for (size_t i = 0; i < n; i++) segmented += seg[i] != 0;
+        (void)tdf;
+        (void)cl;
+        delete o;
+    }
+    std::cout << "{\"run_ms\": [";
+    for (size_t i = 0; i < ms.size(); i++) std::cout << (i ? ", " : "") << ms[i];
+    std::cout << "], \"vertices\": " << vertices << ", \"segmented_voxels\": " << segmented << "}" << std::endl;
+    return 0;
+}
+
 int main(int argc, char **argv) {
     const std::string mode = argc > 1 ? argv[1] : "cpu";
     if (mode == "run" && argc >= 4) return run_mode(argc, argv);
+    if (mode == "bench" && argc >= 4) return bench_mode(argc, argv);
     parameter_tests();
     output_tests();
     io_tests();
