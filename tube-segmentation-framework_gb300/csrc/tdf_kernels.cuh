@@ -270,47 +270,30 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
     while (__any_sync(full, task >= 0)) {
         const bool eval = task >= 0 && inside(task) && radius <= rmax && nr < kMaxRadii;
         const unsigned M = __ballot_sync(full, eval);
-        // sample `lane` of voxel-radius (tv, rv); interior: the unclamped sampler
-        auto dt_of = [&](int tv, float rv, bool interior) -> float {
+        for (unsigned m = M; m; m &= m - 1) {
+            const int v = __ffs(m) - 1;
+            const int tv = __shfl_sync(full, task, v);
+            const float rv = __shfl_sync(full, radius, v);
             const float e2x = se[w][0][tv], e2y = se[w][1][tv], e2z = se[w][2][tv];
             const float e3x = se[w][3][tv], e3y = se[w][4][tv], e3z = se[w][5][tv];
             const float fx = (float)tx(tv), fy = (float)ty(tv), fz = (float)tz(tv);
-            const float va0 = cj * e3x + sj * e2x;
-            const float va1 = cj * e3y + sj * e2y;
-            const float va2 = cj * e3z + sj * e2z;
-            float3 smp;
-            if (interior) {
-                if constexpr (PAIR)
-                    smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
-                else
-                    smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
-            } else {
-                smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
-            }
-            return ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
-        };
-        // two voxel-radii per pass, so each lane keeps two samples' gathers in
-        // flight (an odd last one is evaluated twice and stored once)
-        for (unsigned m = M; m;) {
-            const int v1 = __ffs(m) - 1;
-            m &= m - 1;
-            const int v2 = m ? __ffs(m) - 1 : v1;
-            if (m) m &= m - 1;
-            const int t1 = __shfl_sync(full, task, v1), t2 = __shfl_sync(full, task, v2);
-            const float r1 = __shfl_sync(full, radius, v1), r2 = __shfl_sync(full, radius, v2);
-            const bool i1 = sin_[w][t1], i2 = sin_[w][t2];
-            float d1 = 0.0f, d2 = 0.0f;
+            float dt = 0.0f;
             if (lane < ns) {
-                if (i1 && i2) {                                // uniform: both unclamped, straight-line
-                    d1 = dt_of(t1, r1, true);
-                    d2 = dt_of(t2, r2, true);
+                const float va0 = cj * e3x + sj * e2x;
+                const float va1 = cj * e3y + sj * e2y;
+                const float va2 = cj * e3z + sj * e2z;
+                float3 smp;
+                if (sin_[w][tv]) {
+                    if constexpr (PAIR)
+                        smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                    else
+                        smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
                 } else {
-                    d1 = dt_of(t1, r1, i1);
-                    d2 = dt_of(t2, r2, i2);
+                    smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
                 }
+                dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
             }
-            dtb[w][v1][lane] = d1;
-            dtb[w][v2][lane] = d2;
+            dtb[w][v][lane] = dt;
         }
         __syncwarp();
         bool done = true;
