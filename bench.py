@@ -771,8 +771,8 @@ def run_stage(args):
                                                                 storage=st, ws=ws, samples=12)
         _, fsm = T.vector_field(vol, P["fmax"], P["vsign"], storage=st, planar=False, field4=True)
         runs["small_paired"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws)
-        runs["small_paired_sample_per_lane"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
-                                                                    samples=32, mode=2)
+        runs["small_paired_queue"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
+                                                          samples=32, mode=3)
         runs["small_paired_closed_eigen"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
                                                                  eigen=1)
     for run in runs.values():

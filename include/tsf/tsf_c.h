@@ -290,8 +290,9 @@ int tsf_gvf_one_component(const void *d_field4_in, int X, int Y, int Z, float mu
 int tsf_tdf_circle(const void *d_field4, int X, int Y, int Z, int storage, float rmin, float rmax,
                    float rstep, void *d_T, int tdf_unorm16, float *d_R, void *stream);
 
-/* tsf_tdf_circle with the kernel forced: mode 1 = one voxel per lane, 0 = the
- * default (radius sweeps load-balanced within each warp).  Identical results. */
+/* tsf_tdf_circle with the kernel forced: mode 1 = one voxel per lane, 2 = one
+ * circle sample per lane, 3 = radius sweeps load-balanced within each warp,
+ * 0 = the default (2 when every radius is <= 3, else 3).  Identical results. */
 int tsf_tdf_circle_mode(const void *d_field4, int X, int Y, int Z, int storage, float rmin,
                         float rmax, float rstep, void *d_T, int tdf_unorm16, float *d_R, int mode,
                         void *stream);
@@ -326,9 +327,11 @@ typedef struct {
                       eigenvalues nearly coincide); eigenvector signs are
                       canonical (largest component positive), so T and R agree
                       with mode 0 to the circle's sampling noise, not bit for bit */
-    int kernel;    /* 0: load-balanced sweeps (default), 1: one voxel per lane,
-                      2: one circle sample per lane (a warp evaluates one
-                      voxel-radius at a time); all give the same bits            */
+    int kernel;    /* 0: default (one sample per lane when every radius is
+                      <= 3, else the load-balanced sweeps), 1: one voxel per
+                      lane, 2: one circle sample per lane (a warp evaluates one
+                      voxel-radius at a time), 3: load-balanced sweeps; all give
+                      the same bits                                             */
 } tsf_tdf_options;
 
 /* tsf_tdf_circle_ws with options (NULL: the reference's 32 samples, tql2,

@@ -153,10 +153,10 @@ def _to_device_field4(torch, field4, storage):
 @pytest.mark.parametrize("storage", STORAGES)
 @pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)])
 @pytest.mark.parametrize("unorm", [False, True])
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm, mode):
-    """Both TDF kernels (load-balanced sweeps over 8^3 bricks, one voxel per
-    lane).  X = 26 and X = 150 end in ragged bricks; both shapes hold voxels
+    """Every TDF kernel (0: the default per radius range, 1: one voxel per
+    lane, 2: one sample per lane, 3: load-balanced sweeps over 8^3 bricks).  X = 26 and X = 150 end in ragged bricks; both shapes hold voxels
     whose samples all lie inside (the unclamped sampler) and voxels near the
     faces (the clamped one)."""
     torch = torch_dev

@@ -45,7 +45,7 @@ def _dev(torch, field4, storage):
 
 @pytest.mark.parametrize("storage", ["f32", "f16", "snorm16"])
 @pytest.mark.parametrize("samples,stride", [(12, 1), (8, 4), (16, 2), (32, 1)])
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
 def test_sample_count_bitexact(torch_dev, tsf, oracle, synth, storage, samples, stride, kernel):
     torch = torch_dev
     shape = (26, 30, 34)
@@ -75,12 +75,12 @@ def test_invalid_options_rejected(torch_dev, tsf):
         with pytest.raises(tsf.TSFError, match="TSF_ERR_INVALID_ARG"):
             tsf.tdf_circle(f, 1.0, 3.0, 0.5, samples=samples, stride=stride, eigen=eigen)
     with pytest.raises(tsf.TSFError, match="TSF_ERR_INVALID_ARG"):
-        tsf.tdf_circle(f, 1.0, 3.0, 0.5, samples=32, mode=3)
+        tsf.tdf_circle(f, 1.0, 3.0, 0.5, samples=32, mode=4)
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16", "snorm16"])
 @pytest.mark.parametrize("unorm", [False, True])
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3])
 def test_closed_form_eigen_bitexact(torch_dev, tsf, oracle, synth, storage, unorm, kernel):
     torch = torch_dev
     shape = (28, 32, 36)

@@ -136,7 +136,7 @@ int tsf_tdf_circle_ex(const void *d_field4, int X, int Y, int Z, int storage, fl
                       size_t workspace_bytes, void *stream) {
     const tsf_tdf_options def = {32, 1, 0, 0};
     const tsf_tdf_options &o = options ? *options : def;
-    if (o.kernel < 0 || o.kernel > 2) return fail(TSF_ERR_INVALID_ARG, "kernel must be 0, 1 or 2");
+    if (o.kernel < 0 || o.kernel > 3) return fail(TSF_ERR_INVALID_ARG, "kernel must be 0, 1, 2 or 3");
     return launch_tdf_circle(d_field4, X, Y, Z, storage, rmin, rmax, rstep, d_T, tdf_unorm16, d_R, S(stream),
                              o.kernel, d_workspace, workspace_bytes, o.samples, o.stride, o.eigen);
 }

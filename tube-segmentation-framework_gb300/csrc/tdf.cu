@@ -41,7 +41,8 @@ __global__ void combine_kernel(const void *__restrict__ Ts, const float *__restr
     }
 }
 
-// tdf_mode: 0 = default (load-balanced sweeps), 1 = one voxel per lane.
+// tdf_mode: 0 = default (per radius range, see launch_tdf_kernels), 1 = one
+// voxel per lane, 2 = one sample per lane, 3 = load-balanced sweeps.
 // ws / ws_bytes: room for the x-paired copy of a 16-bit field (tdf_workspace_size);
 // without it, or for FP32 storage, the samples read the field itself.
 // samples / stride: circle samples per radius and the table stride (32 / 1 in
@@ -57,8 +58,8 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
         return fail(TSF_ERR_INVALID_ARG, "samples must be a multiple of 4 in [4, 32] and (samples - 1) * stride < 32");
     if (eigen != 0 && eigen != 1) return fail(TSF_ERR_INVALID_ARG, "eigen mode must be 0 (tql2) or 1 (closed form)");
     const CircleTable tab = host_circle_table(samples, stride);
-    if (tdf_mode < 0 || tdf_mode > 2) return fail(TSF_ERR_INVALID_ARG, "unknown TDF kernel");
-    const bool queue = tdf_mode != 1;   // the brick kernels (0 and 2) may sample the paired copy
+    if (tdf_mode < 0 || tdf_mode > 3) return fail(TSF_ERR_INVALID_ARG, "unknown TDF kernel");
+    const bool queue = tdf_mode != 1;   // the brick kernels (0, 2, 3) may sample the paired copy
     const int fast_ok = (int64_t)X * Y * Z < ((int64_t)1 << 31) - 1;   // 32-bit texel offsets
     const int64_t n = (int64_t)X * Y * Z;
     const size_t need = tdf_workspace_size(X, Y, Z, st);
