@@ -62,6 +62,10 @@ def parse():
                     help="z-planes of the volume one reference-arm step processes")
     ap.add_argument("--accuracy", action="store_true",
                     help="instead of timing: errors of every storage format against the FP64 oracle")
+    ap.add_argument("--polish", action="store_true",
+                    help="16-bit GVF with its last --polish-iters iterations in FP32: vertex list against the FP64 "
+                         "oracle and step time against the FP16 and FP32 paths")
+    ap.add_argument("--polish-iters", type=int, default=20)
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
@@ -1205,6 +1209,78 @@ def run_accuracy(args):
     return out
 
 
+def run_polish(args):
+    """The 16-bit path that reproduces the FP64 centerline: GVF in --storage
+    for K - k iterations, then k in FP32 (the iterate converted, f0 in FP32),
+    the finished field in FP32 and the small-radius pass on the FP32 field of
+    the raw volume; both TDF passes, combine and the candidate stage as in the
+    benchmark step.  Reports, per variant, the vertex list against the FP64
+    oracle run of the same method and the step time (CUDA events, median of 3
+    after a warm-up) next to the plain 16-bit and FP32 paths."""
+    import torch
+    import oracle as O
+    import synthetic
+    import tsf_gb300 as T
+    O.build()
+    n, K, k = args.size, args.iters, args.polish_iters
+    shape = (n, n, n)
+    P = PARAMS
+    vol = synthetic.vascular_tree(shape, seed=args.seed)
+    t0 = time.perf_counter()
+    _, _, _, V64 = fp64_vessel_method(O, vol, K, args.mu)
+    t_oracle = time.perf_counter() - t0
+    g = torch.from_numpy(vol).cuda()
+    L = T.load()
+    ws16 = T.workspace(L.tsf_tdf_workspace_size(n, n, n, T.STORAGE[args.storage]))
+
+    def path(st, kp, fin_st, small_st):
+        b = T.blur(g, P["large_blur"])
+        f0, _ = T.vector_field(b, P["fmax"], P["vsign"], st)
+        v = T.gvf(f0, args.mu, K - kp, st)
+        if kp:
+            f32, _ = T.vector_field(b, P["fmax"], P["vsign"], "f32")
+            v = T.gvf(f32, args.mu, kp, "f32", v=T.convert_field(v, st, "f32"))
+            vst = "f32"
+        else:
+            vst = st
+        if fin_st != vst:
+            v = T.convert_field(v, vst, fin_st)
+        field = T.gvf_finish(v, fin_st)
+        _, fs = T.vector_field(g, P["fmax"], P["vsign"], small_st, planar=False, field4=True)
+        wss = ws16 if small_st != "f32" else None
+        wsl = ws16 if fin_st != "f32" else None
+        Ts, Rs = T.tdf_circle(fs, P["rmin"], 3.0, 0.5, storage=small_st, ws=wss)
+        Tl, Rl = T.tdf_circle(field, max(2.5, P["rmin"]), P["rmax"], P["rstep"], storage=fin_st, ws=wsl)
+        T.tdf_combine(Ts, Rs, Tl, Rl)
+        return T.candidates(Tl, Rl, field, fin_st, P["tdf_high"], P["cube_size"], raise_on_range=False)
+
+    st = args.storage
+    variants = {"%s" % st: (st, 0, st, st), "f32": ("f32", 0, "f32", "f32"),
+                "%s+%d_f32_polish" % (st, k): (st, k, "f32", "f32"),
+                "%s+%d_f32_polish_%s_small" % (st, k, st): (st, k, "f32", st)}
+    s64 = set(map(tuple, V64.tolist()))
+    out = {"size": n, "iterations": K, "mu": args.mu, "fp64_vertices": int(len(V64)), "oracle_s": round(t_oracle, 1),
+           "note": "step = blur, vector fields, GVF, finish, both TDF passes, combine, candidates; CUDA events, "
+                   "median of 3 after one warm-up"}
+    for name, a in variants.items():
+        r = path(*a)
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = path(*a)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        got = r["vertices"].cpu().numpy()
+        sg = set(map(tuple, got.tolist()))
+        out[name] = {"ms": round(float(np.median(times)), 2), "vertices": int(len(got)),
+                     "missing_fp64": len(s64 - sg), "extra": len(sg - s64),
+                     "same_vertex_list": bool(np.array_equal(got, V64))}
+    return out
+
+
 def run_fmg_workload(args):
     """The 512x512x400 lung-airway CT (int16 HU, window [-1100, -600], dark
     tubes: vsign -1) through the hot path with full-multigrid GVF (3 levels,
@@ -1343,6 +1419,9 @@ def main():
         return
     if args.accuracy:
         print(json.dumps(run_accuracy(args)))
+        return
+    if args.polish:
+        print(json.dumps(run_polish(args)))
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

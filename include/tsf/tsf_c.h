@@ -225,6 +225,15 @@ int tsf_gvf_converge(const void *d_f0, void *d_v, int X, int Y, int Z, float mu,
                      int check_every, double tolerance, int storage, int *iterations_done,
                      double *residual_rms, void *d_workspace, size_t workspace_bytes, void *stream);
 
+/* Converts n stored components from one storage format to another: each
+ * value as it reads (e.g. max(-1, s / 32767) for snorm16) rounded to the
+ * target format.  d_in and d_out must not overlap.  No counterpart in the
+ * reference, whose fields keep one format; lets a caller continue a 16-bit
+ * GVF in FP32 (tsf_gvf with FP32 storage from the converted iterate and an
+ * FP32 f0) or store an FP32 field in 16 bits for the TDF. */
+int tsf_convert_field(const void *d_in, int in_storage, void *d_out, int out_storage, int64_t n,
+                      void *stream);
+
 /* Workspace bytes for tsf_gvf_adjoint. */
 size_t tsf_gvf_adjoint_workspace_size(int X, int Y, int Z, int storage, int iterations,
                                       int checkpoint_every);

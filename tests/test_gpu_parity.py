@@ -324,3 +324,22 @@ def test_gvf_two_iterations_per_launch(torch_dev, tsf, oracle, synth, storage, s
     v = tsf.gvf(p, 0.05, iters, storage, mode=3)
     assert np.array_equal(_np_stored(v, storage), oracle.gvf(ref4, 0.05, iters, storage))
     assert tsf.gvf_device_error() == 0
+
+
+@pytest.mark.parametrize("src", STORAGES)
+@pytest.mark.parametrize("dst", STORAGES)
+def test_convert_field(torch_dev, tsf, oracle, src, dst):
+    """tsf_convert_field: each stored value as it reads, rounded to the target
+    format -- the oracle's quantisation of the read value."""
+    torch = torch_dev
+    rng = np.random.default_rng(4)
+    a = np.concatenate([rng.uniform(-1.2, 1.2, 5000), [0.0, -0.0, 1.0, -1.0, 1e-7, 3e-5]]).astype(np.float32)
+    a = oracle.quantize(a, src)
+    if src == "snorm16":
+        t = torch.from_numpy(np.rint(a.astype(np.float64) * 32767).astype(np.int16)).cuda()
+    elif src == "bf16":
+        t = torch.from_numpy(a).to(torch.bfloat16).cuda()
+    else:
+        t = torch.from_numpy(a.astype(np.float16 if src == "f16" else np.float32)).cuda()
+    out = tsf.convert_field(t, src, dst)
+    assert np.array_equal(_np_stored(out, dst), oracle.quantize(a, dst))

@@ -32,7 +32,7 @@ CUDA_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "--expt-re
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE]
 
-CU_SOURCES = ["capi.cu", "vector_field.cu", "gvf.cu", "gvf_zs.cu", "gvf_tb2.cu", "gvf_one.cu", "tdf.cu", "tdf_closed.cu", "candidates.cu", "fmg.cu", "noalloc.cu", "input.cu", "gvf_adjoint.cu", "gvf_adjoint_zs.cu", "tdf_adjoint.cu", "link.cu", "segment.cu", "crop.cu", "tdf_spline.cu", "residual.cu"]
+CU_SOURCES = ["capi.cu", "vector_field.cu", "gvf.cu", "gvf_zs.cu", "gvf_tb2.cu", "gvf_one.cu", "tdf.cu", "tdf_closed.cu", "candidates.cu", "fmg.cu", "noalloc.cu", "input.cu", "gvf_adjoint.cu", "gvf_adjoint_zs.cu", "tdf_adjoint.cu", "link.cu", "segment.cu", "crop.cu", "tdf_spline.cu", "residual.cu", "convert.cu"]
 
 
 def _cuda_lib_dir():

@@ -112,6 +112,7 @@ def _declare(L):
         "tsf_gvf_fmg": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p, _sz, _p]),
         "tsf_gvf_wait_selftest": (_i, [_p, _p, _i, _i, _i, _i, C.c_longlong, _p, _sz, _p]),
         "tsf_tdf_circle_ex": (_i, [_p, _i, _i, _i, _i, _f, _f, _f, _p, _p, _i, _p, _p, _sz, _p]),
+        "tsf_convert_field": (_i, [_p, _i, _p, _i, _i64, _p]),
         "tsf_gvf_residual_workspace_size": (_sz, []),
         "tsf_gvf_residual_norm": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _i, _p, _p, _sz, _p]),
         "tsf_gvf_converge_workspace_size": (_sz, [_i, _i, _i, _i]),
@@ -610,6 +611,14 @@ def gvf_one_component(field4, mu: float, iterations: int, storage: str = "f32", 
     out = torch.empty_like(field4)
     _check(L.tsf_gvf_one_component(_ptr(field4), X, Y, Z, float(mu), int(iterations), STORAGE[storage],
                                    _ptr(out), _ptr(ws), ws.numel(), _stream(stream)))
+    return out
+
+
+def convert_field(t, storage: str, to: str, stream=None):
+    """tsf_convert_field: a new tensor holding t's values in storage `to`."""
+    torch = _torch()
+    out = torch.empty(t.shape, dtype=storage_dtype(to), device=t.device)
+    _check(load().tsf_convert_field(_ptr(t), STORAGE[storage], _ptr(out), STORAGE[to], t.numel(), _stream(stream)))
     return out
 
 
