@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
     __shared__ unsigned char sin_[kTdfWarps][kSeg];
-    __shared__ float dtb[kTdfWarps][32][33];               // [slot][sample], padded row
+    constexpr int kRows = 8;                               // voxel-radii per chunk of a batch
+    __shared__ float dtb[kTdfWarps][kRows][33];            // [row][sample], padded row
     const int XY = X * Y, margin = sample_margin(rmax);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
@@ -270,37 +271,53 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
     while (__any_sync(full, task >= 0)) {
         const bool eval = task >= 0 && inside(task) && radius <= rmax && nr < kMaxRadii;
         const unsigned M = __ballot_sync(full, eval);
-        for (unsigned m = M; m; m &= m - 1) {
-            const int v = __ffs(m) - 1;
-            const int tv = __shfl_sync(full, task, v);
-            const float rv = __shfl_sync(full, radius, v);
-            const float e2x = se[w][0][tv], e2y = se[w][1][tv], e2z = se[w][2][tv];
-            const float e3x = se[w][3][tv], e3y = se[w][4][tv], e3z = se[w][5][tv];
-            const float fx = (float)tx(tv), fy = (float)ty(tv), fz = (float)tz(tv);
-            float dt = 0.0f;
-            if (lane < ns) {
-                const float va0 = cj * e3x + sj * e2x;
-                const float va1 = cj * e3y + sj * e2y;
-                const float va2 = cj * e3z + sj * e2z;
-                float3 smp;
-                if (sin_[w][tv]) {
-                    if constexpr (PAIR)
-                        smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
-                    else
-                        smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
-                } else {
-                    smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+        // chunks of up to kRows voxel-radii: their samples go to the rows of
+        // dtb (row = rank of the owning slot in the chunk), then each owner sums
+        // its row in sample order (a small staging buffer leaves L1 its room)
+        float rs_own = 0.0f;
+        for (unsigned m = M; m;) {
+            unsigned rest = m;
+            for (int q = 0; q < kRows && rest; q++) rest &= rest - 1;
+            const unsigned chunk = m & ~rest;
+            m = rest;
+            int row = 0;
+            for (unsigned c = chunk; c; c &= c - 1, row++) {
+                const int v = __ffs(c) - 1;
+                const int tv = __shfl_sync(full, task, v);
+                const float rv = __shfl_sync(full, radius, v);
+                const float e2x = se[w][0][tv], e2y = se[w][1][tv], e2z = se[w][2][tv];
+                const float e3x = se[w][3][tv], e3y = se[w][4][tv], e3z = se[w][5][tv];
+                const float fx = (float)tx(tv), fy = (float)ty(tv), fz = (float)tz(tv);
+                float dt = 0.0f;
+                if (lane < ns) {
+                    const float va0 = cj * e3x + sj * e2x;
+                    const float va1 = cj * e3y + sj * e2y;
+                    const float va2 = cj * e3z + sj * e2z;
+                    float3 smp;
+                    if (sin_[w][tv]) {
+                        if constexpr (PAIR)
+                            smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                        else
+                            smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                    } else {
+                        smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                    }
+                    dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
                 }
-                dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                dtb[w][row][lane] = dt;
             }
-            dtb[w][v][lane] = dt;
+            __syncwarp();
+            if ((chunk >> lane) & 1u) {
+                const int myrow = __popc(chunk & ((1u << lane) - 1u));
+                float rs = 0.0f;
+                for (int j = 0; j < ns; j++) rs = rs + dtb[w][myrow][j];
+                rs_own = rs;
+            }
+            __syncwarp();
         }
-        __syncwarp();
         bool done = true;
         if (eval) {
-            float rs = 0.0f;
-            for (int j = 0; j < ns; j++) rs = rs + dtb[w][lane][j];
-            rs = rs / (float)ns;
+            const float rs = rs_own / (float)ns;
             if (rs > maxSum) {
                 maxSum = rs;
                 maxRadius = radius;
