@@ -45,9 +45,14 @@
 // rounding), which saves the separate half -> float conversions: the
 // conversion is exact, so each such instruction rounds like convert-then-op,
 // and (f0 - v)|f0|^2 added equals (v - f0)|f0|^2 subtracted bit for bit.
-// Packed f32x2 sums were tried and lost: they do not raise FP32 throughput
-// here, and the assembler fuses packed multiply-add pairs, which changes the
-// rounding.
+// snorm16 has no such shortcut: each stored value costs three instructions to
+// read exactly (snorm16_pair2), so that iteration is bound by instruction
+// issue, not bytes; there the voxel pairs (0, 1) and (2, 3) go through paired
+// FP32 instructions (.f32x2: two operations, each rounded like its scalar
+// twin), with every sum that follows a paired product done one at a time --
+// the assembler contracts a paired product feeding a paired sum into a paired
+// fma despite .rn, which would change the rounding.  (For the 16-bit float
+// formats, which are bound by bytes, paired sums gained nothing.)
 #include <mutex>
 
 #include "packed.cuh"
@@ -248,6 +253,24 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
             sqr[1] = sqadd16v<1>(fraw[2].u, sqadd16v<1>(fraw[1].u, sqadd16v<1>(fraw[0].u, -0.0f)));
             sqr[2] = sqadd16v<2>(fraw[2].u, sqadd16v<2>(fraw[1].u, sqadd16v<2>(fraw[0].u, -0.0f)));
             sqr[3] = sqadd16v<3>(fraw[2].u, sqadd16v<3>(fraw[1].u, sqadd16v<3>(fraw[0].u, -0.0f)));
+        } else if constexpr (ST == TSF_STORE_SNORM16) {
+            // voxel pairs (0, 1) and (2, 3): two FP32 operations per instruction
+            float2 f2[3][2];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                f2[c][0] = snorm16_pair2(fraw[c].u[0]);
+                f2[c][1] = snorm16_pair2(fraw[c].u[1]);
+                fv[c][0] = f2[c][0].x; fv[c][1] = f2[c][0].y; fv[c][2] = f2[c][1].x; fv[c][3] = f2[c][1].y;
+            }
+            // products paired, the sums after them one at a time: the
+            // assembler contracts a paired product that feeds a paired sum
+            // into a paired fma, although .rn asks it not to
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const float2 a = mul2(f2[0][h], f2[0][h]), b = mul2(f2[1][h], f2[1][h]), d = mul2(f2[2][h], f2[2][h]);
+                sqr[2 * h] = (a.x + b.x) + d.x;
+                sqr[2 * h + 1] = (a.y + b.y) + d.y;
+            }
         } else {
 #pragma unroll
             for (int c = 0; c < 3; c++) P::unpack(fraw[c], fv[c]);
@@ -309,6 +332,45 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     const float upd = mu * lap[i] + d[i] * sqr[i];
                     res[i] = cen[i] + upd;
                 }
+            } else if constexpr (ST == TSF_STORE_SNORM16) {
+                // voxel pairs (0, 1) and (2, 3) through paired FP32 operations;
+                // the x neighbours, which straddle the pairs, one at a time.
+                // Per voxel the operations and their order are the scalar path's.
+                const typename P::Raw zr = P::load_plain(vp + c * vstride), yr = P::load_plain(pc + BW),
+                                      mr = P::load_plain(pc - BW);
+                const float2 z01 = snorm16_pair2(zr.u[0]), z23 = snorm16_pair2(zr.u[1]);
+                const float2 y01 = snorm16_pair2(yr.u[0]), y23 = snorm16_pair2(yr.u[1]);
+                const float2 m01 = snorm16_pair2(mr.u[0]), m23 = snorm16_pair2(mr.u[1]);
+                const float xr = Store<ST>::load(pc[4]);
+                const float xl = Store<ST>::load(pc[-1]);
+                const float2 v01 = make_float2(cc[c][0], cc[c][1]), v23 = make_float2(cc[c][2], cc[c][3]);
+                const float2 c01 = make_float2(cm[c][0], cm[c][1]), c23 = make_float2(cm[c][2], cm[c][3]);
+                float2 l01 = mul2(v01, make_float2(-6.0f, -6.0f)), l23 = mul2(v23, make_float2(-6.0f, -6.0f));
+                l01.x = l01.x + cc[c][1];
+                l01.y = l01.y + cc[c][2];
+                l23.x = l23.x + cc[c][3];
+                l23.y = l23.y + xr;
+                l01.x = l01.x + xl;
+                l01.y = l01.y + cc[c][0];
+                l23.x = l23.x + cc[c][1];
+                l23.y = l23.y + cc[c][2];
+                l01 = add2(l01, y01);
+                l23 = add2(l23, y23);
+                l01 = add2(l01, m01);
+                l23 = add2(l23, m23);
+                l01 = add2(l01, rev ? c01 : z01);   // plane q+1
+                l23 = add2(l23, rev ? c23 : z23);
+                l01 = add2(l01, rev ? z01 : c01);   // plane q-1
+                l23 = add2(l23, rev ? z23 : c23);
+                const float2 mu2 = make_float2(mu, mu);
+                const float2 a01 = mul2(mu2, l01), a23 = mul2(mu2, l23);
+                const float2 b01 = mul2(sub2(v01, make_float2(fv[c][0], fv[c][1])), make_float2(sqr[0], sqr[1]));
+                const float2 b23 = mul2(sub2(v23, make_float2(fv[c][2], fv[c][3])), make_float2(sqr[2], sqr[3]));
+                const float2 u01 = make_float2(a01.x - b01.x, a01.y - b01.y);   // one at a time (see sqr)
+                const float2 u23 = make_float2(a23.x - b23.x, a23.y - b23.y);
+                const float2 r01 = add2(v01, u01), r23 = add2(v23, u23);
+                res[0] = r01.x; res[1] = r01.y; res[2] = r23.x; res[3] = r23.y;
+                zp[0] = z01.x; zp[1] = z01.y; zp[2] = z23.x; zp[3] = z23.y;
             } else {
                 float yp[4], ym[4];
                 P::unpack(P::load_plain(vp + c * vstride), zp);
@@ -522,8 +584,7 @@ int launch_gvf_zs(int st, const void *d_f0, const void *src, void *dst, int X, i
     // 16-bit float formats: a copy warp and per-slot release barriers (the
     // compute warps drift up to three planes apart instead of meeting at a
     // CTA barrier every plane).  FP32 and snorm16 measured faster with the
-    // CTA barrier (FP32 is at the copy bandwidth; snorm16's extra warp
-    // pushes its registers into spills).
+    // CTA barrier (FP32 is at the copy bandwidth).
     TSF_DISPATCH_STORAGE(st, ST, {
         r = launch_zs_typed<ST, ST == TSF_STORE_F16 || ST == TSF_STORE_BF16>(d_f0, src, dst, X, Y, Z, mu, s, rev);
     });

@@ -77,28 +77,41 @@ template <> struct Store<TSF_STORE_BF16> {
 // OpenCL CL_SNORM_INT16: write convert_short_sat_rte(v * 32767), read
 // max(-1, s / 32767) (kernels_no_3d_write.cl:9-21, OpenCL 1.1 section 8.3).
 //
-// The read divides without a division instruction: q0 = RN(s * r) with
-// r = RN(1 / 32767); the residual s - q0 * 32767 is exact in one fma, and
-// RN(q0 + residual * r) is the correctly rounded quotient -- Markstein's
-// correction step (P. W. Markstein, "Computation of elementary functions on
-// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  It is
-// checked against exact rational arithmetic for all 65,536 inputs
-// (tests/test_snorm16_read.py), so it gives the bits of s / 32767.
+// The read uses neither a division nor an integer -> float conversion (the
+// conversion unit runs at a fraction of the FMA rate and bounded the 16-bit
+// GVF iteration).  With t = s * 2^-15,
+//   s / 32767 = t / (1 - 2^-15) = t (1 + 2^-15 + 2^-30 + 2^-45 + ...),
+// and one fma gives RN(t + t * c) with c = 2^-15 + 2^-30 (an FP32 value, the
+// same bits as RN(1 / 32767)).  The exact fma operand s (2^30 + 2^15 + 1)
+// 2^-45 lies below s / 32767 by |s| / (2^45 (2^15 - 1)) <= 2^-45: less than
+// one unit of 2^-45, while every rounding boundary of the result is a
+// multiple of that unit and the operand, whose low bits repeat s, is never
+// one -- so both round to the same FP32 value.  t itself comes from the bit
+// pattern: flipping bit 15 of the stored 16 bits gives s + 2^15 (0..65535),
+// and placed as the low mantissa bits of 384.0f (0x43C00000, where one unit
+// of the mantissa is 2^-15) it makes the FP32 value 384 + (s + 2^15) 2^-15
+// = 385 + t; one subtraction (exact: same exponent) leaves t.  Checked
+// against exact rational arithmetic for all 65,536 inputs
+// (tests/test_snorm16_read.py).
+__device__ __forceinline__ float snorm16_from_bits(unsigned u16) {
+    const float t = __fsub_rn(__uint_as_float((u16 & 0xffffu) ^ 0x43C08000u), 385.0f);
+    return fmaxf(-1.0f, __fmaf_rn(t, __uint_as_float(0x38000100u), t));
+}
+
+// convert_short_sat_rte: PTX float -> integer conversions round as asked
+// (.rni: to nearest even), clamp to the destination range and turn NaN into
+// 0 -- the OpenCL rule, in one conversion.
+__device__ __forceinline__ unsigned short snorm16_bits(float v) {
+    const float f = __fmul_rn(v, 32767.0f);
+    unsigned short i;
+    asm("cvt.rni.s16.f32 %0, %1;" : "=h"(i) : "f"(f));
+    return i;
+}
+
 template <> struct Store<TSF_STORE_SNORM16> {
     using T = int16_t;
-    static __device__ __forceinline__ float load(T v) {
-        const float x = (float)v;
-        const float r = __uint_as_float(0x38000100u);      // RN(1 / 32767)
-        const float q0 = __fmul_rn(x, r);
-        const float e = __fmaf_rn(-q0, 32767.0f, x);
-        return fmaxf(-1.0f, __fmaf_rn(e, r, q0));
-    }
-    static __device__ __forceinline__ T store(float v) {
-        float f = __fmul_rn(v, 32767.0f);
-        int i = __float2int_rn(f);          // round to nearest even; NaN -> 0
-        i = max(-32768, min(32767, i));
-        return (int16_t)i;
-    }
+    static __device__ __forceinline__ float load(T v) { return snorm16_from_bits((unsigned)(uint16_t)v); }
+    static __device__ __forceinline__ T store(float v) { return (T)snorm16_bits(v); }
 };
 
 // Value after a store and a load (what the next reader sees).
