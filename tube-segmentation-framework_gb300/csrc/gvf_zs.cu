@@ -215,7 +215,10 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     // is loaded and converted once as a centre.  FP16 / BF16 read both
     // neighbour planes from the ring each plane: they enter the sums
     // unconverted.
-    float cm[3][4], cc[3][4];
+    // FP32 / snorm16: the lane's z column in three register sets that take
+    // the roles of planes q-1, q and q+1 in turn (the plane loop is unrolled
+    // three times, so no values move)
+    float A[3][4], B[3][4], Cz[3][4];
     int sm = 0, sc = 1, sp = 2, sf = 0;                   // slots: previous, current, next v plane; f plane
     uint32_t pp = 0, pf = 0;                              // phase parity of the waits on sp, sf
     ok &= mbar_wait(vbar + 0, 0, wait_limit);
@@ -223,19 +226,21 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
     if constexpr (!MIX) {
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring) + voff + c * vstride), cm[c]);
-            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), cc[c]);
+            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring) + voff + c * vstride), A[c]);
+            P::unpack(P::load_plain(reinterpret_cast<const T *>(vring + C::VSLOT) + voff + c * vstride), B[c]);
         }
     }
 
-    for (int k = 0; k < nf; k++) {
+    // One plane; cm, cc = the z column at planes q-1 and q, zn receives plane
+    // q+1 (q+1 and q-1 downwards).  False: stop (a wait ran out).
+    auto step = [&](int k, float (&cm)[3][4], float (&cc)[3][4], float (&zn)[3][4]) -> bool {
         const int q = rev ? qb - k : qa + k;
         ok &= mbar_wait(vbar + sp, pp, wait_limit);
         ok &= mbar_wait(fbar + sf, pf, wait_limit);
         if constexpr (WS) {
             if (__any_sync(0xffffffffu, !ok)) {
                 ok = false;
-                break;
+                return false;
             }
         }
         const T *vm = reinterpret_cast<const T *>(vring + sm * C::VSLOT) + voff;
@@ -280,7 +285,8 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
 #pragma unroll
         for (int c = 0; c < 3; c++) {
             const T *pc = vc + c * vstride;
-            float zp[4], res[4];
+            float res[4];
+            float *zp = zn[c];
             if constexpr (MIX) {
                 // The centre plane q is converted once; its y neighbours, the
                 // outer x neighbours, planes q -+ 1 and f0 enter the sums
@@ -402,13 +408,6 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                     if (dup_hi) P::store(oc + 2 * plane, res);
                 }
             }
-            if constexpr (!MIX) {
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    cm[c][i] = cc[c][i];
-                    cc[c][i] = zp[i];
-                }
-            }
         }
         o += rev ? -plane : plane;
         if constexpr (WS) {
@@ -425,11 +424,11 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
         pp ^= sp == 0;
         sf = sf + 1 == RF ? 0 : sf + 1;
         pf ^= sf == 0;
-        if constexpr (WS) continue;
+        if constexpr (WS) return true;
         // slots k % RV (v) and k % RF (f) are free once every thread is here
         if (__syncthreads_or(!ok)) {
             ok = false;
-            break;
+            return false;
         }
         if (tid == 0) {
             fence_proxy_async_smem();
@@ -445,6 +444,17 @@ __global__ void __launch_bounds__(ZsCfg<ST>::THREADS + 32 * WS, ZsCfg<ST>::MIN_C
                          rev ? qb - issued_f : qa + issued_f);
                 issued_f++;
             }
+        }
+        return true;
+    };
+    if constexpr (MIX) {
+        for (int k = 0; k < nf; k++)
+            if (!step(k, A, B, Cz)) break;
+    } else {
+        for (int k = 0; k < nf; k += 3) {
+            if (!step(k, A, B, Cz)) break;
+            if (k + 1 >= nf || !step(k + 1, B, Cz, A)) break;
+            if (k + 2 >= nf || !step(k + 2, Cz, A, B)) break;
         }
     }
     if (!ok && lane == 0) atomicOr(&g_gvf_zs_error, 1);

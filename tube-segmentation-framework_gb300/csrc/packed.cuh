@@ -6,64 +6,6 @@
 
 namespace tsf {
 
-// Two FP32 operations in one instruction (PTX .f32x2, sm_100 and later),
-// each rounded like its scalar counterpart.  The explicit .rn keeps the
-// assembler from contracting a product and a following sum into an fma.
-__device__ __forceinline__ float2 add2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
-    return d;
-}
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-    float2 d;
-    asm("{.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;}"
-        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return d;
-}
-
-// Both values of a 32-bit word of two stored snorm16 values (low half
-// first), read as snorm16_from_bits does with the two subtractions and the
-// two fmas paired.  The clamp moves to the integers: s = -32768 and
-// s = -32767 both read as -1, so one paired 16-bit max replaces the two FP32
-// max operations; two byte permutations place each half under 384.0f's
-// exponent.
-__device__ __forceinline__ float2 snorm16_pair2(unsigned w) {
-    const unsigned x = __vmaxs2(w, 0x80018001u) ^ 0x80008000u;   // s + 2^15 in each half
-    const float2 b = make_float2(__uint_as_float(__byte_perm(x, 0x43C00000u, 0x7610)),
-                                 __uint_as_float(__byte_perm(x, 0x43C00000u, 0x7632)));
-    const float2 t = sub2(b, make_float2(385.0f, 385.0f));
-    const float c = __uint_as_float(0x38000100u);
-    return fma2(t, make_float2(c, c), t);
-}
-
-// Two snorm16 values of a pair stored as one 32-bit word (low half first).
-__device__ __forceinline__ unsigned snorm16_store2(float2 v) {
-    const float2 f = mul2(v, make_float2(32767.0f, 32767.0f));
-    unsigned short lo, hi;
-    asm("cvt.rni.s16.f32 %0, %1;" : "=h"(lo) : "f"(f.x));
-    asm("cvt.rni.s16.f32 %0, %1;" : "=h"(hi) : "f"(f.y));
-    unsigned u;
-    asm("mov.b32 %0, {%1, %2};" : "=r"(u) : "h"(lo), "h"(hi));
-    return u;
-}
-
 // BYTES (8 or 16) bytes of stored components -- 4 or 8 voxels of a 16-bit
 // format, 2 or 4 of FP32 -- unpacked / packed two at a time with the paired
 // conversion intrinsics.

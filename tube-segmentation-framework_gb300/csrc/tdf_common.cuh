@@ -126,13 +126,19 @@ __device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY,
     return o;
 }
 
-// One stored 16-bit field4 texel (8 bytes) to floats, as Vec4Load does.
+// One stored 16-bit field4 texel (8 bytes) to floats, as Vec4Load does
+// (snorm16: x and y read together, snorm16_pair2, the same bits).
 template <int ST> __device__ __forceinline__ float4 unpack_texel(uint32_t lo, uint32_t hi) {
     using T = typename Store<ST>::T;
-    const uint2 raw = make_uint2(lo, hi);
-    T c[4];
-    memcpy(c, &raw, 8);
-    return make_float4(Store<ST>::load(c[0]), Store<ST>::load(c[1]), Store<ST>::load(c[2]), Store<ST>::load(c[3]));
+    if constexpr (ST == TSF_STORE_SNORM16) {
+        const float2 xy = snorm16_pair2(lo);
+        return make_float4(xy.x, xy.y, snorm16_from_bits(hi), snorm16_from_bits(hi >> 16));
+    } else {
+        const uint2 raw = make_uint2(lo, hi);
+        T c[4];
+        memcpy(c, &raw, 8);
+        return make_float4(Store<ST>::load(c[0]), Store<ST>::load(c[1]), Store<ST>::load(c[2]), Store<ST>::load(c[3]));
+    }
 }
 
 // sample_linear_in on the x-paired copy of a 16-bit field: entry i holds

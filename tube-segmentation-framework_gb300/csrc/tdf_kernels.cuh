@@ -348,8 +348,10 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
 }
 
 // Launches the sweep kernel of eigen mode EIG.  kernel: 0 = the faster of the
-// two brick kernels for the radius range (one sample per lane while every
-// radius is <= 3 -- the small-radius pass, whose circles stay in L1; else the
+// two brick kernels for the radius range and format (one sample per lane
+// while every radius is <= 3 -- the small-radius pass, whose circles stay in
+// L1 -- and for snorm16 at every radius, whose decode-heavy samples gain most
+// from full lanes (256^3, radii 2.5-7: 10.0 against 13.1 ms); else the
 // load-balanced sweeps), 1 = one voxel per lane (tdf_circle_kernel), 2 = one
 // sample per lane (tdf_lane_kernel), 3 = load-balanced sweeps
 // (tdf_queue_kernel); P: the x-paired 16-bit copy of the field (brick kernels)
@@ -358,7 +360,7 @@ template <int EIG>
 int launch_tdf_kernels(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
                        const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, int kernel,
                        const uint4 *P, int fast_ok) {
-    if (kernel == 0) kernel = rmax <= 3.0f ? 2 : 3;
+    if (kernel == 0) kernel = rmax <= 3.0f || st == TSF_STORE_SNORM16 ? 2 : 3;
     const bool queue = kernel == 3;
     const dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
     const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
