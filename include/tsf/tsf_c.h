@@ -336,8 +336,8 @@ typedef struct {
                       eigenvalues nearly coincide); eigenvector signs are
                       canonical (largest component positive), so T and R agree
                       with mode 0 to the circle's sampling noise, not bit for bit */
-    int kernel;    /* 0: default (one sample per lane when every radius is
-                      <= 3, else the load-balanced sweeps), 1: one voxel per
+    int kernel;    /* 0: default (one circle sample per lane for snorm16
+                      fields, else the load-balanced sweeps), 1: one voxel per
                       lane, 2: one circle sample per lane (a warp evaluates one
                       voxel-radius at a time), 3: load-balanced sweeps; all give
                       the same bits                                             */

@@ -41,7 +41,7 @@ __global__ void combine_kernel(const void *__restrict__ Ts, const float *__restr
     }
 }
 
-// tdf_mode: 0 = default (per radius range, see launch_tdf_kernels), 1 = one
+// tdf_mode: 0 = default (per storage format, see launch_tdf_kernels), 1 = one
 // voxel per lane, 2 = one sample per lane, 3 = load-balanced sweeps.
 // ws / ws_bytes: room for the x-paired copy of a 16-bit field (tdf_workspace_size);
 // without it, or for FP32 storage, the samples read the field itself.

@@ -70,6 +70,66 @@ __device__ __forceinline__ void hessian(const void *F, int X, int Y, int Z, int 
     H[2][0] = Fzx; H[2][1] = Fzy; H[2][2] = Fzz;
 }
 
+// The sample direction a = c e3 + s e2 (per component two products and a
+// sum, kernels.cl:1136), the x and y products paired.
+__device__ __forceinline__ float3 circle_dir(float c, float s, float e2x, float e2y, float e2z, float e3x, float e3y,
+                                             float e3z) {
+    const float2 p = mul2(make_float2(c, c), make_float2(e3x, e3y));
+    const float2 q = mul2(make_float2(s, s), make_float2(e2x, e2y));
+    return make_float3(p.x + q.x, p.y + q.y, c * e3z + s * e2z);
+}
+
+// The sample position x + r a (kernels.cl:1137), the x and y products
+// paired.
+__device__ __forceinline__ float3 circle_point(float fx, float fy, float fz, float r, float3 a) {
+    const float2 p = mul2(make_float2(r, r), make_float2(a.x, a.y));
+    return make_float3(fx + p.x, fy + p.y, fz + r * a.z);
+}
+
+// The sample's radial term ((-g.x) a.x + (-g.y) a.y) + (-g.z) a.z
+// (kernels.cl:1138-1139), the first two products paired.
+__device__ __forceinline__ float radial_term(float3 g, float3 a) {
+    const float2 p = mul2(make_float2(-g.x, -g.y), make_float2(a.x, a.y));
+    return (p.x + p.y) + (-g.z) * a.z;
+}
+
+// The eight trilinear weights w000, w100, w010, w110, w001, w101, w011, w111
+// with the specification's products ((1-a)(1-b))(1-c) ..., the products of
+// the two x-neighbour weights paired (.f32x2: each rounded as alone).
+__device__ __forceinline__ void tri_weights(float a, float b, float c, float w[8]) {
+    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
+    const float2 p0 = mul2(make_float2(ia, a), make_float2(ib, ib));
+    const float2 p1 = mul2(make_float2(ia, a), make_float2(b, b));
+    const float2 q0 = mul2(p0, make_float2(ic, ic)), q1 = mul2(p1, make_float2(ic, ic));
+    const float2 q2 = mul2(p0, make_float2(c, c)), q3 = mul2(p1, make_float2(c, c));
+    w[0] = q0.x; w[1] = q0.y; w[2] = q1.x; w[3] = q1.y;
+    w[4] = q2.x; w[5] = q2.y; w[6] = q3.x; w[7] = q3.y;
+}
+
+// Sum over the eight corners of w_i * t_i for the x, y and z channels, in
+// corner order: the x and y products of a corner paired, every sum one at a
+// time (the assembler contracts a paired product feeding a paired sum).
+__device__ __forceinline__ float3 tri_sum(const float w[8], const float4 t[8]) {
+    float2 pxy[8];
+    float pz[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        pxy[i] = mul2(make_float2(w[i], w[i]), make_float2(t[i].x, t[i].y));
+        pz[i] = w[i] * t[i].z;
+    }
+    float3 o;
+    o.x = pxy[0].x;
+    o.y = pxy[0].y;
+    o.z = pz[0];
+#pragma unroll
+    for (int i = 1; i < 8; i++) {
+        o.x = o.x + pxy[i].x;
+        o.y = o.y + pxy[i].y;
+        o.z = o.z + pz[i];
+    }
+    return o;
+}
+
 // OpenCL linear filter, unnormalised coordinates, clamp to edge (OpenCL 1.1
 // section 8.2); weights summed in the specification's order.
 template <int ST>
@@ -80,23 +140,16 @@ __device__ __forceinline__ float3 sample_linear(const void *F, int X, int Y, int
     int i0 = (int)fu, j0 = (int)fv, k0 = (int)fw;
     const int i1 = clampi(i0 + 1, X), j1 = clampi(j0 + 1, Y), k1 = clampi(k0 + 1, Z);
     i0 = clampi(i0, X); j0 = clampi(j0, Y); k0 = clampi(k0, Z);
-    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
-    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
-    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    float wt[8];
+    tri_weights(a, b, c, wt);
     const int64_t r00 = lin(0, j0, k0, X, Y), r10 = lin(0, j1, k0, X, Y);
     const int64_t r01 = lin(0, j0, k1, X, Y), r11 = lin(0, j1, k1, X, Y);
     const float4 t000 = Vec4Load<ST>::load(F, r00 + i0), t100 = Vec4Load<ST>::load(F, r00 + i1);
     const float4 t010 = Vec4Load<ST>::load(F, r10 + i0), t110 = Vec4Load<ST>::load(F, r10 + i1);
     const float4 t001 = Vec4Load<ST>::load(F, r01 + i0), t101 = Vec4Load<ST>::load(F, r01 + i1);
     const float4 t011 = Vec4Load<ST>::load(F, r11 + i0), t111 = Vec4Load<ST>::load(F, r11 + i1);
-    float3 o;
-    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
-    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
-    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
-    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
-    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
-    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
-    return o;
+    const float4 tt[8] = {t000, t100, t010, t110, t001, t101, t011, t111};
+    return tri_sum(wt, tt);
 }
 
 // sample_linear for a point whose 8 corners are all inside the volume (the
@@ -109,21 +162,14 @@ __device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY,
     const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
     const float a = uu - fu, b = vv - fv, c = ww - fw;
     const int base = (int)fu + X * (int)fv + XY * (int)fw;
-    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
-    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
-    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    float wt[8];
+    tri_weights(a, b, c, wt);
     const float4 t000 = Vec4Load<ST>::load(F, base), t100 = Vec4Load<ST>::load(F, base + 1);
     const float4 t010 = Vec4Load<ST>::load(F, base + X), t110 = Vec4Load<ST>::load(F, base + X + 1);
     const float4 t001 = Vec4Load<ST>::load(F, base + XY), t101 = Vec4Load<ST>::load(F, base + XY + 1);
     const float4 t011 = Vec4Load<ST>::load(F, base + XY + X), t111 = Vec4Load<ST>::load(F, base + XY + X + 1);
-    float3 o;
-    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
-    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
-    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
-    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
-    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
-    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
-    return o;
+    const float4 tt[8] = {t000, t100, t010, t110, t001, t101, t011, t111};
+    return tri_sum(wt, tt);
 }
 
 // One stored 16-bit field4 texel (8 bytes) to floats, as Vec4Load does
@@ -151,23 +197,16 @@ __device__ __forceinline__ float3 sample_linear_pair_in(const uint4 *P, int X, i
     const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
     const float a = uu - fu, b = vv - fv, c = ww - fw;
     const int base = (int)fu + X * (int)fv + XY * (int)fw;
-    const float ia = 1.0f - a, ib = 1.0f - b, ic = 1.0f - c;
-    const float w000 = (ia * ib) * ic, w100 = (a * ib) * ic, w010 = (ia * b) * ic, w110 = (a * b) * ic;
-    const float w001 = (ia * ib) * c, w101 = (a * ib) * c, w011 = (ia * b) * c, w111 = (a * b) * c;
+    float wt[8];
+    tri_weights(a, b, c, wt);
     const uint4 p00 = __ldg(P + base), p10 = __ldg(P + base + X);
     const uint4 p01 = __ldg(P + base + XY), p11 = __ldg(P + base + XY + X);
     const float4 t000 = unpack_texel<ST>(p00.x, p00.y), t100 = unpack_texel<ST>(p00.z, p00.w);
     const float4 t010 = unpack_texel<ST>(p10.x, p10.y), t110 = unpack_texel<ST>(p10.z, p10.w);
     const float4 t001 = unpack_texel<ST>(p01.x, p01.y), t101 = unpack_texel<ST>(p01.z, p01.w);
     const float4 t011 = unpack_texel<ST>(p11.x, p11.y), t111 = unpack_texel<ST>(p11.z, p11.w);
-    float3 o;
-    o.x = w000 * t000.x; o.x = o.x + w100 * t100.x; o.x = o.x + w010 * t010.x; o.x = o.x + w110 * t110.x;
-    o.x = o.x + w001 * t001.x; o.x = o.x + w101 * t101.x; o.x = o.x + w011 * t011.x; o.x = o.x + w111 * t111.x;
-    o.y = w000 * t000.y; o.y = o.y + w100 * t100.y; o.y = o.y + w010 * t010.y; o.y = o.y + w110 * t110.y;
-    o.y = o.y + w001 * t001.y; o.y = o.y + w101 * t101.y; o.y = o.y + w011 * t011.y; o.y = o.y + w111 * t111.y;
-    o.z = w000 * t000.z; o.z = o.z + w100 * t100.z; o.z = o.z + w010 * t010.z; o.z = o.z + w110 * t110.z;
-    o.z = o.z + w001 * t001.z; o.z = o.z + w101 * t101.z; o.z = o.z + w011 * t011.z; o.z = o.z + w111 * t111.z;
-    return o;
+    const float4 tt[8] = {t000, t100, t010, t110, t001, t101, t011, t111};
+    return tri_sum(wt, tt);
 }
 
 // Margin m such that every trilinear corner of a sample at distance <= r

@@ -56,13 +56,10 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
         float rs = 0.0f;
 #pragma unroll 4
         for (int j = 0; j < tab.n; j++) {
-            const float c = tab.c[j], s = tab.s[j];
-            const float va0 = c * e3x + s * e2x;
-            const float va1 = c * e3y + s * e2y;
-            const float va2 = c * e3z + s * e2z;
-            const float3 smp = sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
-            const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
-            rs = rs + dt;
+            const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
+            const float3 u = circle_point(fx, fy, fz, radius, va);
+            const float3 smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
+            rs = rs + radial_term(smp, va);
         }
         rs = rs / (float)tab.n;
         if (rs > maxSum) {
@@ -153,31 +150,22 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                 if (sin_[w][task]) {
 #pragma unroll 4
                     for (int j = 0; j < tab.n; j++) {
-                        const float c = tab.c[j], s = tab.s[j];
-                        const float va0 = c * e3x + s * e2x;
-                        const float va1 = c * e3y + s * e2y;
-                        const float va2 = c * e3z + s * e2z;
+                        const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
+                        const float3 u = circle_point(fx, fy, fz, radius, va);
                         float3 smp;
                         if constexpr (PAIR)
-                            smp = sample_linear_pair_in<ST>(P, X, XY, fx + radius * va0, fy + radius * va1,
-                                                            fz + radius * va2);
+                            smp = sample_linear_pair_in<ST>(P, X, XY, u.x, u.y, u.z);
                         else
-                            smp = sample_linear_in<ST>(F, X, XY, fx + radius * va0, fy + radius * va1,
-                                                       fz + radius * va2);
-                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
-                        rs = rs + dt;
+                            smp = sample_linear_in<ST>(F, X, XY, u.x, u.y, u.z);
+                        rs = rs + radial_term(smp, va);
                     }
                 } else {
 #pragma unroll 4
                     for (int j = 0; j < tab.n; j++) {
-                        const float c = tab.c[j], s = tab.s[j];
-                        const float va0 = c * e3x + s * e2x;
-                        const float va1 = c * e3y + s * e2y;
-                        const float va2 = c * e3z + s * e2z;
-                        const float3 smp =
-                            sample_linear<ST>(F, X, Y, Z, fx + radius * va0, fy + radius * va1, fz + radius * va2);
-                        const float dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
-                        rs = rs + dt;
+                        const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
+                        const float3 u = circle_point(fx, fy, fz, radius, va);
+                        const float3 smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
+                        rs = rs + radial_term(smp, va);
                     }
                 }
                 rs = rs / (float)tab.n;
@@ -290,19 +278,18 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
                 const float fx = (float)tx(tv), fy = (float)ty(tv), fz = (float)tz(tv);
                 float dt = 0.0f;
                 if (lane < ns) {
-                    const float va0 = cj * e3x + sj * e2x;
-                    const float va1 = cj * e3y + sj * e2y;
-                    const float va2 = cj * e3z + sj * e2z;
+                    const float3 va = circle_dir(cj, sj, e2x, e2y, e2z, e3x, e3y, e3z);
+                    const float3 u = circle_point(fx, fy, fz, rv, va);
                     float3 smp;
                     if (sin_[w][tv]) {
                         if constexpr (PAIR)
-                            smp = sample_linear_pair_in<ST>(P, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                            smp = sample_linear_pair_in<ST>(P, X, XY, u.x, u.y, u.z);
                         else
-                            smp = sample_linear_in<ST>(F, X, XY, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                            smp = sample_linear_in<ST>(F, X, XY, u.x, u.y, u.z);
                     } else {
-                        smp = sample_linear<ST>(F, X, Y, Z, fx + rv * va0, fy + rv * va1, fz + rv * va2);
+                        smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
                     }
-                    dt = ((-smp.x) * va0 + (-smp.y) * va1) + (-smp.z) * va2;
+                    dt = radial_term(smp, va);
                 }
                 dtb[w][row][lane] = dt;
             }
@@ -348,11 +335,11 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
 }
 
 // Launches the sweep kernel of eigen mode EIG.  kernel: 0 = the faster of the
-// two brick kernels for the radius range and format (one sample per lane
-// while every radius is <= 3 -- the small-radius pass, whose circles stay in
-// L1 -- and for snorm16 at every radius, whose decode-heavy samples gain most
-// from full lanes (256^3, radii 2.5-7: 10.0 against 13.1 ms); else the
-// load-balanced sweeps), 1 = one voxel per lane (tdf_circle_kernel), 2 = one
+// two brick kernels for the format (one sample per lane for snorm16, whose
+// decode-heavy samples gain most from full lanes -- 256^3, radii 1-3: 7.9
+// against 10.2 ms; the load-balanced sweeps for the others -- f16, radii
+// 1-3: 7.2 against 7.3 ms, radii 2.5-7: 9.5 against 10.0 ms), 1 = one voxel
+// per lane (tdf_circle_kernel), 2 = one
 // sample per lane (tdf_lane_kernel), 3 = load-balanced sweeps
 // (tdf_queue_kernel); P: the x-paired 16-bit copy of the field (brick kernels)
 // or null.  All give the same bits.
@@ -360,7 +347,7 @@ template <int EIG>
 int launch_tdf_kernels(const void *d_field4, int X, int Y, int Z, int st, float rmin, float rmax, float rstep,
                        const CircleTable &tab, void *d_T, int unorm, float *d_R, cudaStream_t s, int kernel,
                        const uint4 *P, int fast_ok) {
-    if (kernel == 0) kernel = rmax <= 3.0f || st == TSF_STORE_SNORM16 ? 2 : 3;
+    if (kernel == 0) kernel = st == TSF_STORE_SNORM16 ? 2 : 3;
     const bool queue = kernel == 3;
     const dim3 b(32, 4, 2), g((X + 31) / 32, (Y + 3) / 4, (Z + 1) / 2);
     const bool norm = !(rmax < 4.0f);   // kernels.cl:1083-1091
