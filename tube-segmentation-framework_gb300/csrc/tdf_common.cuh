@@ -215,6 +215,21 @@ __device__ __forceinline__ float3 sample_linear_pair_in(const uint4 *P, int X, i
 // (then |a| <= 1.0012; corners lie within ceil(|a| r + 0.5) of the voxel).
 __host__ __device__ __forceinline__ int sample_margin(float rmax) { return (int)ceilf(rmax * 1.002f + 0.5f) + 2; }
 
+// Room for the unclamped sampler around a voxel: its distance to the nearest
+// face (capped at 255), or 0 when the eigenvectors are not finite, unit and
+// orthogonal up to rounding.  The samples at radius r may take
+// sample_linear_in when sample_margin(r) <= this value (the margin box of
+// samples_inside, checked per radius instead of for rmax).
+__device__ __forceinline__ unsigned char sample_room(int x, int y, int z, int X, int Y, int Z, const float e2[3],
+                                                     const float e3[3]) {
+    const float n2 = (e2[0] * e2[0] + e2[1] * e2[1]) + e2[2] * e2[2];
+    const float n3 = (e3[0] * e3[0] + e3[1] * e3[1]) + e3[2] * e3[2];
+    const float d = (e2[0] * e3[0] + e2[1] * e3[1]) + e2[2] * e3[2];
+    if (!(n2 <= 1.0001f && n3 <= 1.0001f && d >= -1e-3f && d <= 1e-3f)) return 0;
+    const int m = min(min(min(x, y), z), min(min(X - 1 - x, Y - 1 - y), Z - 1 - z));
+    return (unsigned char)max(0, min(m, 255));
+}
+
 // Whether a voxel's samples can take sample_linear_in: the margin box lies in
 // the volume and the eigenvectors are finite, unit and orthogonal up to
 // rounding (false for NaN / inf, which then take the clamped sampler).

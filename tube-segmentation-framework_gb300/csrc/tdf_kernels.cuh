@@ -108,8 +108,8 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                                                                     const uint4 *__restrict__ P) {
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
-    __shared__ unsigned char sin_[kTdfWarps][kSeg];      // samples stay inside: unclamped sampler
-    const int XY = X * Y, margin = sample_margin(rmax);
+    __shared__ unsigned char room[kTdfWarps][kSeg];      // sample_room: unclamped sampler while the margin fits
+    const int XY = X * Y;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     // brick of this CTA, block of this warp: task t -> (t & 7, (t >> 3) & 3, t >> 5)
     const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
         se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
         se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
         const float e2[3] = {V[0][1], V[1][1], V[2][1]}, e3[3] = {V[0][2], V[1][2], V[2][2]};
-        sin_[w][t] = fast_ok && samples_inside(tx(t), ty(t), tz(t), X, Y, Z, margin, e2, e3);
+        room[w][t] = fast_ok ? sample_room(tx(t), ty(t), tz(t), X, Y, Z, e2, e3) : 0;
     }
     __syncwarp();
     // phase 2: radius sweeps as tasks
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
             const float fx = (float)tx(task), fy = (float)ty(task), fz = (float)tz(task);
             if (radius <= rmax && nr < kMaxRadii) {
                 float rs = 0.0f;
-                if (sin_[w][task]) {
+                if (sample_margin(radius) <= room[w][task]) {
 #pragma unroll 4
                     for (int j = 0; j < tab.n; j++) {
                         const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
@@ -222,10 +222,10 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
                                                                    const uint4 *__restrict__ P) {
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
-    __shared__ unsigned char sin_[kTdfWarps][kSeg];
+    __shared__ unsigned char room[kTdfWarps][kSeg];
     constexpr int kRows = 8;                               // voxel-radii per chunk of a batch
     __shared__ float dtb[kTdfWarps][kRows][33];            // [row][sample], padded row
-    const int XY = X * Y, margin = sample_margin(rmax);
+    const int XY = X * Y;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int nbx = (X + 7) >> 3, nby = (Y + 7) >> 3;
     const int b = blockIdx.x;
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
         se[w][0][t] = V[0][1]; se[w][1][t] = V[1][1]; se[w][2][t] = V[2][1];
         se[w][3][t] = V[0][2]; se[w][4][t] = V[1][2]; se[w][5][t] = V[2][2];
         const float e2[3] = {V[0][1], V[1][1], V[2][1]}, e3[3] = {V[0][2], V[1][2], V[2][2]};
-        sin_[w][t] = fast_ok && samples_inside(tx(t), ty(t), tz(t), X, Y, Z, margin, e2, e3);
+        room[w][t] = fast_ok ? sample_room(tx(t), ty(t), tz(t), X, Y, Z, e2, e3) : 0;
     }
     __syncwarp();
     // phase 2: batches of voxel-radii, one sample per lane
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
                     const float3 va = circle_dir(cj, sj, e2x, e2y, e2z, e3x, e3y, e3z);
                     const float3 u = circle_point(fx, fy, fz, rv, va);
                     float3 smp;
-                    if (sin_[w][tv]) {
+                    if (sample_margin(rv) <= room[w][tv]) {
                         if constexpr (PAIR)
                             smp = sample_linear_pair_in<ST>(P, X, XY, u.x, u.y, u.z);
                         else
