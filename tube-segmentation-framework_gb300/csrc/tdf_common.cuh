@@ -209,6 +209,34 @@ __device__ __forceinline__ float3 sample_linear_pair_in(const uint4 *P, int X, i
     return tri_sum(wt, tt);
 }
 
+// sample_linear (clamp to edge) on the x-paired copy: entry (i, j, k) holds
+// texels i and min(i + 1, X - 1) of row (j, k), so with i = clamp(i0) one
+// 16-byte load gives both x corners of a corner row -- except for i0 < 0, where
+// both corners clamp to column 0 and the entry's first texel serves twice.
+// The same texels, weights and sums, so the same bits as sample_linear
+// (X * Y * Z < 2^31 for the 32-bit offsets, as for the paired copy itself).
+template <int ST>
+__device__ __forceinline__ float3 sample_linear_pair_clamped(const uint4 *P, int X, int Y, int Z, float u, float v,
+                                                             float w) {
+    const float uu = u - 0.5f, vv = v - 0.5f, ww = w - 0.5f;
+    const float fu = floorf(uu), fv = floorf(vv), fw = floorf(ww);
+    const float a = uu - fu, b = vv - fv, c = ww - fw;
+    const int i0 = (int)fu, j0 = (int)fv, k0 = (int)fw;
+    const int ic = clampi(i0, X);
+    const int j1 = clampi(j0 + 1, Y), k1 = clampi(k0 + 1, Z), jc = clampi(j0, Y), kc = clampi(k0, Z);
+    const bool xlo = i0 < 0;
+    float wt[8];
+    tri_weights(a, b, c, wt);
+    const uint4 p00 = __ldg(P + ic + X * (jc + Y * kc)), p10 = __ldg(P + ic + X * (j1 + Y * kc));
+    const uint4 p01 = __ldg(P + ic + X * (jc + Y * k1)), p11 = __ldg(P + ic + X * (j1 + Y * k1));
+    const float4 t000 = unpack_texel<ST>(p00.x, p00.y), t010 = unpack_texel<ST>(p10.x, p10.y);
+    const float4 t001 = unpack_texel<ST>(p01.x, p01.y), t011 = unpack_texel<ST>(p11.x, p11.y);
+    const float4 t100 = xlo ? t000 : unpack_texel<ST>(p00.z, p00.w), t110 = xlo ? t010 : unpack_texel<ST>(p10.z, p10.w);
+    const float4 t101 = xlo ? t001 : unpack_texel<ST>(p01.z, p01.w), t111 = xlo ? t011 : unpack_texel<ST>(p11.z, p11.w);
+    const float4 tt[8] = {t000, t100, t010, t110, t001, t101, t011, t111};
+    return tri_sum(wt, tt);
+}
+
 // Margin m such that every trilinear corner of a sample at distance <= r
 // from a voxel lies within m - 1 voxels of it, for sample directions
 // a = cos e3 + sin e2 with |e2|, |e3| <= 1.00005 and |e2 . e3| <= 1e-3

@@ -164,7 +164,11 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                     for (int j = 0; j < tab.n; j++) {
                         const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
                         const float3 u = circle_point(fx, fy, fz, radius, va);
-                        const float3 smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
+                        float3 smp;
+                        if constexpr (PAIR)
+                            smp = sample_linear_pair_clamped<ST>(P, X, Y, Z, u.x, u.y, u.z);
+                        else
+                            smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
                         rs = rs + radial_term(smp, va);
                     }
                 }
@@ -287,7 +291,10 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_lane_kernel(const void *__
                         else
                             smp = sample_linear_in<ST>(F, X, XY, u.x, u.y, u.z);
                     } else {
-                        smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
+                        if constexpr (PAIR)
+                            smp = sample_linear_pair_clamped<ST>(P, X, Y, Z, u.x, u.y, u.z);
+                        else
+                            smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
                     }
                     dt = radial_term(smp, va);
                 }
