@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
     int nr = 0;
     for (float radius = rmin; radius <= rmax && nr < kMaxRadii; radius = radius + rstep, nr++) {
         float rs = 0.0f;
-#pragma unroll 4
+#pragma unroll 2
         for (int j = 0; j < tab.n; j++) {
             const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
             const float3 u = circle_point(fx, fy, fz, radius, va);
@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
             if (radius <= rmax && nr < kMaxRadii) {
                 float rs = 0.0f;
                 if (sample_margin(radius) <= room[w][task]) {
-#pragma unroll 4
+#pragma unroll 2
                     for (int j = 0; j < tab.n; j++) {
                         const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
                         const float3 u = circle_point(fx, fy, fz, radius, va);
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *_
                         rs = rs + radial_term(smp, va);
                     }
                 } else {
-#pragma unroll 4
+#pragma unroll 2
                     for (int j = 0; j < tab.n; j++) {
                         const float3 va = circle_dir(tab.c[j], tab.s[j], e2x, e2y, e2z, e3x, e3y, e3z);
                         const float3 u = circle_point(fx, fy, fz, radius, va);
