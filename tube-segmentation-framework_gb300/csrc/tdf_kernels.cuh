@@ -101,7 +101,7 @@ constexpr int kTdfWarps = 4;
 // PAIR: interior samples read the x-paired copy P of a 16-bit field (one
 // 16-byte load per corner row, sample_linear_pair_in) instead of F.
 template <int ST, bool NORM, bool UNORM, bool PAIR, int EIG>
-__global__ void __launch_bounds__(32 * kTdfWarps) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
+__global__ void __launch_bounds__(32 * kTdfWarps, 6) tdf_queue_kernel(const void *__restrict__ F, int X, int Y, int Z,
                                                                     float rmin, float rmax, float rstep,
                                                                     const CircleTable tab, void *T,
                                                                     float *__restrict__ Rout, int fast_ok,
