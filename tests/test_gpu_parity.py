@@ -155,7 +155,7 @@ def _to_device_field4(torch, field4, storage):
 @pytest.mark.parametrize("unorm", [False, True])
 @pytest.mark.parametrize("mode", [0, 1, 2, 3])
 def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm, mode):
-    """Every TDF kernel (0: the default per radius range, 1: one voxel per
+    """Every TDF kernel (0: the default per storage format, 1: one voxel per
     lane, 2: one sample per lane, 3: load-balanced sweeps over 8^3 bricks).  X = 26 and X = 150 end in ragged bricks; both shapes hold voxels
     whose samples all lie inside (the unclamped sampler) and voxels near the
     faces (the clamped one)."""
@@ -174,12 +174,15 @@ def test_tdf_bitexact(torch_dev, tsf, oracle, synth, storage, rng_, unorm, mode)
 
 
 @pytest.mark.parametrize("storage", STORAGES)
-@pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5)])
+@pytest.mark.parametrize("rng_", [(1.0, 3.0, 0.5), (2.5, 7.0, 0.5), (2.5, 9.0, 0.5)])
 def test_tdf_paired_texels(torch_dev, tsf, oracle, synth, storage, rng_):
-    """tsf_tdf_circle_ws: for 16-bit storage the interior samples read the
-    x-paired copy of the field (four 16-byte loads per sample); T and R are the
-    oracle's bit for bit, and a workspace that is too small or misaligned
-    falls back to the plain path with the same result."""
+    """tsf_tdf_circle_ws: for 16-bit storage the samples read the x-paired
+    copy of the field (four 16-byte loads per sample) -- unclamped while the
+    current radius's margin fits inside the volume, clamped to the edge near
+    the faces (radii up to 9 reach past every face of a 40 x 44 x 49 volume
+    from most voxels); T and R are the oracle's bit for bit, and a workspace
+    that is too small or misaligned falls back to the plain path with the same
+    result."""
     torch = torch_dev
     shape = (40, 44, 49)
     field4, _ = _field(oracle, synth, shape, 8, storage)
