@@ -777,6 +777,8 @@ def run_stage(args):
         runs["small_paired"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws)
         runs["small_paired_queue"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
                                                           samples=32, mode=3)
+        runs["small_paired_sample_per_lane"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
+                                                                    samples=32, mode=2)
         runs["small_paired_closed_eigen"] = lambda: T.tdf_circle(fsm, P["rmin"], 3.0, 0.5, storage=st, ws=ws,
                                                                  eigen=1)
     for run in runs.values():
@@ -1214,9 +1216,12 @@ def run_polish(args):
     for K - k iterations, then k in FP32 (the iterate converted, f0 in FP32),
     the finished field in FP32 and the small-radius pass on the FP32 field of
     the raw volume; both TDF passes, combine and the candidate stage as in the
-    benchmark step.  Reports, per variant, the vertex list against the FP64
-    oracle run of the same method and the step time (CUDA events, median of 3
-    after a warm-up) next to the plain 16-bit and FP32 paths."""
+    benchmark step.  Variants store the polished field in snorm16 or in the
+    16-bit format again for the finish and the large-radius pass, and the
+    small-radius field in snorm16, FP32 or the 16-bit format.  Reports, per
+    variant, the vertex list against the FP64 oracle run of the same method and
+    the step time (CUDA events, median of 3 after a warm-up) next to the plain
+    16-bit and FP32 paths."""
     import torch
     import oracle as O
     import synthetic
@@ -1257,7 +1262,12 @@ def run_polish(args):
     st = args.storage
     variants = {"%s" % st: (st, 0, st, st), "f32": ("f32", 0, "f32", "f32"),
                 "%s+%d_f32_polish" % (st, k): (st, k, "f32", "f32"),
-                "%s+%d_f32_polish_%s_small" % (st, k, st): (st, k, "f32", st)}
+                "%s+%d_f32_polish_%s_small" % (st, k, st): (st, k, "f32", st),
+                # the polished field stored in snorm16 (finer than f16 near unit magnitude) for the finish and
+                # the large-radius pass, the small-radius field in snorm16 or FP32; or back in the 16-bit format
+                "%s+%d_f32_polish_snorm16_tdf" % (st, k): (st, k, "snorm16", "snorm16"),
+                "%s+%d_f32_polish_snorm16_large_f32_small" % (st, k): (st, k, "snorm16", "f32"),
+                "%s+%d_f32_polish_%s_large_f32_small" % (st, k, st): (st, k, st, "f32")}
     s64 = set(map(tuple, V64.tolist()))
     out = {"size": n, "iterations": K, "mu": args.mu, "fp64_vertices": int(len(V64)), "oracle_s": round(t_oracle, 1),
            "note": "step = blur, vector fields, GVF, finish, both TDF passes, combine, candidates; CUDA events, "
