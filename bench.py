@@ -569,6 +569,8 @@ def run_api_timing(args, vol, repeats=3):
     med = float(np.median(r["run_ms"]))
     return {"ms_per_volume": round(med, 2), "volumes_per_s": round(1e3 / med, 3),
             "gvox_iter_s": round(n ** 3 * args.iters / (med * 1e-3) / 1e9, 2), "runs_ms": r["run_ms"],
+            "run_call_ms": round(float(np.median(r["run_call_ms"])), 2),
+            "getters_ms": round(float(np.median(r["getters_ms"])), 2),
             "vertices": r["vertices"], "segmented_voxels": r["segmented_voxels"],
             "note": "run() through the C++ API, host clock, median of %d after one warm-up; includes reading the "
                     "%d MB .raw file" % (repeats, n ** 3 * 4 // 1000000)}

@@ -414,7 +414,8 @@ int tsf_rasterize_trees(const int *d_vertices, const int *d_edges, int n_edges, 
  * each edge by its mean (createCenterlineVoxels, :287-321; radius X*Y*Z
  * float, updated).  The final graph goes to out_vertices (x, y, z) and
  * out_edges; both counts are returned, and TSF_ERR_CAPACITY when either
- * exceeds `capacity` (call again with more).  TSF_ERR_COUNT_RANGE when no
+ * exceeds `capacity` (radius and centerlines are then left unchanged: call
+ * again with more).  TSF_ERR_COUNT_RANGE when no
  * vertex survives ("Centerline graph size is 0").
  * tsf_remove_loops: removeLoops alone.
  * tsf_write_centerline_vtk: writeToVtkFile (inputOutput.cpp:48-63). */

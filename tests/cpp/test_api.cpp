@@ -223,7 +223,7 @@ static int bench_mode(int argc, char **argv) {
     args.push_back(argv[2]);
     for (int i = 4; i < argc; i++) args.push_back(argv[i]);
     const int repeats = std::atoi(argv[3]);
-    std::vector<double> ms;
+    std::vector<double> ms, run_ms, get_ms;
     size_t vertices = 0, segmented = 0;
     for (int k = -1; k < repeats; k++) {
         paramList parameters = getParameters((int)args.size(), args.data());
@@ -235,13 +235,18 @@ static int bench_mode(int argc, char **argv) {
             std::cerr << "SIPLException: " << e.what() << std::endl;
             return 3;
         }
+        const auto tr = std::chrono::steady_clock::now();
         const SIPL::int3 s = *o->getSize();
         const size_t n = (size_t)s.x * s.y * s.z;
         const float *tdf = o->getTDF();
         const char *cl = o->hasCenterlineVoxels() ? o->getCenterlineVoxels() : nullptr;
         const char *seg = o->hasSegmentation() ? o->getSegmentation() : nullptr;
         const auto t1 = std::chrono::steady_clock::now();
-        if (k >= 0) ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+        if (k >= 0) {
+            ms.push_back(std::chrono::duration<double, std::milli>(t1 - t0).count());
+            run_ms.push_back(std::chrono::duration<double, std::milli>(tr - t0).count());
+            get_ms.push_back(std::chrono::duration<double, std::milli>(t1 - tr).count());
+        }
         vertices = o->getCenterpoints().size();
         segmented = 0;
         if (seg)
@@ -250,9 +255,16 @@ static int bench_mode(int argc, char **argv) {
         (void)cl;
         delete o;
     }
-    std::cout << "{\"run_ms\": [";
-    for (size_t i = 0; i < ms.size(); i++) std::cout << (i ? ", " : "") << ms[i];
-    std::cout << "], \"vertices\": " << vertices << ", \"segmented_voxels\": " << segmented << "}" << std::endl;
+    auto list = [](const char *key, const std::vector<double> &v) {
+        std::cout << "\"" << key << "\": [";
+        for (size_t i = 0; i < v.size(); i++) std::cout << (i ? ", " : "") << v[i];
+        std::cout << "], ";
+    };
+    std::cout << "{";
+    list("run_ms", ms);
+    list("run_call_ms", run_ms);
+    list("getters_ms", get_ms);
+    std::cout << "\"vertices\": " << vertices << ", \"segmented_voxels\": " << segmented << "}" << std::endl;
     return 0;
 }
 

@@ -123,6 +123,36 @@ def test_graph_stage_filters_trees_and_rasterises(tsf):
     assert np.array_equal(rad[~on], radius[~on])
 
 
+def test_short_capacity_writes_nothing(tsf):
+    """TSF_ERR_CAPACITY returns both counts and leaves radius and centerlines
+    as they were, so a second call with enough room gives the full result."""
+    import ctypes as C
+    L = tsf.load()
+    v = np.array([[2 + 3 * i, 6, 6] for i in range(6)], np.int32)
+    e = np.array([[i, i + 1] for i in range(5)], np.int32)
+    labels, sizes = np.zeros(6, np.int32), np.array([6, 0, 0, 0, 0, 0], np.int32)
+    radius = np.random.default_rng(2).random((12, 12, 20)).astype(np.float32)
+    Z, Y, X = radius.shape
+
+    def call(cap, rad, cl):
+        ov, oe = np.zeros((max(cap, 1), 3), np.int32), np.zeros((max(cap, 1), 2), np.int32)
+        nv, ne = C.c_int(0), C.c_int(0)
+        code = L.tsf_centerline_graph(tsf._np_ptr(v), 6, tsf._np_ptr(e), 5, tsf._np_ptr(labels),
+                                      tsf._np_ptr(sizes), 1, 0, X, Y, Z, tsf._np_ptr(rad), tsf._np_ptr(cl),
+                                      tsf._np_ptr(ov), tsf._np_ptr(oe), cap, C.byref(nv), C.byref(ne))
+        return code, nv.value, ne.value
+
+    rad, cl = radius.copy(), np.zeros(radius.shape, np.int8)
+    code, nv, ne = call(3, rad, cl)
+    assert code == 6 and (nv, ne) == (6, 5)                        # TSF_ERR_CAPACITY with the counts
+    assert np.array_equal(rad, radius) and not cl.any()            # nothing written
+    code, nv, ne = call(8, rad, cl)
+    assert code == 0 and (nv, ne) == (6, 5)
+    ref_cl, ref_rad = _raster(v, e, radius)
+    assert np.array_equal(cl, ref_cl)
+    assert cl.any() and not np.array_equal(rad, radius)
+
+
 def test_edge_splitting_for_the_vtk_file(tsf):
     v = np.array([[2, 4, 4], [14, 4, 4], [20, 4, 4]])
     e = np.array([[0, 1], [1, 2]])

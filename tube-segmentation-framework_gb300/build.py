@@ -30,7 +30,7 @@ NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-fmad=false", "--expt-relaxed-constexpr",
                      "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", INCLUDE]
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", INCLUDE]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-I", INCLUDE]
 
 CU_SOURCES = ["capi.cu", "vector_field.cu", "gvf.cu", "gvf_zs.cu", "gvf_tb2.cu", "gvf_one.cu", "tdf.cu", "tdf_closed.cu", "candidates.cu", "fmg.cu", "noalloc.cu", "input.cu", "gvf_adjoint.cu", "gvf_adjoint_zs.cu", "tdf_adjoint.cu", "link.cu", "segment.cu", "crop.cu", "tdf_spline.cu", "residual.cu", "convert.cu"]
 
@@ -62,6 +62,8 @@ def _deps():
     hdr = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     hdr += [os.path.join(INCLUDE, "tsf", f) for f in os.listdir(os.path.join(INCLUDE, "tsf"))
             if f.endswith((".h", ".hpp"))]
+    if os.path.isdir(HOST):
+        hdr += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".h", ".hpp"))]
     return hdr
 
 
@@ -98,7 +100,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     cudadir = _cuda_lib_dir()
     if jobs or not os.path.exists(LIB):
         _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs +
-             ["-cudart", "shared", "-L", cudadir, "-Xlinker", "-rpath," + cudadir])
+             ["-cudart", "shared", "-lpthread", "-L", cudadir, "-Xlinker", "-rpath," + cudadir])
     # C++ test driver of the drop-in API (tests/cpp/test_api.cpp)
     src = os.path.join(ROOT, "tests", "cpp", "test_api.cpp")
     if os.path.exists(src) and _newer([src, LIB] + deps, API_TESTS):

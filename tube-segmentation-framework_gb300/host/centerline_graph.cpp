@@ -86,13 +86,15 @@ public:
             throw std::runtime_error("Centerline graph size is 0! Can't continue. Maybe lower min-tree-length?");
 
         // minimum spanning forest
+        // (the next root is the last unvisited node; nodes never become
+        // unvisited, so that index only moves down)
         std::unordered_set<int64_t> visited;
         std::vector<int> tree = spanning_tree(graph[0], visited);
+        int last = (int)graph.size() - 1;
         while (tree.size() < graph.size()) {
-            int root = -1;
-            for (int i = 0; i < (int)graph.size(); i++)
-                if (!visited.count(key(nodes_[graph[i]].pos))) root = i;
-            const std::vector<int> more = spanning_tree(graph[root], visited);
+            while (last >= 0 && visited.count(key(nodes_[graph[last]].pos))) last--;
+            if (last < 0) break;   // nodes sharing a position count as one
+            const std::vector<int> more = spanning_tree(graph[last], visited);
             tree.insert(tree.end(), more.begin(), more.end());
         }
 
@@ -301,6 +303,11 @@ extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const i
     } catch (const std::exception &) {
         return TSF_ERR_COUNT_RANGE;
     }
+    // the counts first: when they exceed the capacity, radius and centerlines
+    // are left as they were, so the caller can call again with more
+    *n_out_vertices = (int)v.size();
+    *n_out_edges = (int)e.size();
+    if ((int)v.size() > capacity || (int)e.size() > capacity) return TSF_ERR_CAPACITY;
     tsf_host::centerline_voxels(v, e, radius, centerlines, V3{X, Y, Z});
     return copy_out(v, e, out_vertices, out_edges, capacity, n_out_vertices, n_out_edges);
 }

@@ -2,9 +2,14 @@
 // inputOutput.hpp / inputOutput.cpp).
 #include <cuda_runtime_api.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <fstream>
+#include <memory>
+#include <thread>
+#include <vector>
 
+#include "first_touch.hpp"
 #include "tsf/SIPL/Exceptions.hpp"
 #include "tsf/inputOutput.hpp"
 
@@ -75,10 +80,25 @@ float *TSFOutput::getTDF() {
     const int64_t n = voxels(size);
     TDF = new float[n];
     if (TDFis16bit) {
-        std::vector<uint16_t> tmp((size_t)n);
-        copy_to_host(tmp.data(), d_TDF, sizeof(uint16_t) * (size_t)n);
-        for (int64_t i = 0; i < n; i++) TDF[i] = (float)tmp[(size_t)i] / 65535.0f;
+        // the unorm16 TDF read as v / 65535, as the reference's getter does
+        // (inputOutput.cpp:164), on up to 16 host threads
+        std::unique_ptr<uint16_t[]> tmp(new uint16_t[(size_t)n]);
+        tsf_host::parallel_fill(tmp.get(), 0, sizeof(uint16_t) * (size_t)n);
+        copy_to_host(tmp.get(), d_TDF, sizeof(uint16_t) * (size_t)n);
+        const uint16_t *src = tmp.get();
+        float *dst = TDF;
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int64_t nt = std::max<int64_t>(1, std::min<int64_t>({hw ? (int64_t)hw : 1, 16, n >> 20}));
+        auto work = [=](int64_t t) {
+            const int64_t i0 = n * t / nt, i1 = n * (t + 1) / nt;
+            for (int64_t i = i0; i < i1; i++) dst[i] = (float)src[i] / 65535.0f;
+        };
+        std::vector<std::thread> pool;
+        for (int64_t t = 1; t < nt; t++) pool.emplace_back(work, t);
+        work(0);
+        for (auto &th : pool) th.join();
     } else {
+        tsf_host::parallel_fill(TDF, 0, sizeof(float) * (size_t)n);
         copy_to_host(TDF, d_TDF, sizeof(float) * (size_t)n);
     }
     hostHasTDF = true;
@@ -90,6 +110,7 @@ char *TSFOutput::getSegmentation() {
     if (!deviceHasSegmentation)
         throw SIPL::SIPLException("Trying to fetch non existing data from TSFOutput", __LINE__, __FILE__);
     segmentation = new char[voxels(size)];
+    tsf_host::parallel_fill(segmentation, 0, (size_t)voxels(size));
     copy_to_host(segmentation, d_segmentation, (size_t)voxels(size));
     hostHasSegmentation = true;
     return segmentation;
@@ -100,6 +121,7 @@ char *TSFOutput::getCenterlineVoxels() {
     if (!deviceHasCenterlineVoxels)
         throw SIPL::SIPLException("Trying to fetch non existing data from TSFOutput", __LINE__, __FILE__);
     centerlineVoxels = new char[voxels(size)];
+    tsf_host::parallel_fill(centerlineVoxels, 0, (size_t)voxels(size));
     copy_to_host(centerlineVoxels, d_centerline, (size_t)voxels(size));
     hostHasCenterlineVoxels = true;
     return centerlineVoxels;

@@ -26,15 +26,22 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iostream>
 #include <limits>
+#include <memory>
 #include <sstream>
+#include <thread>
 #include <vector>
 
+#include <fcntl.h>
+#include <unistd.h>
+
+#include "first_touch.hpp"
 #include "tsf/tsf_c.h"
 #include "tsf/tube-segmentation.hpp"
 
@@ -86,6 +93,52 @@ struct Stream {
     }
 };
 
+// The "timing" parameter (parameters:21): each stage's duration printed as
+// "RUNTIME <stage>: <ms> ms", as the reference does with a marker before and
+// after the stage and a finish of its queue at the second one
+// (tube-segmentation.cpp:297-298,446-452 and the other stages).  Here the
+// markers are events on the run's stream, so a stage's time includes host
+// work between its launches; host-only stages use the host clock.  Off: no
+// events, no synchronisation.
+class StageTimer {
+  public:
+    StageTimer(bool on, cudaStream_t s) : on_(on), s_(s) {
+        if (!on_) return;
+        check_cuda(cudaEventCreate(&e0_), "cudaEventCreate");
+        check_cuda(cudaEventCreate(&e1_), "cudaEventCreate");
+    }
+    ~StageTimer() {
+        if (e0_) cudaEventDestroy(e0_);
+        if (e1_) cudaEventDestroy(e1_);
+    }
+    bool on() const { return on_; }
+    void start() {
+        if (on_) check_cuda(cudaEventRecord(e0_, s_), "cudaEventRecord");
+    }
+    void stop(const char *stage) {
+        if (!on_) return;
+        check_cuda(cudaEventRecord(e1_, s_), "cudaEventRecord");
+        check_cuda(cudaEventSynchronize(e1_), "cudaEventSynchronize");
+        float ms = 0.0f;
+        check_cuda(cudaEventElapsedTime(&ms, e0_, e1_), "cudaEventElapsedTime");
+        std::cout << "RUNTIME " << stage << ": " << ms << " ms" << std::endl;
+    }
+    void host_start() { h0_ = std::chrono::steady_clock::now(); }
+    void host_stop(const char *stage) {
+        if (!on_) return;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0_).count();
+        std::cout << "RUNTIME " << stage << ": " << ms << " ms" << std::endl;
+    }
+    StageTimer(const StageTimer &) = delete;
+    StageTimer &operator=(const StageTimer &) = delete;
+
+  private:
+    bool on_;
+    cudaStream_t s_;
+    cudaEvent_t e0_ = nullptr, e1_ = nullptr;
+    std::chrono::steady_clock::time_point h0_;
+};
+
 std::string trim(const std::string &v) {
     size_t b = 0, e = v.size();
     while (b < e && std::isspace((unsigned char)v[b])) b++;
@@ -104,24 +157,66 @@ bool header_value(const std::string &line, const char *key, std::string &value) 
 }
 
 struct HostVolume {
-    std::vector<char> data;
+    std::unique_ptr<char[]> data;   // the raw file, not initialised before the read
+    size_t bytes = 0;
     int type = -1;           // TSF_TYPE_*
     int elem = 0;
     SIPL::int3 size;
     SIPL::float3 spacing{1, 1, 1};
 };
 
-template <typename T> void limits_of(const std::vector<char> &raw, float &lo, float &hi) {
-    const T *p = reinterpret_cast<const T *>(raw.data());
-    const size_t n = raw.size() / sizeof(T);
-    // reference getMinimum/getMaximum start from numeric_limits<T>::max()/min()
+// Minimum and maximum of p[0, n) as the reference's getMinimum/getMaximum
+// fold them (tube-segmentation.cpp:1380-1396): from numeric_limits<T>::max()
+// and ::min(), std::min / std::max per element.
+template <typename T> struct Limits {
     T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::min();
-    for (size_t i = 0; i < n; i++) {
-        mn = std::min(mn, p[i]);
-        mx = std::max(mx, p[i]);
+    void fold(const T *p, size_t n) {
+        for (size_t i = 0; i < n; i++) {
+            mn = std::min(mn, p[i]);
+            mx = std::max(mx, p[i]);
+        }
     }
-    lo = (float)mn;
-    hi = (float)mx;
+};
+
+// Reads `bytes` of the file at fd into dst with up to 16 threads, each one
+// contiguous slice (pread), and folds each slice into its own Limits<T> while
+// it is still in cache when `limits` is set.  The slices' results are folded
+// in file order: std::min / std::max keep the first of equal values and never
+// take a NaN, so the result equals the sequential fold over the whole file.
+template <typename T>
+bool read_slices(int fd, char *dst, size_t bytes, bool limits, float &lo, float &hi) {
+    const size_t min_slice = (size_t)4 << 20;
+    unsigned hw = std::thread::hardware_concurrency();
+    size_t nt = std::min<size_t>(hw ? hw : 1, 16);
+    nt = std::max<size_t>(1, std::min(nt, bytes / min_slice));
+    const size_t elems = bytes / sizeof(T), per = (elems + nt - 1) / nt;
+    std::vector<Limits<T>> part(nt);
+    std::vector<char> ok(nt, 0);
+    auto work = [&](size_t t) {
+        const size_t e0 = std::min(elems, t * per), e1 = std::min(elems, e0 + per);
+        size_t off = e0 * sizeof(T);
+        const size_t end = t + 1 == nt ? bytes : e1 * sizeof(T);
+        while (off < end) {
+            const ssize_t r = pread(fd, dst + off, end - off, (off_t)off);
+            if (r <= 0) return;
+            off += (size_t)r;
+        }
+        if (limits) part[t].fold(reinterpret_cast<const T *>(dst) + e0, e1 - e0);
+        ok[t] = 1;
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nt; t++) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+    Limits<T> all;
+    for (size_t t = 0; t < nt; t++) {
+        if (!ok[t]) return false;
+        all.mn = std::min(all.mn, part[t].mn);
+        all.mx = std::max(all.mx, part[t].mx);
+    }
+    lo = (float)all.mn;
+    hi = (float)all.mx;
+    return true;
 }
 
 HostVolume read_volume(const std::string &filename, paramList &parameters, float &minimum, float &maximum) {
@@ -157,23 +252,25 @@ HostVolume read_volume(const std::string &filename, paramList &parameters, float
     else raise("unsupported data type " + typeName);
 
     const size_t bytes = (size_t)v.size.x * v.size.y * v.size.z * v.elem;
-    v.data.resize(bytes);
-    FILE *f = std::fopen(rawName.c_str(), "rb");
-    if (!f) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
-    const size_t got = std::fread(v.data.data(), 1, bytes, f);
-    std::fclose(f);
-    if (got != bytes) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
-
-    // getLimits (tube-segmentation.cpp:1380-1396)
-    float lo = 0.0f, hi = 1.0f;
-    switch (v.type) {
-    case TSF_TYPE_INT16: limits_of<int16_t>(v.data, lo, hi); break;
-    case TSF_TYPE_UINT16: limits_of<uint16_t>(v.data, lo, hi); break;
-    case TSF_TYPE_INT8: limits_of<int8_t>(v.data, lo, hi); break;
-    case TSF_TYPE_UINT8: limits_of<uint8_t>(v.data, lo, hi); break;
-    default: limits_of<float>(v.data, lo, hi); break;
-    }
+    v.data.reset(new char[bytes ? bytes : 1]);
+    v.bytes = bytes;
+    const int fd = open(rawName.c_str(), O_RDONLY);
+    if (fd < 0) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
+    // getLimits (tube-segmentation.cpp:1380-1396); its result is used only
+    // where "minimum" or "maximum" is off
     const std::string pmin = getParamStr(parameters, "minimum"), pmax = getParamStr(parameters, "maximum");
+    const bool limits = pmin == "off" || pmax == "off";
+    float lo = 0.0f, hi = 1.0f;
+    bool got = false;
+    switch (v.type) {
+    case TSF_TYPE_INT16: got = read_slices<int16_t>(fd, v.data.get(), bytes, limits, lo, hi); break;
+    case TSF_TYPE_UINT16: got = read_slices<uint16_t>(fd, v.data.get(), bytes, limits, lo, hi); break;
+    case TSF_TYPE_INT8: got = read_slices<int8_t>(fd, v.data.get(), bytes, limits, lo, hi); break;
+    case TSF_TYPE_UINT8: got = read_slices<uint8_t>(fd, v.data.get(), bytes, limits, lo, hi); break;
+    default: got = read_slices<float>(fd, v.data.get(), bytes, limits, lo, hi); break;
+    }
+    close(fd);
+    if (!got) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
     minimum = pmin != "off" ? (float)std::atof(pmin.c_str()) : lo;
     maximum = pmax != "off" ? (float)std::atof(pmax.c_str()) : hi;
     if (v.type == TSF_TYPE_UINT16) {
@@ -244,7 +341,7 @@ struct FieldResult {
 
 // runCircleFittingMethod, tube-segmentation.cpp:212-939
 void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z, int st, bool tdf16,
-                           cudaStream_t s, FieldResult &out) {
+                           cudaStream_t s, StageTimer &tm, FieldResult &out) {
     const float rMin = getParam(P, "radius-min"), rMax = getParam(P, "radius-max"), rStep = getParam(P, "radius-step");
     const float fmax = getParam(P, "fmax");
     const int vsign = getParamStr(P, "mode") == "black" ? -1 : 1;
@@ -254,6 +351,7 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
 
     DevBuf Ts, Rs, f4small;
     if (rMin < 2.5f) {
+        tm.start();
         DevBuf blurred;
         const float *src = d_vol;
         if (smallBlur > 0) {
@@ -263,12 +361,15 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         }
         f4small.alloc(n * 4 * es);
         check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4small.p, S), "vector field");
+        tm.stop("of Create vector field");
+        tm.start();
         Ts.alloc(n * ts);
         Rs.alloc(n * 4);
         const size_t twb = tsf_tdf_workspace_size(X, Y, Z, st);
         DevBuf tws(twb);
         check(tsf_tdf_circle_ws(f4small.p, X, Y, Z, st, rMin, 3.0f, 0.5f, Ts.p, tdf16, Rs.as<float>(), tws.p, twb, S),
               "TDF");
+        tm.stop("of TDF small");
         if (rMax < 2.5f) {
             out.T.p = Ts.release();
             out.R.p = Rs.release();
@@ -278,6 +379,7 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         f4small.alloc(0);   // free early, as the reference does
     }
 
+    tm.start();
     DevBuf blurred;
     const float *src = d_vol;
     if (largeBlur > 0) {
@@ -285,27 +387,37 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
         check(tsf_blur(d_vol, blurred.as<float>(), X, Y, Z, largeBlur, S), "blur");
         src = blurred.as<float>();
     }
+    tm.stop("blurring");
     out.field.alloc(n * 4 * es);
     const int iterations = (int)getParam(P, "gvf-iterations");
     const float mu = getParam(P, "gvf-mu");
     if (getParamBool(P, "use-fmg-gvf")) {
+        tm.start();
         DevBuf f4in(n * 4 * es);
         check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, nullptr, f4in.p, S), "vector field");
         blurred.alloc(0);
+        tm.stop("Create vector field");
+        tm.start();
         DevBuf ws(tsf_gvf_fmg_workspace_size(X, Y, Z, st));
         check(tsf_gvf_fmg(f4in.p, out.field.p, X, Y, Z, mu, iterations, st, ws.p,
                           tsf_gvf_fmg_workspace_size(X, Y, Z, st), S), "multigrid GVF");
+        tm.stop("of GVF");
     } else {
+        tm.start();
         DevBuf f0(n * 3 * es), v(n * 3 * es);
         check(tsf_vector_field(src, X, Y, Z, fmax, vsign, st, f0.p, nullptr, S), "vector field");
         blurred.alloc(0);
+        tm.stop("Create vector field");
+        tm.start();
         check_cuda(cudaMemcpyAsync(v.p, f0.p, n * 3 * es, cudaMemcpyDeviceToDevice, s), "copy");
         const size_t wsb = tsf_gvf_workspace_size(X, Y, Z, st);
         DevBuf ws(wsb);
         // the reference's ping-pong returns the even part of the iteration count
         check(tsf_gvf(f0.p, v.p, X, Y, Z, mu, iterations - iterations % 2, st, ws.p, wsb, S), "GVF");
         check(tsf_gvf_finish(v.p, out.field.p, X, Y, Z, st, S), "GVF finish");
+        tm.stop("of GVF");
     }
+    tm.start();
     out.T.alloc(n * ts);
     out.R.alloc(n * 4);
     if (getParamBool(P, "use-spline-tdf"))
@@ -318,8 +430,12 @@ void circle_fitting_method(paramList &P, const float *d_vol, int X, int Y, int Z
                                 out.R.as<float>(), tws.p, twb, S),
               "TDF");
     }
-    if (rMin < 2.5f)
+    tm.stop("of TDF large");
+    if (rMin < 2.5f) {
+        tm.start();
         check(tsf_tdf_combine(Ts.p, Rs.as<float>(), out.T.p, out.R.as<float>(), (int64_t)n, tdf16, S), "combine");
+        tm.stop("of combine");
+    }
 }
 
 }  // namespace
@@ -330,13 +446,19 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
     const std::string method = getParamStr(parameters, "centerline-method");
     if (method != "gpu") raise("centerline-method " + method + " is not part of this library (use gpu)");
 
-    float minimum = 0.0f, maximum = 1.0f;
-    HostVolume hv = read_volume(filename, parameters, minimum, maximum);
-    std::cout << "Dataset of size " << hv.size.x << " " << hv.size.y << " " << hv.size.z << " loaded" << std::endl;
     Stream stream;
     void *S = (void *)stream.s;
-    DevBuf raw(hv.data.size());
-    check_cuda(cudaMemcpyAsync(raw.p, hv.data.data(), hv.data.size(), cudaMemcpyHostToDevice, stream.s), "upload");
+    StageTimer tm(getParamBool(parameters, "timing"), stream.s);
+    float minimum = 0.0f, maximum = 1.0f;
+    tm.host_start();
+    HostVolume hv = read_volume(filename, parameters, minimum, maximum);
+    tm.host_stop("of reading the dataset");
+    tm.start();
+    DevBuf raw(hv.bytes);
+    check_cuda(cudaMemcpyAsync(raw.p, hv.data.get(), hv.bytes, cudaMemcpyHostToDevice, stream.s), "upload");
+    std::cout << "Dataset of size " << hv.size.x << " " << hv.size.y << " " << hv.size.z << " loaded" << std::endl;
+    tm.stop("of data transfer to device");
+    tm.start();
     int box[6];
     const SIPL::int3 shift = input_box(parameters, hv, raw.p, stream.s, box);
     const int X = box[3], Y = box[4], Z = box[5];
@@ -346,7 +468,8 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         check(tsf_crop_copy(raw.p, hv.type, hv.size.x, hv.size.y, hv.size.z, box, cropped.p, S), "cropping");
         raw.swap(cropped);
     }
-    std::vector<char>().swap(hv.data);   // the upload has been staged; the host copy is not needed again
+    tm.stop("of cropping");
+    hv.data.reset();   // the upload has been staged; the host copy is not needed again
     const bool tdf16 = getParamBool(parameters, "16bit-vectors");
     const int st = storage_from_parameters(parameters);
 
@@ -354,12 +477,14 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
     output->setSpacing(hv.spacing);
     output->setShiftVector(shift);
     try {
+        tm.start();
         DevBuf vol(n * 4);
         check(tsf_to_float(raw.p, hv.type, (int64_t)n, minimum, maximum, vol.as<float>(), S), "toFloat");
         raw.alloc(0);
+        tm.stop("of to float conversion");
 
         FieldResult fr;
-        circle_fitting_method(parameters, vol.as<float>(), X, Y, Z, st, tdf16, stream.s, fr);
+        circle_fitting_method(parameters, vol.as<float>(), X, Y, Z, st, tdf16, stream.s, tm, fr);
         vol.alloc(0);
         check_cuda(cudaStreamSynchronize(stream.s), "TDF");
         void *d_T = fr.T.p;                      // the output owns it from here on
@@ -367,6 +492,7 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         if (getParamBool(parameters, "tdf-only")) return output;
 
         // runNewCenterlineAlg, front half (parallelCenterlineExtraction.cpp:667-899)
+        tm.start();
         const size_t wsb = tsf_candidates_workspace_size(X, Y, Z);
         const int64_t max_vertices = 16384;
         DevBuf ws(wsb), cp(n), verts(sizeof(int32_t) * 3 * max_vertices);
@@ -397,8 +523,10 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         std::vector<SIPL::int3> vlist((size_t)nv);
         for (int64_t i = 0; i < nv; i++) vlist[(size_t)i] = SIPL::int3(hv3[3 * i], hv3[3 * i + 1], hv3[3 * i + 2]);
         output->setCenterpoints(vlist);
+        tm.stop("centerpoint extraction");
 
         // runNewCenterlineAlg, back half (parallelCenterlineExtraction.cpp:911-1332)
+        tm.start();
         const int nvi = (int)nv;
         const size_t lwb = tsf_link_workspace_size(nvi);
         DevBuf lws(lwb), dedges(sizeof(int32_t) * 4 * (size_t)nvi), dlabels(sizeof(int32_t) * (size_t)nvi),
@@ -411,6 +539,8 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         std::cout << "number of edges detected " << ne << std::endl;
         if (lcode == TSF_ERR_COUNT_RANGE) throw SIPL::SIPLException("No edges were found", __LINE__, __FILE__);
         check(lcode, "linking");
+        tm.stop("linking");
+        tm.start();
         const int min_tree = (int)getParam(parameters, "min-tree-length");
         const std::string vtk = getParamStr(parameters, "centerline-vtk-file");
         const bool segment = !getParamBool(parameters, "no-segmentation");
@@ -419,46 +549,46 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         if (vtk != "off" || getParamBool(parameters, "loop-removal")) {
             // host loop removal and rasterisation (parallelCenterlineExtraction.cpp:1168-1247)
             std::vector<int32_t> he(2 * (size_t)ne), hl((size_t)nvi), hs((size_t)nvi);
-            std::vector<float> radius(n);
+            std::unique_ptr<float[]> radius(new float[n]);   // filled by the copy below
+            tsf_host::parallel_fill(radius.get(), 0, n * sizeof(float));
             check_cuda(cudaMemcpyAsync(he.data(), dedges.p, he.size() * 4, cudaMemcpyDeviceToHost, stream.s), "edges");
             check_cuda(cudaMemcpyAsync(hl.data(), dlabels.p, hl.size() * 4, cudaMemcpyDeviceToHost, stream.s), "labels");
             check_cuda(cudaMemcpyAsync(hs.data(), dsizes.p, hs.size() * 4, cudaMemcpyDeviceToHost, stream.s), "sizes");
-            check_cuda(cudaMemcpyAsync(radius.data(), fr.R.p, n * 4, cudaMemcpyDeviceToHost, stream.s), "radius");
+            check_cuda(cudaMemcpyAsync(radius.get(), fr.R.p, n * 4, cudaMemcpyDeviceToHost, stream.s), "radius");
             check_cuda(cudaStreamSynchronize(stream.s), "graph download");
             const int split = vtk != "off" ? (int)getParam(parameters, "max-edge-distance") : 0;
-            char *centerlines = new char[n]();
+            std::unique_ptr<char[]> centerlines(new char[n]);
+            tsf_host::parallel_fill(centerlines.get(), 0, n);
             int cap = 4 * (nvi + ne) + 1024, nov = 0, noe = 0, gcode;
             std::vector<int32_t> ov, oe;
-            std::vector<float> rad;
+            StageTimer graph_tm(tm.on(), stream.s);
+            graph_tm.host_start();
             for (;;) {
                 ov.assign(3 * (size_t)cap, 0);
                 oe.assign(2 * (size_t)cap, 0);
-                std::memset(centerlines, 0, n);
-                rad = radius;
+                // a short capacity leaves radius and centerlines untouched
                 gcode = tsf_centerline_graph(hv3.data(), nvi, he.data(), ne, hl.data(), hs.data(), min_tree, split,
-                                             X, Y, Z, rad.data(), reinterpret_cast<int8_t *>(centerlines), ov.data(),
-                                             oe.data(), cap, &nov, &noe);
+                                             X, Y, Z, radius.get(), reinterpret_cast<int8_t *>(centerlines.get()),
+                                             ov.data(), oe.data(), cap, &nov, &noe);
                 if (gcode != TSF_ERR_CAPACITY) break;
                 cap = 2 * std::max(nov, noe);
             }
-            if (gcode == TSF_ERR_COUNT_RANGE) {
-                delete[] centerlines;
+            graph_tm.host_stop("of loop removal and centerline voxels (host)");
+            if (gcode == TSF_ERR_COUNT_RANGE)
                 throw SIPL::SIPLException("Centerline graph size is 0! Can't continue. Maybe lower min-tree-length?",
                                           __LINE__, __FILE__);
-            }
-            if (gcode != TSF_OK) {
-                delete[] centerlines;
-                check(gcode, "centerline graph");
-            }
-            output->setCenterlineVoxels(centerlines);
+            check(gcode, "centerline graph");
             if (segment) {
                 // the reference writes the centerlines and the averaged radius back to its images
-                // (parallelCenterlineExtraction.cpp:1235-1249)
+                // (parallelCenterlineExtraction.cpp:1235-1249); pageable sources are staged before the
+                // copies return
                 dcl.alloc(n);
-                check_cuda(cudaMemcpyAsync(dcl.p, centerlines, n, cudaMemcpyHostToDevice, stream.s), "centerlines");
-                check_cuda(cudaMemcpyAsync(fr.R.p, rad.data(), n * 4, cudaMemcpyHostToDevice, stream.s), "radius");
+                check_cuda(cudaMemcpyAsync(dcl.p, centerlines.get(), n, cudaMemcpyHostToDevice, stream.s),
+                           "centerlines");
+                check_cuda(cudaMemcpyAsync(fr.R.p, radius.get(), n * 4, cudaMemcpyHostToDevice, stream.s), "radius");
                 d_cl = dcl.as<int8_t>();
             }
+            output->setCenterlineVoxels(centerlines.release());
             if (vtk != "off" && tsf_write_centerline_vtk(vtk.c_str(), ov.data(), nov, oe.data(), noe) != TSF_OK)
                 throw SIPL::IOException(vtk.c_str(), __LINE__, __FILE__);
         } else {
@@ -472,8 +602,10 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
             d_cl = cl.as<int8_t>();        // owned by the output from here on
             output->setDeviceCenterlineVoxels(static_cast<int8_t *>(cl.release()));
         }
+        tm.stop("of removing small trees");
         // runInverseGradientSegmentation / runSphereSegmentation (tube-segmentation.cpp:967-976)
         if (segment) {
+            tm.start();
             DevBuf seg(n);
             if (!getParamBool(parameters, "sphere-segmentation")) {
                 const size_t swb = tsf_segment_workspace_size(X, Y, Z);
@@ -488,6 +620,7 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
             }
             check_cuda(cudaStreamSynchronize(stream.s), "segmentation");
             output->setDeviceSegmentation(static_cast<int8_t *>(seg.release()));
+            tm.stop("of segmentation");
         }
         if (getParamStr(parameters, "storage-dir") != "off")
             writeDataToDisk(output, getParamStr(parameters, "storage-dir"), getParamStr(parameters, "storage-name"));
