@@ -215,7 +215,7 @@ def test_run_threshold_cropping(api_tests, oracle, synth, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", ["tdf-only", "centerpoints-only", "no-loop-removal", "default", "vtk",
-                                  "sphere", "no-segmentation"])
+                                  "sphere", "no-segmentation", "timing"])
 def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     """run() of the Synthetic-Vascusynth preset on an .mhd volume: the TDF,
     the centerpoints and vertices bit for bit against the oracle; without loop
@@ -225,7 +225,9 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
     centerline volume (split vertices may land on existing positions, which
     the reference's position-keyed loop removal merges).  The segmentation
     (inverse gradient, or spheres) of those centerlines bit for bit against
-    the oracle, with the radius averaged along the edges after loop removal."""
+    the oracle, with the radius averaged along the edges after loop removal.
+    With the timing parameter: the same results, and one "RUNTIME <stage>:
+    <ms> ms" line per stage (the reference's stage names)."""
     pytest.importorskip("torch")
     vol = synth.vascular_tree((44, 52, 60), seed=11)
     vol_u8 = np.round(vol * 90.0).astype(np.uint8)          # some voxels above the preset maximum 75
@@ -245,8 +247,22 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
         args += ["--no-segmentation", "true"]
     elif mode == "vtk":
         args += ["--centerline-vtk-file", vtk]
+    elif mode == "timing":
+        args += ["--timing", "true"]
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
+    runtime = [l for l in out.stdout.splitlines() if l.startswith("RUNTIME ")]
+    if mode != "timing":
+        assert not runtime
+    else:
+        stages = [l[len("RUNTIME "):l.rindex(":")] for l in runtime]
+        assert stages == ["of reading the dataset", "of data transfer to device", "of cropping",
+                          "of to float conversion", "of Create vector field", "of TDF small", "blurring",
+                          "Create vector field", "of GVF", "of TDF large", "of combine", "centerpoint extraction",
+                          "linking", "of loop removal and centerline voxels (host)", "of removing small trees",
+                          "of segmentation"], stages
+        for l in runtime:
+            assert l.endswith(" ms") and float(l[l.rindex(":") + 1:-3]) >= 0.0
     X, Y, Z = map(int, open(tmp_path / "size.txt").read().split())
     assert (X, Y, Z) == (60, 52, 44)
     tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(Z, Y, X)
@@ -278,10 +294,10 @@ def test_run_matches_oracle(api_tests, oracle, synth, tmp_path, mode):
             assert np.array_equal(seg, ref_seg)
         return
     import tsf_gb300 as tsf
-    if mode in ("default", "no-segmentation"):
+    if mode in ("default", "no-segmentation", "timing"):
         ref_cl, rad, _, _ = tsf.centerline_graph(ref["vertices"], edges, labels, sizes, 3, R)
         assert np.array_equal(cl, ref_cl)
-        if mode == "default":
+        if mode in ("default", "timing"):
             assert np.array_equal(seg, oracle.segment_inverse_gradient(ref_cl, field, rad)[0])
         return
     pts, ve = _read_vtk(vtk)

@@ -446,13 +446,18 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
     const std::string method = getParamStr(parameters, "centerline-method");
     if (method != "gpu") raise("centerline-method " + method + " is not part of this library (use gpu)");
 
+    // the file first: a missing file raises SIPL::IOException before any device work
+    const bool timing = getParamBool(parameters, "timing");
+    float minimum = 0.0f, maximum = 1.0f;
+    const auto t_read = std::chrono::steady_clock::now();
+    HostVolume hv = read_volume(filename, parameters, minimum, maximum);
+    if (timing)
+        std::cout << "RUNTIME of reading the dataset: "
+                  << std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_read).count()
+                  << " ms" << std::endl;
     Stream stream;
     void *S = (void *)stream.s;
-    StageTimer tm(getParamBool(parameters, "timing"), stream.s);
-    float minimum = 0.0f, maximum = 1.0f;
-    tm.host_start();
-    HostVolume hv = read_volume(filename, parameters, minimum, maximum);
-    tm.host_stop("of reading the dataset");
+    StageTimer tm(timing, stream.s);
     tm.start();
     DevBuf raw(hv.bytes);
     check_cuda(cudaMemcpyAsync(raw.p, hv.data.get(), hv.bytes, cudaMemcpyHostToDevice, stream.s), "upload");
