@@ -424,6 +424,37 @@ int tsf_centerline_graph(const int *vertices, int n_vertices, const int *edges, 
                          int max_edge_distance, int X, int Y, int Z, float *radius,
                          int8_t *centerlines, int *out_vertices, int *out_edges, int capacity,
                          int *n_out_vertices, int *n_out_edges);
+/* tsf_centerline_graph for volumes kept on the device: the same graph
+ * (out_vertices, out_edges, both counts, the capacity rule) and, instead of
+ * writing centerlines and radius, the cells createCenterlineVoxels visits
+ * (parallelCenterlineExtraction.cpp:287-321), edge after edge in order:
+ * cells[edge_start[k] .. edge_start[k+1]) for output edge k, as x + X*(y +
+ * Y*z); edge_start holds n_out_edges + 1 entries (room for capacity + 1).
+ * *n_cells is returned too, and TSF_ERR_CAPACITY also when it exceeds
+ * cell_capacity.
+ * tsf_centerline_smooth_radius: given values[i] = radius at cells[i] (read
+ * with tsf_gather_cells), replays the edge-ordered mean of the radius along
+ * each edge and returns each distinct cell once, in first-visit order, with
+ * its final radius (room for edge_start[n_edges] entries).
+ * tsf_gather_cells / tsf_centerline_apply (device): d_values[i] =
+ * d_volume[d_cells[i]]; d_centerlines[d_cells[i]] = 1 and, unless d_radius
+ * is NULL, d_radius[d_cells[i]] = d_values[i].  Cells outside [0, X*Y*Z)
+ * are skipped.  Together these give the centerlines and radius of
+ * tsf_centerline_graph without copying the volumes to the host. */
+int tsf_centerline_graph_cells(const int *vertices, int n_vertices, const int *edges, int n_edges,
+                               const int *labels, const int *tree_sizes, int min_tree_length,
+                               int max_edge_distance, int X, int Y, int Z, int *out_vertices,
+                               int *out_edges, int capacity, int *n_out_vertices, int *n_out_edges,
+                               int64_t *cells, int64_t *edge_start, int64_t cell_capacity,
+                               int64_t *n_cells);
+int tsf_centerline_smooth_radius(const int64_t *cells, const int64_t *edge_start, int n_edges,
+                                 const float *values, int64_t *unique_cells, float *unique_values,
+                                 int64_t *n_unique);
+int tsf_gather_cells(const float *d_volume, int X, int Y, int Z, const int64_t *d_cells,
+                     int64_t n_cells, float *d_values, void *stream);
+int tsf_centerline_apply(int8_t *d_centerlines, float *d_radius, int X, int Y, int Z,
+                         const int64_t *d_cells, const float *d_values, int64_t n_cells,
+                         void *stream);
 int tsf_remove_loops(const int *vertices, int n_vertices, const int *edges, int n_edges, int X,
                      int Y, int Z, int *out_vertices, int *out_edges, int capacity,
                      int *n_out_vertices, int *n_out_edges);

@@ -153,6 +153,66 @@ def test_short_capacity_writes_nothing(tsf):
     assert cl.any() and not np.array_equal(rad, radius)
 
 
+def _graph_cells(tsf, v, e, labels, sizes, min_tree, shape, split=0, cap=4096, ccap=1 << 16):
+    import ctypes as C
+    Z, Y, X = shape
+    v, e = np.ascontiguousarray(v, np.int32), np.ascontiguousarray(e, np.int32)
+    labels, sizes = np.ascontiguousarray(labels, np.int32), np.ascontiguousarray(sizes, np.int32)
+    ov, oe = np.zeros((cap, 3), np.int32), np.zeros((cap, 2), np.int32)
+    cells, start = np.zeros(ccap, np.int64), np.zeros(cap + 1, np.int64)
+    nv, ne, nc = C.c_int(0), C.c_int(0), C.c_int64(0)
+    code = tsf.load().tsf_centerline_graph_cells(
+        tsf._np_ptr(v), len(v), tsf._np_ptr(e), len(e), tsf._np_ptr(labels), tsf._np_ptr(sizes), min_tree, split,
+        X, Y, Z, tsf._np_ptr(ov), tsf._np_ptr(oe), cap, C.byref(nv), C.byref(ne), tsf._np_ptr(cells),
+        tsf._np_ptr(start), C.c_int64(ccap), C.byref(nc))
+    return code, ov[:nv.value], oe[:ne.value], cells[:nc.value], start[:ne.value + 1]
+
+
+def test_cells_and_smoothing_equal_the_volume_stage(tsf):
+    """tsf_centerline_graph_cells + tsf_centerline_smooth_radius, applied to
+    the volumes, give exactly tsf_centerline_graph's centerlines and radius
+    (loops, shared cells between edges, a dropped small tree)."""
+    import ctypes as C
+    rng = np.random.default_rng(7)
+    pos = set()
+    while len(pos) < 50:
+        pos.add(tuple(rng.integers(0, 30, 3).tolist()))
+    v = np.array(sorted(pos))
+    e = {(int(rng.integers(0, i)), i) for i in range(1, 45)}
+    while len(e) < 60:
+        a, b = rng.integers(0, 45, 2)
+        if a != b and (b, a) not in e:
+            e.add((int(a), int(b)))
+    e = np.array(sorted(e) + [(45, 46), (47, 48)])               # plus two 2-vertex trees (dropped at 3)
+    labels = np.array([0] * 45 + [45, 45, 47, 47, 49])
+    sizes = np.zeros(50, np.int32)
+    sizes[0], sizes[45], sizes[47], sizes[49] = 45, 2, 2, 1
+    shape = (30, 30, 30)
+    radius = rng.random(shape).astype(np.float32)
+    cl_ref, rad_ref, ov_ref, oe_ref = tsf.centerline_graph(v, e, labels, sizes, 3, radius)
+    code, ov, oe, cells, start = _graph_cells(tsf, v, e, labels, sizes, 3, shape)
+    assert code == 0
+    assert np.array_equal(ov, ov_ref) and np.array_equal(oe, oe_ref)
+    assert start[0] == 0 and start[-1] == len(cells) and np.all(np.diff(start) >= 0)
+    assert len(np.unique(cells)) < len(cells)                      # edges share their end cells
+    flat = radius.reshape(-1)
+    vals = np.ascontiguousarray(flat[cells])
+    uc, uv = np.zeros(len(cells), np.int64), np.zeros(len(cells), np.float32)
+    nu = C.c_int64(0)
+    assert tsf.load().tsf_centerline_smooth_radius(tsf._np_ptr(cells), tsf._np_ptr(start), len(oe),
+                                                   tsf._np_ptr(vals), tsf._np_ptr(uc), tsf._np_ptr(uv),
+                                                   C.byref(nu)) == 0
+    uc, uv = uc[:nu.value], uv[:nu.value]
+    assert len(np.unique(uc)) == len(uc) and set(uc.tolist()) == set(cells.tolist())
+    cl, rad = np.zeros(flat.shape, np.int8), flat.copy()
+    cl[uc], rad[uc] = 1, uv
+    assert np.array_equal(cl.reshape(shape), cl_ref)
+    assert np.array_equal(rad.reshape(shape).view(np.uint32), rad_ref.view(np.uint32))
+    # a short cell capacity: the counts come back, nothing else is needed
+    code, _, _, short, _ = _graph_cells(tsf, v, e, labels, sizes, 3, shape, ccap=len(cells) - 1)
+    assert code == 6
+
+
 def test_edge_splitting_for_the_vtk_file(tsf):
     v = np.array([[2, 4, 4], [14, 4, 4], [20, 4, 4]])
     e = np.array([[0, 1], [1, 2]])

@@ -72,3 +72,35 @@ def test_link_no_edges(torch_dev, tsf):
     with pytest.raises(tsf.TSFError) as e:
         tsf.link_centerpoints(v, T, 0.5, 5.0)
     assert e.value.code == 4 and "No edges" in str(e.value)
+
+
+def test_gather_and_apply_cells(torch_dev, tsf):
+    """tsf_gather_cells / tsf_centerline_apply (createCenterlineVoxels'
+    device side): the radius read at the listed cells, the centerline mark and
+    the new radius written there, cells outside the volume skipped (read as
+    0, nothing written)."""
+    torch = torch_dev
+    L = tsf.load()
+    Z, Y, X = 20, 24, 28
+    n = X * Y * Z
+    rng = np.random.default_rng(5)
+    rad = rng.random((Z, Y, X)).astype(np.float32)
+    cells = np.concatenate([rng.choice(n, 500, replace=False), [-1, n, n + 7]]).astype(np.int64)
+    d_rad = torch.from_numpy(rad).cuda()
+    d_cells = torch.from_numpy(cells).cuda()
+    d_vals = torch.empty(len(cells), dtype=torch.float32, device="cuda")
+    assert L.tsf_gather_cells(tsf._ptr(d_rad), X, Y, Z, tsf._ptr(d_cells), len(cells), tsf._ptr(d_vals), None) == 0
+    got = d_vals.cpu().numpy()
+    assert np.array_equal(got[:500], rad.reshape(-1)[cells[:500]]) and not got[500:].any()
+    new = rng.random(len(cells)).astype(np.float32)
+    d_cl = torch.zeros((Z, Y, X), dtype=torch.int8, device="cuda")
+    assert L.tsf_centerline_apply(tsf._ptr(d_cl), tsf._ptr(d_rad), X, Y, Z, tsf._ptr(d_cells),
+                                  tsf._ptr(torch.from_numpy(new).cuda()), len(cells), None) == 0
+    want_cl, want_rad = np.zeros(n, np.int8), rad.reshape(-1).copy()
+    want_cl[cells[:500]], want_rad[cells[:500]] = 1, new[:500]
+    assert np.array_equal(d_cl.cpu().numpy().reshape(-1), want_cl)
+    assert np.array_equal(d_rad.cpu().numpy().reshape(-1), want_rad)
+    # the centerline mark alone (no radius)
+    d_cl.zero_()
+    assert L.tsf_centerline_apply(tsf._ptr(d_cl), None, X, Y, Z, tsf._ptr(d_cells), None, len(cells), None) == 0
+    assert np.array_equal(d_cl.cpu().numpy().reshape(-1), want_cl)

@@ -347,7 +347,66 @@ int run_rasterize_trees(const int *d_v, const int *d_edges, int ne, const int *d
     return TSF_OK;
 }
 
+// createCenterlineVoxels' device side (parallelCenterlineExtraction.cpp:
+// 287-321): the host lists the cells the kept edges visit; these read the
+// radius there and write the centerline mark and the smoothed radius back.
+// Cells outside [0, X*Y*Z) are skipped.
+__global__ void gather_cells_kernel(const float *__restrict__ vol, int64_t nvox, const int64_t *__restrict__ cells,
+                                    int64_t n, float *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t p = cells[i];
+    out[i] = (p >= 0 && p < nvox) ? vol[p] : 0.0f;
+}
+
+__global__ void centerline_apply_kernel(int8_t *__restrict__ cl, float *__restrict__ radius, int64_t nvox,
+                                        const int64_t *__restrict__ cells, const float *__restrict__ values,
+                                        int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t p = cells[i];
+    if (p < 0 || p >= nvox) return;
+    cl[p] = 1;
+    if (radius) radius[p] = values[i];
+}
+
+int run_gather_cells(const float *d_vol, int X, int Y, int Z, const int64_t *d_cells, int64_t n, float *d_out,
+                     cudaStream_t s) {
+    int r = check_dims(X, Y, Z);
+    if (r) return r;
+    if (n < 0 || (n > 0 && (!d_vol || !d_cells || !d_out))) return fail(TSF_ERR_INVALID_ARG, "invalid gather arguments");
+    if (n == 0) return TSF_OK;
+    gather_cells_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_vol, (int64_t)X * Y * Z, d_cells, n, d_out);
+    TSF_CHECK_LAUNCH("gather_cells_kernel");
+    return TSF_OK;
+}
+
+int run_centerline_apply(int8_t *d_cl, float *d_radius, int X, int Y, int Z, const int64_t *d_cells,
+                         const float *d_values, int64_t n, cudaStream_t s) {
+    int r = check_dims(X, Y, Z);
+    if (r) return r;
+    if (n < 0 || (n > 0 && (!d_cl || !d_cells || (d_radius && !d_values))))
+        return fail(TSF_ERR_INVALID_ARG, "invalid centerline arguments");
+    if (n == 0) return TSF_OK;
+    centerline_apply_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_cl, d_radius, (int64_t)X * Y * Z, d_cells,
+                                                                       d_values, n);
+    TSF_CHECK_LAUNCH("centerline_apply_kernel");
+    return TSF_OK;
+}
+
 }  // namespace tsf
+
+extern "C" int tsf_gather_cells(const float *d_volume, int X, int Y, int Z, const int64_t *d_cells, int64_t n_cells,
+                                float *d_values, void *stream) {
+    return tsf::run_gather_cells(d_volume, X, Y, Z, d_cells, n_cells, d_values,
+                                 reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tsf_centerline_apply(int8_t *d_centerlines, float *d_radius, int X, int Y, int Z,
+                                    const int64_t *d_cells, const float *d_values, int64_t n_cells, void *stream) {
+    return tsf::run_centerline_apply(d_centerlines, d_radius, X, Y, Z, d_cells, d_values, n_cells,
+                                     reinterpret_cast<cudaStream_t>(stream));
+}
 
 extern "C" size_t tsf_link_workspace_size(int n_vertices) { return tsf::link_workspace_size(n_vertices); }
 

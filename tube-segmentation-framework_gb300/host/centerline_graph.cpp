@@ -12,6 +12,7 @@
 // (smallest distance on top) and its push order, so equal distances resolve
 // the same way; new roots are the last unvisited node, as there.  Nodes and
 // edges are indices into arrays here rather than heap objects.
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -187,31 +188,43 @@ private:
     }
 };
 
-// createCenterlineVoxels: ceil(|ab|) steps from a towards b; the radius along
-// the edge is replaced by its mean there
+// createCenterlineVoxels: ceil(|ab|) steps from a towards b, in order (a
+// cell may repeat when the edge is short and the rounding lands twice)
+static void edge_cells(const V3 &a, const V3 &b, V3 size, std::vector<int64_t> &cells) {
+    const float d = dist(a, b);
+    const float dir[3] = {(float)(b.x - a.x), (float)(b.y - a.y), (float)(b.z - a.z)};
+    const int n = (int)std::ceil(d);
+    for (int j = 0; j < n; j++) {
+        const float ratio = (float)j / (float)n;
+        const int x = (int)std::round((float)a.x + dir[0] * ratio);
+        const int y = (int)std::round((float)a.y + dir[1] * ratio);
+        const int z = (int)std::round((float)a.z + dir[2] * ratio);
+        cells.push_back((int64_t)x + (int64_t)size.x * (y + (int64_t)size.y * z));
+    }
+}
+
+// the radius along each edge replaced by its mean there, edge after edge:
+// `at(p)` is the current radius of cell p (earlier edges' means included)
+template <typename At>
+static void smooth_edges(const std::vector<int64_t> &cells, const std::vector<int64_t> &start, At at) {
+    for (size_t k = 0; k + 1 < start.size(); k++) {
+        const int64_t c0 = start[k], c1 = start[k + 1];
+        float avg = 0.0f;
+        for (int64_t i = c0; i < c1; i++) avg = avg + at(cells[(size_t)i]);
+        avg = avg / (float)(c1 - c0);
+        for (int64_t i = c0; i < c1; i++) at(cells[(size_t)i]) = avg;
+    }
+}
+
 static void centerline_voxels(const std::vector<V3> &v, const std::vector<std::array<int, 2>> &e, float *radius,
                               int8_t *out, V3 size) {
-    auto pos = [&](int x, int y, int z) { return (int64_t)x + (int64_t)size.x * (y + (int64_t)size.y * z); };
+    std::vector<int64_t> cells, start{0};
     for (const auto &ed : e) {
-        const V3 a = v[ed[0]], b = v[ed[1]];
-        const float d = dist(a, b);
-        const float dir[3] = {(float)(b.x - a.x), (float)(b.y - a.y), (float)(b.z - a.z)};
-        const int n = (int)std::ceil(d);
-        float avg = 0.0f;
-        std::vector<int64_t> cells;
-        for (int j = 0; j < n; j++) {
-            const float ratio = (float)j / (float)n;
-            const int x = (int)std::round((float)a.x + dir[0] * ratio);
-            const int y = (int)std::round((float)a.y + dir[1] * ratio);
-            const int z = (int)std::round((float)a.z + dir[2] * ratio);
-            const int64_t p = pos(x, y, z);
-            out[p] = 1;
-            avg = avg + radius[p];
-            cells.push_back(p);
-        }
-        avg = avg / (float)n;
-        for (int64_t p : cells) radius[p] = avg;
+        edge_cells(v[ed[0]], v[ed[1]], size, cells);
+        start.push_back((int64_t)cells.size());
     }
+    for (int64_t p : cells) out[p] = 1;
+    smooth_edges(cells, start, [&](int64_t p) -> float & { return radius[p]; });
 }
 
 }  // namespace tsf_host
@@ -257,16 +270,12 @@ extern "C" int tsf_remove_loops(const int *vertices, int n_vertices, const int *
     return copy_out(v, e, out_vertices, out_edges, capacity, n_out_vertices, n_out_edges);
 }
 
-extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const int *edges, int n_edges,
-                                    const int *labels, const int *tree_sizes, int min_tree_length,
-                                    int max_edge_distance, int X, int Y, int Z, float *radius,
-                                    int8_t *centerlines, int *out_vertices, int *out_edges, int capacity,
-                                    int *n_out_vertices, int *n_out_edges) {
-    if (!vertices || !edges || !labels || !tree_sizes || !radius || !centerlines || !out_vertices || !out_edges ||
-        !n_out_vertices || !n_out_edges || n_vertices < 0 || n_edges < 0)
-        return TSF_ERR_INVALID_ARG;
-    // vertices and edges of the large trees (parallelCenterlineExtraction.cpp:1187-1225)
-    std::vector<V3> v;
+// the large trees' vertices and edges (parallelCenterlineExtraction.cpp:
+// 1187-1225), edges longer than max_edge_distance split, loops removed;
+// TSF_ERR_COUNT_RANGE when nothing is left
+static int large_tree_graph(const int *vertices, int n_vertices, const int *edges, int n_edges, const int *labels,
+                            const int *tree_sizes, int min_tree_length, int max_edge_distance, int X, int Y, int Z,
+                            std::vector<V3> &v, std::vector<std::array<int, 2>> &e) {
     std::vector<int> index(n_vertices, -1);
     for (int i = 0; i < n_vertices; i++) {
         if (tree_sizes[labels[i]] >= min_tree_length) {
@@ -274,7 +283,6 @@ extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const i
             v.push_back(V3{vertices[3 * i], vertices[3 * i + 1], vertices[3 * i + 2]});
         }
     }
-    std::vector<std::array<int, 2>> e;
     for (int i = 0; i < n_edges; i++) {
         const int a = edges[2 * i], b = edges[2 * i + 1];
         if (tree_sizes[labels[a]] < min_tree_length || tree_sizes[labels[b]] < min_tree_length) continue;
@@ -303,6 +311,22 @@ extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const i
     } catch (const std::exception &) {
         return TSF_ERR_COUNT_RANGE;
     }
+    return TSF_OK;
+}
+
+extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const int *edges, int n_edges,
+                                    const int *labels, const int *tree_sizes, int min_tree_length,
+                                    int max_edge_distance, int X, int Y, int Z, float *radius,
+                                    int8_t *centerlines, int *out_vertices, int *out_edges, int capacity,
+                                    int *n_out_vertices, int *n_out_edges) {
+    if (!vertices || !edges || !labels || !tree_sizes || !radius || !centerlines || !out_vertices || !out_edges ||
+        !n_out_vertices || !n_out_edges || n_vertices < 0 || n_edges < 0)
+        return TSF_ERR_INVALID_ARG;
+    std::vector<V3> v;
+    std::vector<std::array<int, 2>> e;
+    const int r = large_tree_graph(vertices, n_vertices, edges, n_edges, labels, tree_sizes, min_tree_length,
+                                   max_edge_distance, X, Y, Z, v, e);
+    if (r) return r;
     // the counts first: when they exceed the capacity, radius and centerlines
     // are left as they were, so the caller can call again with more
     *n_out_vertices = (int)v.size();
@@ -310,6 +334,60 @@ extern "C" int tsf_centerline_graph(const int *vertices, int n_vertices, const i
     if ((int)v.size() > capacity || (int)e.size() > capacity) return TSF_ERR_CAPACITY;
     tsf_host::centerline_voxels(v, e, radius, centerlines, V3{X, Y, Z});
     return copy_out(v, e, out_vertices, out_edges, capacity, n_out_vertices, n_out_edges);
+}
+
+extern "C" int tsf_centerline_graph_cells(const int *vertices, int n_vertices, const int *edges, int n_edges,
+                                          const int *labels, const int *tree_sizes, int min_tree_length,
+                                          int max_edge_distance, int X, int Y, int Z, int *out_vertices,
+                                          int *out_edges, int capacity, int *n_out_vertices, int *n_out_edges,
+                                          int64_t *cells, int64_t *edge_start, int64_t cell_capacity,
+                                          int64_t *n_cells) {
+    if (!vertices || !edges || !labels || !tree_sizes || !out_vertices || !out_edges || !n_out_vertices ||
+        !n_out_edges || !cells || !edge_start || !n_cells || n_vertices < 0 || n_edges < 0 || X <= 0 || Y <= 0 ||
+        Z <= 0)
+        return TSF_ERR_INVALID_ARG;
+    std::vector<V3> v;
+    std::vector<std::array<int, 2>> e;
+    const int r = large_tree_graph(vertices, n_vertices, edges, n_edges, labels, tree_sizes, min_tree_length,
+                                   max_edge_distance, X, Y, Z, v, e);
+    if (r) return r;
+    std::vector<int64_t> c, start{0};
+    for (const auto &ed : e) {
+        tsf_host::edge_cells(v[ed[0]], v[ed[1]], V3{X, Y, Z}, c);
+        start.push_back((int64_t)c.size());
+    }
+    *n_out_vertices = (int)v.size();
+    *n_out_edges = (int)e.size();
+    *n_cells = (int64_t)c.size();
+    if ((int)v.size() > capacity || (int)e.size() > capacity || (int64_t)c.size() > cell_capacity)
+        return TSF_ERR_CAPACITY;
+    std::copy(c.begin(), c.end(), cells);
+    std::copy(start.begin(), start.end(), edge_start);
+    return copy_out(v, e, out_vertices, out_edges, capacity, n_out_vertices, n_out_edges);
+}
+
+extern "C" int tsf_centerline_smooth_radius(const int64_t *cells, const int64_t *edge_start, int n_edges,
+                                            const float *values, int64_t *unique_cells, float *unique_values,
+                                            int64_t *n_unique) {
+    if (!cells || !edge_start || !values || !unique_cells || !unique_values || !n_unique || n_edges < 0)
+        return TSF_ERR_INVALID_ARG;
+    const int64_t n = edge_start[n_edges];
+    // current radius per distinct cell, starting from the gathered values
+    std::unordered_map<int64_t, size_t> slot;
+    std::vector<int64_t> uc;
+    std::vector<float> uv;
+    for (int64_t i = 0; i < n; i++) {
+        if (slot.emplace(cells[i], uc.size()).second) {
+            uc.push_back(cells[i]);
+            uv.push_back(values[i]);
+        }
+    }
+    const std::vector<int64_t> c(cells, cells + n), start(edge_start, edge_start + n_edges + 1);
+    tsf_host::smooth_edges(c, start, [&](int64_t p) -> float & { return uv[slot[p]]; });
+    std::copy(uc.begin(), uc.end(), unique_cells);
+    std::copy(uv.begin(), uv.end(), unique_values);
+    *n_unique = (int64_t)uc.size();
+    return TSF_OK;
 }
 
 extern "C" int tsf_write_centerline_vtk(const char *path, const int *vertices, int n_vertices, const int *edges,

@@ -41,7 +41,6 @@
 #include <fcntl.h>
 #include <unistd.h>
 
-#include "first_touch.hpp"
 #include "tsf/tsf_c.h"
 #include "tsf/tube-segmentation.hpp"
 
@@ -550,50 +549,66 @@ TSFOutput *run(std::string filename, paramList &parameters, std::string /*kernel
         const std::string vtk = getParamStr(parameters, "centerline-vtk-file");
         const bool segment = !getParamBool(parameters, "no-segmentation");
         const int8_t *d_cl = nullptr;   // the centerlines on the device, for the segmentation
-        DevBuf dcl;
         if (vtk != "off" || getParamBool(parameters, "loop-removal")) {
-            // host loop removal and rasterisation (parallelCenterlineExtraction.cpp:1168-1247)
+            // host loop removal (parallelCenterlineExtraction.cpp:1168-1247); the centerline voxels and
+            // the radius smoothing of createCenterlineVoxels (:287-321) touch only the cells along the kept
+            // edges, which are read from and written to the device volumes (the reference writes the
+            // centerlines and the averaged radius back to its images, :1235-1249)
             std::vector<int32_t> he(2 * (size_t)ne), hl((size_t)nvi), hs((size_t)nvi);
-            std::unique_ptr<float[]> radius(new float[n]);   // filled by the copy below
-            tsf_host::parallel_fill(radius.get(), 0, n * sizeof(float));
             check_cuda(cudaMemcpyAsync(he.data(), dedges.p, he.size() * 4, cudaMemcpyDeviceToHost, stream.s), "edges");
             check_cuda(cudaMemcpyAsync(hl.data(), dlabels.p, hl.size() * 4, cudaMemcpyDeviceToHost, stream.s), "labels");
             check_cuda(cudaMemcpyAsync(hs.data(), dsizes.p, hs.size() * 4, cudaMemcpyDeviceToHost, stream.s), "sizes");
-            check_cuda(cudaMemcpyAsync(radius.get(), fr.R.p, n * 4, cudaMemcpyDeviceToHost, stream.s), "radius");
             check_cuda(cudaStreamSynchronize(stream.s), "graph download");
             const int split = vtk != "off" ? (int)getParam(parameters, "max-edge-distance") : 0;
-            std::unique_ptr<char[]> centerlines(new char[n]);
-            tsf_host::parallel_fill(centerlines.get(), 0, n);
-            int cap = 4 * (nvi + ne) + 1024, nov = 0, noe = 0, gcode;
-            std::vector<int32_t> ov, oe;
             StageTimer graph_tm(tm.on(), stream.s);
             graph_tm.host_start();
+            int cap = 4 * (nvi + ne) + 1024, nov = 0, noe = 0, gcode;
+            int64_t ccap = 16 * (int64_t)cap, nc = 0;
+            std::vector<int32_t> ov, oe;
+            std::vector<int64_t> cells, start;
             for (;;) {
                 ov.assign(3 * (size_t)cap, 0);
                 oe.assign(2 * (size_t)cap, 0);
-                // a short capacity leaves radius and centerlines untouched
-                gcode = tsf_centerline_graph(hv3.data(), nvi, he.data(), ne, hl.data(), hs.data(), min_tree, split,
-                                             X, Y, Z, radius.get(), reinterpret_cast<int8_t *>(centerlines.get()),
-                                             ov.data(), oe.data(), cap, &nov, &noe);
+                cells.resize((size_t)ccap);
+                start.resize((size_t)cap + 1);
+                gcode = tsf_centerline_graph_cells(hv3.data(), nvi, he.data(), ne, hl.data(), hs.data(), min_tree,
+                                                   split, X, Y, Z, ov.data(), oe.data(), cap, &nov, &noe,
+                                                   cells.data(), start.data(), ccap, &nc);
                 if (gcode != TSF_ERR_CAPACITY) break;
-                cap = 2 * std::max(nov, noe);
+                cap = std::max(cap, 2 * std::max(nov, noe));
+                ccap = std::max(ccap, 2 * nc);
             }
-            graph_tm.host_stop("of loop removal and centerline voxels (host)");
             if (gcode == TSF_ERR_COUNT_RANGE)
                 throw SIPL::SIPLException("Centerline graph size is 0! Can't continue. Maybe lower min-tree-length?",
                                           __LINE__, __FILE__);
             check(gcode, "centerline graph");
-            if (segment) {
-                // the reference writes the centerlines and the averaged radius back to its images
-                // (parallelCenterlineExtraction.cpp:1235-1249); pageable sources are staged before the
-                // copies return
-                dcl.alloc(n);
-                check_cuda(cudaMemcpyAsync(dcl.p, centerlines.get(), n, cudaMemcpyHostToDevice, stream.s),
-                           "centerlines");
-                check_cuda(cudaMemcpyAsync(fr.R.p, radius.get(), n * 4, cudaMemcpyHostToDevice, stream.s), "radius");
-                d_cl = dcl.as<int8_t>();
-            }
-            output->setCenterlineVoxels(centerlines.release());
+            DevBuf dcells(sizeof(int64_t) * (size_t)std::max<int64_t>(nc, 1)),
+                dvals(sizeof(float) * (size_t)std::max<int64_t>(nc, 1));
+            std::vector<float> vals((size_t)nc);
+            check_cuda(cudaMemcpyAsync(dcells.p, cells.data(), sizeof(int64_t) * (size_t)nc, cudaMemcpyHostToDevice,
+                                       stream.s), "cells");
+            check(tsf_gather_cells(fr.R.as<float>(), X, Y, Z, dcells.as<int64_t>(), nc, dvals.as<float>(), S),
+                  "radius");
+            check_cuda(cudaMemcpyAsync(vals.data(), dvals.p, sizeof(float) * (size_t)nc, cudaMemcpyDeviceToHost,
+                                       stream.s), "radius");
+            check_cuda(cudaStreamSynchronize(stream.s), "radius");
+            std::vector<int64_t> ucells((size_t)nc);
+            std::vector<float> uvals((size_t)nc);
+            int64_t nu = 0;
+            check(tsf_centerline_smooth_radius(cells.data(), start.data(), noe, vals.data(), ucells.data(),
+                                               uvals.data(), &nu), "centerline radius");
+            graph_tm.host_stop("of loop removal and centerline voxels (host)");
+            DevBuf cl(n);
+            check_cuda(cudaMemsetAsync(cl.p, 0, n, stream.s), "centerlines");
+            check_cuda(cudaMemcpyAsync(dcells.p, ucells.data(), sizeof(int64_t) * (size_t)nu, cudaMemcpyHostToDevice,
+                                       stream.s), "cells");
+            check_cuda(cudaMemcpyAsync(dvals.p, uvals.data(), sizeof(float) * (size_t)nu, cudaMemcpyHostToDevice,
+                                       stream.s), "radius");
+            check(tsf_centerline_apply(cl.as<int8_t>(), segment ? fr.R.as<float>() : nullptr, X, Y, Z,
+                                       dcells.as<int64_t>(), dvals.as<float>(), nu, S), "centerlines");
+            check_cuda(cudaStreamSynchronize(stream.s), "centerlines");
+            d_cl = cl.as<int8_t>();        // owned by the output from here on
+            output->setDeviceCenterlineVoxels(static_cast<int8_t *>(cl.release()));
             if (vtk != "off" && tsf_write_centerline_vtk(vtk.c_str(), ov.data(), nov, oe.data(), noe) != TSF_OK)
                 throw SIPL::IOException(vtk.c_str(), __LINE__, __FILE__);
         } else {

@@ -84,6 +84,11 @@ def _declare(L):
         "tsf_remove_loops": (_i, [_p, _i, _p, _i, _i, _i, _i, _p, _p, _i, _p, _p]),
         "tsf_centerline_graph": (_i, [_p, _i, _p, _i, _p, _p, _i, _i, _i, _i, _i, _p, _p, _p, _p, _i, _p, _p]),
         "tsf_write_centerline_vtk": (_i, [C.c_char_p, _p, _i, _p, _i]),
+        "tsf_centerline_graph_cells": (_i, [_p, _i, _p, _i, _p, _p, _i, _i, _i, _i, _i, _p, _p, _i, _p, _p, _p, _p,
+                                            _i64, _p]),
+        "tsf_centerline_smooth_radius": (_i, [_p, _p, _i, _p, _p, _p, _p]),
+        "tsf_gather_cells": (_i, [_p, _i, _i, _i, _p, _i64, _p, _p]),
+        "tsf_centerline_apply": (_i, [_p, _p, _i, _i, _i, _p, _p, _i64, _p]),
         "tsf_gvf_adjoint_checkpoint_interval": (_i, [_i, _i, _i, _i, _i, _sz]),
         "tsf_gvf_finish": (_i, [_p, _p, _i, _i, _i, _i, _p]),
         "tsf_gvf_static": (_i, [_p, _p, _i, _i, _i, _f, _i, _i, _p]),
