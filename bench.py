@@ -1220,7 +1220,8 @@ def run_polish(args):
     the raw volume; both TDF passes, combine and the candidate stage as in the
     benchmark step.  Variants store the polished field in snorm16 or in the
     16-bit format again for the finish and the large-radius pass, and the
-    small-radius field in snorm16, FP32 or the 16-bit format.  Reports, per
+    small-radius field in snorm16, FP32 or the 16-bit format; one runs the last
+    k iterations in snorm16 instead of FP32.  Reports, per
     variant, the vertex list against the FP64 oracle run of the same method and
     the step time (CUDA events, median of 3 after a warm-up) next to the plain
     16-bit and FP32 paths."""
@@ -1240,14 +1241,14 @@ def run_polish(args):
     L = T.load()
     ws16 = T.workspace(L.tsf_tdf_workspace_size(n, n, n, T.STORAGE[args.storage]))
 
-    def path(st, kp, fin_st, small_st):
+    def path(st, kp, fin_st, small_st, pol_st="f32"):
         b = T.blur(g, P["large_blur"])
         f0, _ = T.vector_field(b, P["fmax"], P["vsign"], st)
         v = T.gvf(f0, args.mu, K - kp, st)
         if kp:
-            f32, _ = T.vector_field(b, P["fmax"], P["vsign"], "f32")
-            v = T.gvf(f32, args.mu, kp, "f32", v=T.convert_field(v, st, "f32"))
-            vst = "f32"
+            fp, _ = T.vector_field(b, P["fmax"], P["vsign"], pol_st)
+            v = T.gvf(fp, args.mu, kp, pol_st, v=T.convert_field(v, st, pol_st))
+            vst = pol_st
         else:
             vst = st
         if fin_st != vst:
@@ -1269,7 +1270,9 @@ def run_polish(args):
                 # the large-radius pass, the small-radius field in snorm16 or FP32; or back in the 16-bit format
                 "%s+%d_f32_polish_snorm16_tdf" % (st, k): (st, k, "snorm16", "snorm16"),
                 "%s+%d_f32_polish_snorm16_large_f32_small" % (st, k): (st, k, "snorm16", "f32"),
-                "%s+%d_f32_polish_%s_large_f32_small" % (st, k, st): (st, k, st, "f32")}
+                "%s+%d_f32_polish_%s_large_f32_small" % (st, k, st): (st, k, st, "f32"),
+                # the last k iterations in snorm16 instead of FP32, the field left in snorm16
+                "%s+%d_snorm16_polish_f32_small" % (st, k): (st, k, "snorm16", "f32", "snorm16")}
     s64 = set(map(tuple, V64.tolist()))
     out = {"size": n, "iterations": K, "mu": args.mu, "fp64_vertices": int(len(V64)), "oracle_s": round(t_oracle, 1),
            "note": "step = blur, vector fields, GVF, finish, both TDF passes, combine, candidates; CUDA events, "
