@@ -170,6 +170,24 @@ static void io_tests() {
     paramList p3 = initParameters(PARAMETERS_DIR);
     setParameter(p3, "device", "cpu");
     EXPECT_THROW(run("x.mhd", p3, KERNELS_DIR), SIPL::SIPLException);
+    // a .raw file shorter than DimSize x the element size: IOException before any device call
+    // (the read splits the file over threads; a short slice fails the whole read)
+    const std::string name = "tsf_api_truncated_" + std::to_string((long long)std::chrono::steady_clock::now()
+                                                                        .time_since_epoch()
+                                                                        .count());
+    const std::string base = "/tmp/" + name;
+    {
+        std::ofstream(base + ".mhd") << "ObjectType = Image\nNDims = 3\nDimSize = 256 256 160\n"
+                                        "ElementType = MET_FLOAT\nElementDataFile = " << name << ".raw\n";
+        std::vector<float> part((size_t)256 * 256 * 159, 0.5f);   // one plane short of 40 MB
+        FILE *f = std::fopen((base + ".raw").c_str(), "wb");
+        std::fwrite(part.data(), sizeof(float), part.size(), f);
+        std::fclose(f);
+    }
+    paramList p4 = initParameters(PARAMETERS_DIR);
+    EXPECT_THROW(run(base + ".mhd", p4, KERNELS_DIR), SIPL::IOException);
+    std::remove((base + ".mhd").c_str());
+    std::remove((base + ".raw").c_str());
 }
 
 static int run_mode(int argc, char **argv) {

@@ -6,7 +6,6 @@
 #include <cstdio>
 #include <fstream>
 #include <memory>
-#include <thread>
 #include <vector>
 
 #include "first_touch.hpp"
@@ -87,16 +86,11 @@ float *TSFOutput::getTDF() {
         copy_to_host(tmp.get(), d_TDF, sizeof(uint16_t) * (size_t)n);
         const uint16_t *src = tmp.get();
         float *dst = TDF;
-        const unsigned hw = std::thread::hardware_concurrency();
-        const int64_t nt = std::max<int64_t>(1, std::min<int64_t>({hw ? (int64_t)hw : 1, 16, n >> 20}));
-        auto work = [=](int64_t t) {
-            const int64_t i0 = n * t / nt, i1 = n * (t + 1) / nt;
+        const int64_t nt = (int64_t)tsf_host::host_threads(sizeof(float) * (size_t)n);
+        tsf_host::parallel_tasks((size_t)nt, [=](size_t t) {
+            const int64_t i0 = n * (int64_t)t / nt, i1 = n * ((int64_t)t + 1) / nt;
             for (int64_t i = i0; i < i1; i++) dst[i] = (float)src[i] / 65535.0f;
-        };
-        std::vector<std::thread> pool;
-        for (int64_t t = 1; t < nt; t++) pool.emplace_back(work, t);
-        work(0);
-        for (auto &th : pool) th.join();
+        });
     } else {
         tsf_host::parallel_fill(TDF, 0, sizeof(float) * (size_t)n);
         copy_to_host(TDF, d_TDF, sizeof(float) * (size_t)n);

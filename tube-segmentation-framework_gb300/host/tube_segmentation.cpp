@@ -35,12 +35,12 @@
 #include <limits>
 #include <memory>
 #include <sstream>
-#include <thread>
 #include <vector>
 
 #include <fcntl.h>
 #include <unistd.h>
 
+#include "first_touch.hpp"
 #include "tsf/tsf_c.h"
 #include "tsf/tube-segmentation.hpp"
 
@@ -184,10 +184,7 @@ template <typename T> struct Limits {
 // take a NaN, so the result equals the sequential fold over the whole file.
 template <typename T>
 bool read_slices(int fd, char *dst, size_t bytes, bool limits, float &lo, float &hi) {
-    const size_t min_slice = (size_t)4 << 20;
-    unsigned hw = std::thread::hardware_concurrency();
-    size_t nt = std::min<size_t>(hw ? hw : 1, 16);
-    nt = std::max<size_t>(1, std::min(nt, bytes / min_slice));
+    const size_t nt = tsf_host::host_threads(bytes);
     const size_t elems = bytes / sizeof(T), per = (elems + nt - 1) / nt;
     std::vector<Limits<T>> part(nt);
     std::vector<char> ok(nt, 0);
@@ -203,10 +200,7 @@ bool read_slices(int fd, char *dst, size_t bytes, bool limits, float &lo, float 
         if (limits) part[t].fold(reinterpret_cast<const T *>(dst) + e0, e1 - e0);
         ok[t] = 1;
     };
-    std::vector<std::thread> pool;
-    for (size_t t = 1; t < nt; t++) pool.emplace_back(work, t);
-    work(0);
-    for (auto &th : pool) th.join();
+    tsf_host::parallel_tasks(nt, work);
     Limits<T> all;
     for (size_t t = 0; t < nt; t++) {
         if (!ok[t]) return false;
