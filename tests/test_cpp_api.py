@@ -38,11 +38,13 @@ def _write_mhd(path, vol_u8, element="MET_UCHAR"):
     vol_u8.tofile(path + ".raw")
 
 
-def _oracle_run(oracle, vol_u8, iters, spline=False, sixteen_bit=True):
+def _oracle_run(oracle, vol_u8, iters, spline=False, sixteen_bit=True, window=(0.0, 75.0)):
     """run() with the Synthetic-Vascusynth preset, restated with the oracle
     (spline: the large-radius TDF is the spline TDF from max(1.5, radius-min);
-    sixteen_bit False: the 32-bit mode, FP32 fields and a float TDF)."""
-    v = np.clip(vol_u8.astype(np.float32), np.float32(0), np.float32(75)) / np.float32(75)   # toFloat
+    sixteen_bit False: the 32-bit mode, FP32 fields and a float TDF; window:
+    the toFloat limits, the preset's 0 and 75 unless given)."""
+    lo, hi = np.float32(window[0]), np.float32(window[1])
+    v = (np.clip(vol_u8.astype(np.float32), lo, hi) - lo) / (hi - lo)                       # toFloat
     st = "snorm16" if sixteen_bit else "f32"
     f_small = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                          # small-blur 1.0
     Ts, Rs = oracle.tdf_circle(f_small, 0.5, 3.0, 0.5)
@@ -90,6 +92,30 @@ def test_run_32bit_vectors(api_tests, oracle, synth, tmp_path):
     ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
     got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
     assert len(got) > 20 and np.array_equal(got, ref["vertices"])
+
+
+@pytest.mark.gpu
+def test_run_limits_from_the_data(api_tests, oracle, synth, tmp_path):
+    """minimum and maximum off: toFloat takes the volume's own limits
+    (getLimits, tube-segmentation.cpp:1380-1396), which run() folds over
+    several threads' slices of the raw file (a 10 MB MET_FLOAT volume with
+    negative values); the TDF equals the oracle's with numpy's min and max."""
+    pytest.importorskip("torch")
+    vol = synth.vascular_tree((160, 128, 128), seed=13)
+    rng = np.random.default_rng(6)
+    data = (vol * 90.0 - 20.0 + rng.normal(scale=0.5, size=vol.shape)).astype(np.float32)
+    base = str(tmp_path / "vol")
+    _write_mhd(base, data, "MET_FLOAT")
+    iters = 20
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
+            "--centerline-method", "gpu", "--gvf-iterations", str(iters), "--minimum", "off", "--maximum", "off",
+            "--tdf-only"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    T, _, _ = _oracle_run(oracle, data, iters, window=(float(data.min()), float(data.max())))
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(T.shape)
+    assert np.array_equal(tdf, T)
+    assert (tdf > 0).any()
 
 
 @pytest.mark.gpu
