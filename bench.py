@@ -127,16 +127,28 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.first = 0
 
-    def start(self):
+    def start(self, ready_s=3.0):
+        """Starts sampling every 100 ms and returns once the first sample has
+        arrived (at most ready_s), so that the sampler is live when the timed
+        region begins; only samples after mark() count."""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < ready_s:
+                time.sleep(0.01)
+            self.first = len(self.lines)
         except Exception:
             self.proc = None
+
+    def mark(self):
+        """Samples from here on belong to the timed region."""
+        self.first = len(self.lines)
 
     def _read(self):
         for line in self.proc.stdout:
@@ -152,7 +164,7 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[self.first:]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -278,13 +290,13 @@ def run_tsf(args, rank, world):
             torch.distributed.barrier()
 
     # ---- device-resident timed region --------------------------------------------
+    clocks = ClockSampler(dev_index)
+    clocks.start()                        # live before the warm-up; samples counted from mark()
     for _ in range(args.warmup):
         pipe.step()
     torch.cuda.synchronize()
     barrier()
-    clocks = ClockSampler(dev_index)
-    clocks.start()
-    torch.cuda.synchronize()
+    clocks.mark()
     l0 = T.kernel_launches()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
