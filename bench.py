@@ -134,8 +134,11 @@ class ClockSampler:
         arrived (at most ready_s), so that the sampler is live when the timed
         region begins; only samples after mark() count."""
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+            import shutil
+            # into a pipe nvidia-smi's output is block-buffered: ask for lines
+            pre = ["stdbuf", "-oL"] if shutil.which("stdbuf") else []
+            self.proc = subprocess.Popen(pre + ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                                "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
@@ -479,12 +482,37 @@ def run_tsf(args, rank, world):
                                               rank == 0 and world == 1 and not args.no_cpu_baseline)
     res["spline_tdf"] = spline_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
     res["run_api"] = run_api_timing(args, vol)
+    res["seed_sweep"] = seed_sweep(torch, pipe, args, rank)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(args, vol)
     return res
+
+
+def seed_sweep(torch, pipe, args, rank, steps=5):
+    """The step on the vessel-tree volumes of three seeds (this run's seed and
+    the next two; the measurement plan asks for the median over seeds): ms per
+    step and vertices for each, CUDA events over `steps` steps after one
+    warm-up.  Leaves the last volume in the pipeline."""
+    import synthetic
+    n = args.size
+    seeds = [args.seed + rank + i for i in range(3)]
+    ms, verts = [], []
+    for sd in seeds:
+        pipe.vol.copy_(torch.from_numpy(synthetic.vascular_tree((n, n, n), seed=sd)))
+        pipe.step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            pipe.step()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(round(a.elapsed_time(b) / steps, 3))
+        verts.append(int(pipe.last["n_vertices"]))
+    return {"seeds": seeds, "ms_per_step": ms, "median_ms": float(np.median(ms)), "vertices": verts}
 
 
 def fwd_adjoint_timing(torch, pipe, args, storage=None, checkpoint_every=None):
