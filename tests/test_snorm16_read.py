@@ -102,3 +102,21 @@ def test_paired_read_bits():
     c = _f32(0x38000100)
     t = Fraction(-32767, 2 ** 15)
     assert _rn32(t + t * c) == -1
+
+
+def test_offset_form_reads():
+    """snorm16_offset2 / snorm16_offset_lo (csrc/tsf_common.cuh), used by the
+    TDF's x-paired copy: the copy stores max(s, -32767) + 2^15 per half; its
+    low-half read (byte permutation under 384.0f, minus 385, the fma) gives
+    t = max(s, -32767) 2^-15 and then the same value as the clamped read of
+    s, with no clamp left (the fma read of -32767 is exactly -1)."""
+    s = np.arange(-32768, 32768, dtype=np.int64)
+    off = (np.maximum(s, -32767) + 32768).astype(np.uint32)              # the stored offset half
+    x = ((np.maximum(s, -32767) & 0xFFFF) ^ 0x8000).astype(np.uint32)    # vmaxs2, then the xor
+    assert np.array_equal(x, off) and off.min() == 1
+    t = (off | np.uint32(0x43C00000)).view(np.float32) - np.float32(385.0)
+    assert np.array_equal(t.astype(np.float64), np.maximum(s, -32767) * 2.0 ** -15)
+    c = _f32(0x38000100)
+    for si in (-32768, -32767, -32766, -1, 0, 1, 12345, 32767):
+        ti = Fraction(max(si, -32767), 2 ** 15)
+        assert _rn32(ti + ti * c) == max(_rn32(Fraction(si, 32767)), Fraction(-1)), si

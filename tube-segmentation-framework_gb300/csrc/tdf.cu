@@ -12,13 +12,19 @@ int launch_tdf_kernels_closed(const void *d_field4, int X, int Y, int Z, int st,
                               const uint4 *P, int fast_ok);
 
 // The x-paired copy of a 16-bit field4 image: P[i] = (texel i, texel of the
-// next x, clamped at the last column), 16 bytes per voxel.
+// next x, clamped at the last column), 16 bytes per voxel.  OFFSET (snorm16):
+// the texels in the offset form (snorm16_offset2), which the samplers of the
+// copy read with one step less per value.
+template <bool OFFSET>
 __global__ void tdf_pair_kernel(const uint2 *__restrict__ F, uint4 *__restrict__ P, int X, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int x = (int)(i % X);
     const uint2 a = __ldg(F + i), b = __ldg(F + i + (x + 1 < X ? 1 : 0));
-    P[i] = make_uint4(a.x, a.y, b.x, b.y);
+    if (OFFSET)
+        P[i] = make_uint4(snorm16_offset2(a.x), snorm16_offset2(a.y), snorm16_offset2(b.x), snorm16_offset2(b.y));
+    else
+        P[i] = make_uint4(a.x, a.y, b.x, b.y);
 }
 
 size_t tdf_workspace_size(int X, int Y, int Z, int st) {
@@ -67,7 +73,12 @@ int launch_tdf_circle(const void *d_field4, int X, int Y, int Z, int st, float r
                       (reinterpret_cast<uintptr_t>(ws) & 15) == 0 && (reinterpret_cast<uintptr_t>(d_field4) & 7) == 0;
     uint4 *P = pair ? static_cast<uint4 *>(ws) : nullptr;
     if (pair) {
-        tdf_pair_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const uint2 *>(d_field4), P, X, n);
+        if (st == TSF_STORE_SNORM16)
+            tdf_pair_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const uint2 *>(d_field4), P,
+                                                                               X, n);
+        else
+            tdf_pair_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<const uint2 *>(d_field4),
+                                                                                P, X, n);
         TSF_CHECK_LAUNCH("tdf_pair_kernel");
     }
     if (eigen == 1)

@@ -172,13 +172,14 @@ __device__ __forceinline__ float3 sample_linear_in(const void *F, int X, int XY,
     return tri_sum(wt, tt);
 }
 
-// One stored 16-bit field4 texel (8 bytes) to floats, as Vec4Load does
-// (snorm16: x and y read together, snorm16_pair2, the same bits).
+// One field4 texel (8 bytes) of the x-paired copy to floats, the values
+// Vec4Load gives for the stored texel.  snorm16: the copy holds the offset
+// form (snorm16_offset2, written by the pair kernel), x and y read together.
 template <int ST> __device__ __forceinline__ float4 unpack_texel(uint32_t lo, uint32_t hi) {
     using T = typename Store<ST>::T;
     if constexpr (ST == TSF_STORE_SNORM16) {
-        const float2 xy = snorm16_pair2(lo);
-        return make_float4(xy.x, xy.y, snorm16_from_bits(hi), snorm16_from_bits(hi >> 16));
+        const float2 xy = snorm16_offset_pair2(lo);
+        return make_float4(xy.x, xy.y, snorm16_offset_lo(hi), snorm16_offset_lo(hi >> 16));
     } else {
         const uint2 raw = make_uint2(lo, hi);
         T c[4];

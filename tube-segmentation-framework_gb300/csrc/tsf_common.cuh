@@ -155,6 +155,29 @@ __device__ __forceinline__ float2 snorm16_pair2(unsigned w) {
     return fma2(t, make_float2(c, c), t);
 }
 
+// The offset form of a word of two snorm16 values: each half clamped to
+// -32767 and moved to s + 2^15 (1..65535) -- the first step of
+// snorm16_pair2, done once where a copy of the field is written so that the
+// readers of the copy skip it.  Same values on reading: -32768 and -32767
+// both read as -1.
+__device__ __forceinline__ unsigned snorm16_offset2(unsigned w) { return __vmaxs2(w, 0x80018001u) ^ 0x80008000u; }
+
+// Reads of the offset form (snorm16_offset2): the two values of a word, and
+// the low half alone; the same bits as snorm16_pair2 / snorm16_from_bits of
+// the original values (t >= -32767 2^-15, whose fma read is exactly -1, so
+// no clamp is left to do).
+__device__ __forceinline__ float2 snorm16_offset_pair2(unsigned x) {
+    const float2 b = make_float2(__uint_as_float(__byte_perm(x, 0x43C00000u, 0x7610)),
+                                 __uint_as_float(__byte_perm(x, 0x43C00000u, 0x7632)));
+    const float2 t = sub2(b, make_float2(385.0f, 385.0f));
+    const float c = __uint_as_float(0x38000100u);
+    return fma2(t, make_float2(c, c), t);
+}
+__device__ __forceinline__ float snorm16_offset_lo(unsigned x) {
+    const float t = __fsub_rn(__uint_as_float(__byte_perm(x, 0x43C00000u, 0x7610)), 385.0f);
+    return __fmaf_rn(t, __uint_as_float(0x38000100u), t);
+}
+
 // Two snorm16 values of a pair stored as one 32-bit word (low half first).
 __device__ __forceinline__ unsigned snorm16_store2(float2 v) {
     const float2 f = mul2(v, make_float2(32767.0f, 32767.0f));
