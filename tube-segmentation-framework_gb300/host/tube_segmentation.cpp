@@ -247,7 +247,13 @@ HostVolume read_volume(const std::string &filename, paramList &parameters, float
     const size_t bytes = (size_t)v.size.x * v.size.y * v.size.z * v.elem;
     v.data.reset(new char[bytes ? bytes : 1]);
     v.bytes = bytes;
-    const int fd = open(rawName.c_str(), O_RDONLY);
+    struct File {
+        int fd;
+        ~File() {
+            if (fd >= 0) close(fd);
+        }
+    } file{open(rawName.c_str(), O_RDONLY)};
+    const int fd = file.fd;
     if (fd < 0) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
     // getLimits (tube-segmentation.cpp:1380-1396); its result is used only
     // where "minimum" or "maximum" is off
@@ -262,7 +268,6 @@ HostVolume read_volume(const std::string &filename, paramList &parameters, float
     case TSF_TYPE_UINT8: got = read_slices<uint8_t>(fd, v.data.get(), bytes, limits, lo, hi); break;
     default: got = read_slices<float>(fd, v.data.get(), bytes, limits, lo, hi); break;
     }
-    close(fd);
     if (!got) throw SIPL::IOException(rawName.c_str(), __LINE__, __FILE__);
     minimum = pmin != "off" ? (float)std::atof(pmin.c_str()) : lo;
     maximum = pmax != "off" ? (float)std::atof(pmax.c_str()) : hi;
