@@ -30,24 +30,16 @@ namespace tsf {
 
 constexpr int kMaxRadiiBwd = 4096;
 
-// One thread per voxel; a CTA of 128 threads is an 8 x 4 x 4 block, so the
-// gathers and scatters of neighbouring threads stay close.  GIVEN: the
-// forward's response T and arg-max radius R are read instead of re-running the
-// sweep (the forward computed them with the same arithmetic).
+// One voxel's backward pass (the voxel has a gradient: gT != 0 and, GIVEN,
+// a positive response).  GIVEN: the forward's response T and arg-max radius R
+// are read instead of re-running the sweep (the forward computed them with the
+// same arithmetic).
 template <int ST, bool NORM, bool GIVEN>
-__global__ void __launch_bounds__(128) tdf_backward_kernel(const void *__restrict__ F, int X, int Y, int Z,
-                                                           float rmin, float rmax, float rstep, const CircleTable tab,
-                                                           const float *__restrict__ gT, const float *__restrict__ Tin,
-                                                           const float *__restrict__ Rin, float4 *__restrict__ gV) {
-    const int t = threadIdx.x;
-    const int x = blockIdx.x * 8 + (t & 7);
-    const int y = blockIdx.y * 4 + ((t >> 3) & 3);
-    const int z = blockIdx.z * 4 + (t >> 5);
-    if (x >= X || y >= Y || z >= Z) return;
+__device__ __forceinline__ void tdf_backward_voxel(const void *__restrict__ F, int X, int Y, int Z, int x, int y,
+                                                   int z, float g, float rmin, float rmax, float rstep,
+                                                   const CircleTable &tab, const float *__restrict__ Tin,
+                                                   const float *__restrict__ Rin, float4 *__restrict__ gV) {
     const int64_t vi = lin(x, y, z, X, Y);
-    const float g = gT[vi];
-    if (g == 0.0f) return;
-    if (GIVEN && !(Tin[vi] > 0.0f)) return;
     float H[3][3], V[3][3], d[3];
     hessian<ST, NORM>(F, X, Y, Z, x, y, z, H);
     eig3<float>(H, V, d);
@@ -156,6 +148,56 @@ __global__ void __launch_bounds__(128) tdf_backward_kernel(const void *__restric
             o[2] = (o[2] - uz * ug) * iw;
         }
         atomicAdd(&gV[nb[q]], make_float4(o[0], o[1], o[2], 0.0f));
+    }
+}
+
+// A CTA of 128 threads covers a 16 x 8 x 4 region (four 8 x 4 x 4 blocks).
+// Phase 1 lists the region's voxels that have a gradient to pass back, in
+// region order (x fastest); phase 2 hands them to the threads in turn, so
+// every warp works on voxels with a gradient (about half of a volume's voxels
+// have a zero response and nothing to pass back) and consecutive threads on
+// neighbouring voxels, whose gathers and scatters stay close.
+constexpr int kBwdRX = 16, kBwdRY = 8, kBwdRZ = 4, kBwdRounds = kBwdRX * kBwdRY * kBwdRZ / 128;
+
+template <int ST, bool NORM, bool GIVEN>
+__global__ void __launch_bounds__(128) tdf_backward_kernel(const void *__restrict__ F, int X, int Y, int Z,
+                                                           float rmin, float rmax, float rstep, const CircleTable tab,
+                                                           const float *__restrict__ gT, const float *__restrict__ Tin,
+                                                           const float *__restrict__ Rin, float4 *__restrict__ gV) {
+    __shared__ short list[kBwdRounds * 128];
+    __shared__ int wcount[kBwdRounds][4];
+    const int t = threadIdx.x, lane = t & 31, wp = t >> 5;
+    const int bx = blockIdx.x * kBwdRX, by = blockIdx.y * kBwdRY, bz = blockIdx.z * kBwdRZ;
+    unsigned ballot[kBwdRounds];
+#pragma unroll
+    for (int k = 0; k < kBwdRounds; k++) {
+        const int v = k * 128 + t;
+        const int x = bx + (v % kBwdRX), y = by + (v / kBwdRX) % kBwdRY, z = bz + v / (kBwdRX * kBwdRY);
+        bool act = false;
+        if (x < X && y < Y && z < Z) {
+            const int64_t vi = lin(x, y, z, X, Y);
+            act = gT[vi] != 0.0f && (!GIVEN || Tin[vi] > 0.0f);
+        }
+        ballot[k] = __ballot_sync(0xffffffffu, act);
+        if (lane == 0) wcount[k][wp] = __popc(ballot[k]);
+    }
+    __syncthreads();
+    int total = 0, base[kBwdRounds];
+#pragma unroll
+    for (int k = 0; k < kBwdRounds; k++)
+        for (int w2 = 0; w2 < 4; w2++) {
+            if (w2 == wp) base[k] = total;
+            total += wcount[k][w2];
+        }
+#pragma unroll
+    for (int k = 0; k < kBwdRounds; k++)
+        if ((ballot[k] >> lane) & 1u) list[base[k] + __popc(ballot[k] & ((1u << lane) - 1u))] = (short)(k * 128 + t);
+    __syncthreads();
+    for (int e = t; e < total; e += 128) {
+        const int v = list[e];
+        const int x = bx + (v % kBwdRX), y = by + (v / kBwdRX) % kBwdRY, z = bz + v / (kBwdRX * kBwdRY);
+        tdf_backward_voxel<ST, NORM, GIVEN>(F, X, Y, Z, x, y, z, gT[lin(x, y, z, X, Y)], rmin, rmax, rstep, tab, Tin,
+                                            Rin, gV);
     }
 }
 
@@ -288,7 +330,8 @@ int run_tdf_backward(const void *F, int X, int Y, int Z, int st, float rmin, flo
     float4 *acc = (float4 *)ws;
     TSF_TRY_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * (size_t)n, s));
     const CircleTable tab = host_circle_table();
-    const dim3 b(128), g((X + 7) / 8, (Y + 3) / 4, (Z + 3) / 4);
+    const dim3 b(128), g((X + kBwdRX - 1) / kBwdRX, (Y + kBwdRY - 1) / kBwdRY, (Z + kBwdRZ - 1) / kBwdRZ);
+    if (g.y > 65535u || g.z > 65535u) return fail(TSF_ERR_INVALID_ARG, "volume too large for the grid");
     const bool norm = !(rmax < 4.0f);
     if ((Tin == nullptr) != (Rin == nullptr)) return fail(TSF_ERR_INVALID_ARG, "give both T and R, or neither");
     const bool given = Tin != nullptr;
