@@ -72,3 +72,30 @@ def test_argument_validation_without_gpu(tsf):
     assert L.tsf_gvf(None, None, 8, 8, 8, C.c_float(0.1), 5, 7, None, 0, None) == 1
     assert L.tsf_gvf(C.c_void_p(16), C.c_void_p(16), 8, 8, 8, C.c_float(0.1), 5, 0, None, 0, None) == 3
     assert L.tsf_blur_mask(C.c_float(1.0), None, None) == 1
+
+
+def test_centerline_cell_functions_validate_without_gpu(tsf):
+    """The cell path of the centerline stage: argument errors, an empty cell
+    list (nothing to launch), and the replay of an empty graph."""
+    L = tsf.load()
+    i64 = C.c_int64
+    # device side: bad extents, a negative count, null buffers with cells; zero cells launch nothing
+    assert L.tsf_gather_cells(None, 2, 8, 8, None, i64(4), None, None) == 1
+    assert L.tsf_gather_cells(None, 8, 8, 8, None, i64(-1), None, None) == 1
+    assert L.tsf_gather_cells(None, 8, 8, 8, None, i64(4), None, None) == 1
+    assert L.tsf_gather_cells(None, 8, 8, 8, None, i64(0), None, None) == 0
+    assert L.tsf_centerline_apply(None, None, 8, 8, 8, None, None, i64(3), None) == 1
+    assert L.tsf_centerline_apply(C.c_void_p(16), C.c_void_p(16), 8, 8, 8, C.c_void_p(16), None, i64(3), None) == 1
+    assert L.tsf_centerline_apply(None, None, 8, 8, 8, None, None, i64(0), None) == 0
+    # host side: null outputs are argument errors; no edges replay to no cells
+    nv, ne, nc = C.c_int(0), C.c_int(0), i64(0)
+    assert L.tsf_centerline_graph_cells(None, 0, None, 0, None, None, 3, 0, 8, 8, 8, None, None, 0, C.byref(nv),
+                                        C.byref(ne), None, None, i64(0), C.byref(nc)) == 1
+    start = np.zeros(1, np.int64)
+    cells = np.zeros(1, np.int64)
+    vals = np.zeros(1, np.float32)
+    uc, uv = np.zeros(1, np.int64), np.zeros(1, np.float32)
+    nu = i64(-1)
+    assert L.tsf_centerline_smooth_radius(tsf._np_ptr(cells), tsf._np_ptr(start), 0, tsf._np_ptr(vals),
+                                          tsf._np_ptr(uc), tsf._np_ptr(uv), C.byref(nu)) == 0
+    assert nu.value == 0
