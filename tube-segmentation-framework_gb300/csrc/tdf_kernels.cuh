@@ -87,8 +87,10 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 // shared memory, then treats each voxel's sweep as a task: a lane evaluates
 // one radius (its 32 samples, in order) per round and, when its voxel's sweep
 // ends, takes the next unstarted voxel, in lane order.  Lanes stay busy until
-// the queue drains, and each voxel's arithmetic is exactly that of
-// tdf_circle_kernel.
+// the queue drains; after that, once few sweeps are left (tdf_tail), the warp
+// runs them one voxel at a time with lane j computing sample j and every lane
+// summing the 32 staged samples in sample order.  Each voxel's arithmetic is
+// exactly that of tdf_circle_kernel.
 //
 // Locality: a warp's voxels form an 8 x 4 x 4 block and a CTA's four warps an
 // 8 x 8 x 8 brick, so the circles sampled by a CTA stay within a
@@ -97,6 +99,10 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 // trilinear corners).
 constexpr int kSeg = 128;
 constexpr int kTdfWarps = 4;
+// Sweeps left when the load-balanced kernel switches to one sample per lane:
+// measured best at 24 for the large-radius pass (normalised Hessian, radii to
+// 7: 8.21 -> 7.93 ms at 256^3 f16) and 8 for the small-radius one (6.37 -> 6.24).
+template <bool NORM> constexpr int tdf_tail() { return NORM ? 24 : 8; }
 
 // PAIR: interior samples read the x-paired copy P of a 16-bit field (one
 // 16-byte load per corner row, sample_linear_pair_in) instead of F.
@@ -109,6 +115,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps, 6) tdf_queue_kernel(const void
     static_assert(kTdfWarps == 4 && kSeg == 128, "a CTA is an 8x8x8 brick of four 8x4x4 warp blocks");
     __shared__ float se[kTdfWarps][6][kSeg];
     __shared__ unsigned char room[kTdfWarps][kSeg];      // sample_room: unclamped sampler while the margin fits
+    __shared__ float stage[kTdfWarps][32];               // the tail's samples of one voxel-radius
     const int XY = X * Y;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     // brick of this CTA, block of this warp: task t -> (t & 7, (t >> 3) & 3, t >> 5)
@@ -140,6 +147,66 @@ __global__ void __launch_bounds__(32 * kTdfWarps, 6) tdf_queue_kernel(const void
     float radius = rmin, maxSum = 0.0f, maxRadius = 0.0f;
     int nr = 0;
     while (__any_sync(full, task >= 0)) {
+        if (next >= ntask) {
+            // The queue is empty: once few sweeps are left, the warp finishes
+            // them one voxel at a time, lane j computing sample j of each
+            // radius (the same samples; the owner's sum in sample order), so
+            // that the lanes whose sweeps ended do not idle while the longest
+            // ones run.
+            unsigned act = __ballot_sync(full, task >= 0 && inside(task));
+            if (__popc(act) <= tdf_tail<NORM>()) {
+                while (act) {
+                    const int o = __ffs(act) - 1;
+                    act &= act - 1u;
+                    const int t = __shfl_sync(full, task, o);
+                    float r = __shfl_sync(full, radius, o), ms = __shfl_sync(full, maxSum, o);
+                    float mr = __shfl_sync(full, maxRadius, o);
+                    int n = __shfl_sync(full, nr, o);
+                    const float e2x = se[w][0][t], e2y = se[w][1][t], e2z = se[w][2][t];
+                    const float e3x = se[w][3][t], e3y = se[w][4][t], e3z = se[w][5][t];
+                    const float fx = (float)tx(t), fy = (float)ty(t), fz = (float)tz(t);
+                    const int rm = room[w][t];
+                    while (r <= rmax && n < kMaxRadii) {
+                        float term = 0.0f;
+                        if (lane < tab.n) {
+                            const float3 va = circle_dir(tab.c[lane], tab.s[lane], e2x, e2y, e2z, e3x, e3y, e3z);
+                            const float3 u = circle_point(fx, fy, fz, r, va);
+                            float3 smp;
+                            if (sample_margin(r) <= rm) {
+                                if constexpr (PAIR)
+                                    smp = sample_linear_pair_in<ST>(P, X, XY, u.x, u.y, u.z);
+                                else
+                                    smp = sample_linear_in<ST>(F, X, XY, u.x, u.y, u.z);
+                            } else {
+                                if constexpr (PAIR)
+                                    smp = sample_linear_pair_clamped<ST>(P, X, Y, Z, u.x, u.y, u.z);
+                                else
+                                    smp = sample_linear<ST>(F, X, Y, Z, u.x, u.y, u.z);
+                            }
+                            term = radial_term(smp, va);
+                        }
+                        stage[w][lane] = term;
+                        __syncwarp();
+                        float rs = 0.0f;
+                        for (int j = 0; j < tab.n; j++) rs = rs + stage[w][j];
+                        __syncwarp();
+                        rs = rs / (float)tab.n;
+                        if (!(rs > ms)) break;
+                        ms = rs;
+                        mr = r;
+                        r = r + rstep;
+                        n++;
+                    }
+                    if (lane == 0) {
+                        const int64_t i = lin(tx(t), ty(t), tz(t), X, Y);
+                        if (UNORM) reinterpret_cast<uint16_t *>(T)[i] = to_unorm16(ms);
+                        else reinterpret_cast<float *>(T)[i] = ms;
+                        Rout[i] = mr;
+                    }
+                }
+                return;
+            }
+        }
         bool done = true;
         if (task >= 0 && inside(task)) {
             const float e2x = se[w][0][task], e2y = se[w][1][task], e2z = se[w][2][task];
