@@ -99,10 +99,14 @@ __global__ void __launch_bounds__(256) tdf_circle_kernel(const void *__restrict_
 // trilinear corners).
 constexpr int kSeg = 128;
 constexpr int kTdfWarps = 4;
-// Sweeps left when the load-balanced kernel switches to one sample per lane:
-// measured best at 24 for the large-radius pass (normalised Hessian, radii to
-// 7: 8.21 -> 7.93 ms at 256^3 f16) and 8 for the small-radius one (6.37 -> 6.24).
-template <bool NORM> constexpr int tdf_tail() { return NORM ? 24 : 8; }
+// Sweeps left when the load-balanced kernel switches to one sample per lane,
+// as measured at 256^3: 16-bit fields 24 for the large-radius pass
+// (normalised Hessian, radii to 7: 8.21 -> 7.93 ms) and 8 for the small-radius
+// one (6.37 -> 6.24 ms); FP32 fields 8 for the small pass (9.64 -> 9.47 ms) and
+// none for the large one, where the switch cost time (13.57 -> 14.10 ms).
+template <int ST, bool NORM> constexpr int tdf_tail() {
+    return NORM ? (ST == TSF_STORE_F32 ? 0 : 24) : 8;
+}
 
 // PAIR: interior samples read the x-paired copy P of a 16-bit field (one
 // 16-byte load per corner row, sample_linear_pair_in) instead of F.
@@ -154,7 +158,7 @@ __global__ void __launch_bounds__(32 * kTdfWarps, 6) tdf_queue_kernel(const void
             // that the lanes whose sweeps ended do not idle while the longest
             // ones run.
             unsigned act = __ballot_sync(full, task >= 0 && inside(task));
-            if (__popc(act) <= tdf_tail<NORM>()) {
+            if (__popc(act) <= tdf_tail<ST, NORM>()) {
                 while (act) {
                     const int o = __ffs(act) - 1;
                     act &= act - 1u;
