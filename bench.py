@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--polish", action="store_true",
                     help="16-bit GVF with its last --polish-iters iterations in FP32: vertex list against the FP64 "
                          "oracle and step time against the FP16 and FP32 paths")
-    ap.add_argument("--polish-iters", type=int, default=20)
+    ap.add_argument("--polish-iters", type=int, default=4)
     ap.add_argument("--fmg", action="store_true",
                     help="instead of the default workload: the 512x512x400 lung CT with multigrid GVF")
     ap.add_argument("--fmg-cycles", type=int, default=10)
