@@ -38,14 +38,15 @@ def _write_mhd(path, vol_u8, element="MET_UCHAR"):
     vol_u8.tofile(path + ".raw")
 
 
-def _oracle_run(oracle, vol_u8, iters, spline=False, sixteen_bit=True, window=(0.0, 75.0)):
+def _oracle_run(oracle, vol_u8, iters, spline=False, sixteen_bit=True, window=(0.0, 75.0), storage=None):
     """run() with the Synthetic-Vascusynth preset, restated with the oracle
     (spline: the large-radius TDF is the spline TDF from max(1.5, radius-min);
     sixteen_bit False: the 32-bit mode, FP32 fields and a float TDF; window:
-    the toFloat limits, the preset's 0 and 75 unless given)."""
+    the toFloat limits, the preset's 0 and 75 unless given; storage: the
+    fields' format when gvf-storage names one)."""
     lo, hi = np.float32(window[0]), np.float32(window[1])
     v = (np.clip(vol_u8.astype(np.float32), lo, hi) - lo) / (hi - lo)                       # toFloat
-    st = "snorm16" if sixteen_bit else "f32"
+    st = storage or ("snorm16" if sixteen_bit else "f32")
     f_small = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                          # small-blur 1.0
     Ts, Rs = oracle.tdf_circle(f_small, 0.5, 3.0, 0.5)
     f4 = oracle.vector_field(oracle.blur(v, 1.0), 0.1, 1, st)                               # large-blur 1.0
@@ -87,6 +88,30 @@ def test_run_32bit_vectors(api_tests, oracle, synth, tmp_path):
     out = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     T, R, field = _oracle_run(oracle, vol_u8, iters, sixteen_bit=False)
+    tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(T.shape)
+    assert np.array_equal(tdf, T)
+    ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
+    got = np.loadtxt(tmp_path / "vertices.txt", dtype=np.int32).reshape(-1, 3)
+    assert len(got) > 20 and np.array_equal(got, ref["vertices"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_run_gvf_storage(api_tests, oracle, synth, tmp_path, storage):
+    """The gvf-storage parameter (no counterpart in the reference): run() with
+    the fields stored in FP16 or BF16 and the 16-bit mode's unorm16 TDF gives
+    the oracle's TDF and vertices for that storage."""
+    pytest.importorskip("torch")
+    vol_u8 = np.round(synth.vascular_tree((44, 52, 60), seed=11) * 90.0).astype(np.uint8)
+    base = str(tmp_path / "vol")
+    _write_mhd(base, vol_u8)
+    iters = 21
+    args = [api_tests, "run", base + ".mhd", str(tmp_path), "--parameters", "Synthetic-Vascusynth",
+            "--centerline-method", "gpu", "--gvf-iterations", str(iters), "--gvf-storage", storage,
+            "--no-segmentation", "true"]
+    out = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    T, R, field = _oracle_run(oracle, vol_u8, iters, storage=storage)
     tdf = np.fromfile(tmp_path / "tdf.raw", np.float32).reshape(T.shape)
     assert np.array_equal(tdf, T)
     ref = oracle.centerpoints(T, R, field, tdf_high=0.35, cube_size=3)
