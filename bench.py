@@ -484,12 +484,35 @@ def run_tsf(args, rank, world):
     res["spline_tdf"] = spline_timing(torch, T, pipe, rank == 0 and world == 1 and not args.no_cpu_baseline)
     res["run_api"] = run_api_timing(args, vol)
     res["seed_sweep"] = seed_sweep(torch, pipe, args, rank)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.storage in ("f16", "bf16"):
+        res["exact_centerline_16bit"] = exact_centerline_timing(args)
     traffic = _traffic_from_profile(args.storage)
     if traffic:
         res["roofline"]["traffic"] = traffic
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(args, vol)
     return res
+
+
+def exact_centerline_timing(args):
+    """The 16-bit step that reproduces the FP64 run's vertex list (GVF in the
+    16-bit format for K - 4 iterations and 4 in snorm16, the field in snorm16
+    for the finish and the large-radius pass, the small-radius pass on the FP32
+    field) beside the FP32 step; the vertex list is compared with the FP64
+    oracle run of the same method on the host (bench.py --polish for more
+    variants)."""
+    import types
+    a = types.SimpleNamespace(**vars(args))
+    a.polish_iters = 4
+    st, k = args.storage, a.polish_iters
+    name = "%s+%d_snorm16_polish_f32_small" % (st, k)
+    r = run_polish(a, only=("f32", name))
+    v = r[name]
+    return {"variant": "%d iterations in %s, the last %d in snorm16; snorm16 field for the finish and the "
+                       "large-radius pass; FP32 small-radius field" % (args.iters - k, st, k),
+            "ms": v["ms"], "f32_path_ms": r["f32"]["ms"], "speedup_vs_f32_path": round(r["f32"]["ms"] / v["ms"], 3),
+            "same_vertex_list_as_fp64": v["same_vertex_list"], "vertices": v["vertices"],
+            "fp64_vertices": r["fp64_vertices"], "oracle_s": r["oracle_s"]}
 
 
 def seed_sweep(torch, pipe, args, rank, steps=5):
@@ -1254,7 +1277,7 @@ def run_accuracy(args):
     return out
 
 
-def run_polish(args):
+def run_polish(args, only=None):
     """The 16-bit path that reproduces the FP64 centerline: GVF in --storage
     for K - k iterations, then k in FP32 (the iterate converted, f0 in FP32),
     the finished field in FP32 and the small-radius pass on the FP32 field of
@@ -1314,6 +1337,8 @@ def run_polish(args):
                 "%s+%d_f32_polish_%s_large_f32_small" % (st, k, st): (st, k, st, "f32"),
                 # the last k iterations in snorm16 instead of FP32, the field left in snorm16
                 "%s+%d_snorm16_polish_f32_small" % (st, k): (st, k, "snorm16", "f32", "snorm16")}
+    if only is not None:
+        variants = {name: a for name, a in variants.items() if name in only}
     s64 = set(map(tuple, V64.tolist()))
     out = {"size": n, "iterations": K, "mu": args.mu, "fp64_vertices": int(len(V64)), "oracle_s": round(t_oracle, 1),
            "note": "step = blur, vector fields, GVF, finish, both TDF passes, combine, candidates; CUDA events, "
